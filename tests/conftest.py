@@ -1,0 +1,19 @@
+import json
+import os
+import sys
+
+import pytest
+
+ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+if ROOT not in sys.path:
+    sys.path.insert(0, ROOT)
+
+
+def pytest_configure(config):
+    config.addinivalue_line("markers", "gpu: needs a CUDA GPU (sm_103a) and the built extension")
+
+
+@pytest.fixture(scope="session")
+def reference_cases():
+    with open(os.path.join(ROOT, "tests", "golden", "reference_cases.json")) as fh:
+        return json.load(fh)
