@@ -1,0 +1,235 @@
+/*
+ * medyan_mech.h — C ABI of the GB300 mechanical-equilibration engine.
+ *
+ * Drop-in for the path MEDYAN's MController drives before handing control
+ * back to the chemistry: the ForceFieldManager / ForceField plugin set, the
+ * CGMethod Polak-Ribiere minimizer with backtracking line search, and the
+ * neighbor lists those force fields read.  Paths below are relative to
+ * medyan-5.4.0/src of the reference.
+ *
+ * Conventions
+ *   - every function returns MECH_OK (0) or a MECH_ERR_* code; nothing throws
+ *     across the ABI;
+ *   - host arrays are copied in; the library keeps no caller pointer;
+ *   - coordinates and forces use the reference's DOF layout: one double per
+ *     component, bead after bead (x0 y0 z0 x1 ...), in the caller's bead
+ *     order (Structure/DofSerializer.hpp:64-187);
+ *   - one context binds one CUDA device and one stream; calls on a context
+ *     are not thread-safe, contexts are independent.
+ */
+#ifndef MEDYAN_MECH_H
+#define MEDYAN_MECH_H
+
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define MECH_ABI_VERSION 1
+
+/* Status codes. */
+#define MECH_OK                  0
+#define MECH_ERR_ARG            -1   /* bad argument or size */
+#define MECH_ERR_TOPOLOGY       -2   /* filament cylinders do not chain bead to bead */
+#define MECH_ERR_CUDA           -3   /* a CUDA call failed; see mech_last_error */
+#define MECH_ERR_NONFINITE      -4   /* max |F| not finite (CGMethod.hpp:202-212 throws here) */
+#define MECH_ERR_LINESEARCH     -5   /* line search failed with recovery disabled (MinimizationResult::errorLineSearch) */
+#define MECH_ERR_ITER_LIMIT     -6   /* device loop gave up after its own iteration cap */
+#define MECH_ERR_CAPACITY       -7   /* a device list outgrew its capacity */
+#define MECH_ERR_NO_DEVICE      -8   /* no CUDA device visible */
+#define MECH_ERR_STATE          -9   /* call made in the wrong order (e.g. no network) */
+
+/* Precision of the force/geometry arithmetic. */
+#define MECH_PREC_FP64   0   /* everything in FP64 */
+#define MECH_PREC_MIXED  1   /* FP32 forces and pair geometry; FP64 energy sums, dots, beta, Armijo */
+
+/* Force fields, in MController's order (Controller/MController.cpp:65-196). */
+#define MECH_FF_STRETCHING  0   /* FilamentStretching<Harmonic>   */
+#define MECH_FF_BENDING     1   /* FilamentBending<Cosine>        */
+#define MECH_FF_LINKER      2   /* LinkerStretching<Harmonic>     */
+#define MECH_FF_MOTOR       3   /* MotorGhostStretching<Harmonic> */
+#define MECH_FF_EXVOL       4   /* CylinderExclVolume<CylinderExclVolRepulsion> */
+#define MECH_FF_BOUNDARY    5   /* BoundaryCylinderRepulsion<Exp> */
+#define MECH_NUM_FF         6
+
+/*
+ * One network: what serializeDof + the force fields' vectorize() consume.
+ * Cylinders are listed filament by filament, minus end first; cylinder i of a
+ * filament shares its second bead with cylinder i+1's first bead.
+ */
+typedef struct MechNetwork {
+    int32_t n_beads;
+    const double* coord;            /* [3*n_beads] */
+
+    int32_t n_filaments;
+    const int32_t* fil_cyl_start;   /* [n_filaments+1] cylinder ranges */
+
+    int32_t n_cylinders;
+    const int32_t* cyl_bead;        /* [2*n_cylinders] first, second bead */
+    const int64_t* cyl_id;          /* unique cylinder IDs: half list keeps id_c > id_n */
+    const int32_t* cyl_filament_id; /* filament ID (same-filament exclusion) */
+    const int32_t* cyl_position;    /* position on filament */
+    const int32_t* cyl_type;        /* filament type */
+    const double* cyl_eq_length;    /* l0 (MCylinder::getEqLength) */
+    const double* cyl_k_stretch;    /* MCylinder::getStretchingConst */
+    const double* cyl_k_bend;       /* MCylinder::getBendingConst */
+    const double* cyl_eq_theta;     /* MCylinder::getEqTheta */
+    const double* cyl_k_exvol;      /* MCylinder::getExVolConst */
+
+    int32_t n_linkers;
+    const int32_t* lk_cyl;          /* [2*n] first, second cylinder */
+    const double* lk_pos;           /* [2*n] relative positions on each cylinder */
+    const double* lk_k;
+    const double* lk_eq_length;
+
+    int32_t n_motors;
+    const int32_t* mt_cyl;
+    const double* mt_pos;
+    const double* mt_k;
+    const double* mt_eq_length;
+
+    int32_t n_planes;               /* plane boundary elements */
+    const double* planes;           /* [4*n_planes] a, b, c, d of a x + b y + c z + d = 0 */
+    const double* plane_k;          /* repulsion constant */
+    const double* plane_screen;     /* screening length */
+
+    double box[3];                  /* extent of the bin grid (SysParams NX*compartmentSizeX, ...) */
+    double exvol_cutoff;            /* VolumeCutoff (rMax of the cylinder pair list; rMin = 0) */
+    double boundary_cutoff;         /* BoundaryCutoff */
+} MechNetwork;
+
+/* Mirrors ConjugateGradientParams (Mechanics/Minimizer/CGMethod.hpp:44-63). */
+typedef struct MechCGParams {
+    int32_t method;                 /* 0 steepest, 1 Fletcher-Reeves, 2 Polak-Ribiere */
+    double max_dist;
+    double lambda_max;
+    double grad_tol;
+    double energy_rel_tol;
+    int32_t energy_call_limit;      /* 0: none */
+    int32_t force_call_limit;       /* effective limit is max(this, 3 * beads) */
+    int32_t report_on_call_limit;
+    int32_t try_to_recover;
+} MechCGParams;
+
+/* Mirrors MinimizationResult (Mechanics/Minimizer/MinimizationTypes.hpp:10-66)
+ * and the two EnergyReports, plus device-side counters. */
+typedef struct MechResult {
+    uint32_t error_flags;           /* bit 0: line search error */
+    int32_t status;                 /* MECH_OK or MECH_ERR_* */
+    int32_t num_energy_call;        /* counted as the reference counts them */
+    int32_t energy_call_limit;
+    int32_t num_force_call;
+    int32_t force_call_limit;
+    int32_t num_iter;
+    int32_t num_safe_mode;
+    int32_t num_recover;
+    int32_t num_line_search_trials;
+    int32_t num_energy_eval;        /* energy evaluations actually run */
+    int32_t used_backup;
+    double grad_inf_norm;
+    double grad_tol;
+    double energy_rel_change;
+    double energy_rel_tol;
+    double energies_before[MECH_NUM_FF + 1];   /* per force field, then total */
+    double energies_after[MECH_NUM_FF + 1];
+    double seconds;                 /* wall time of the minimization on the host clock */
+} MechResult;
+
+/* Counts of the lists built by the last neighbor-list rebuild. */
+typedef struct MechListInfo {
+    int64_t n_exvol_pairs;          /* cylinder-cylinder half list */
+    int64_t n_boundary_beads;       /* boundary interactions (beads) */
+    int64_t n_boundary_cyl;         /* boundary-cylinder neighbor entries */
+    double cell_size;               /* bin edge used by the rebuild */
+    int64_t n_cells;
+} MechListInfo;
+
+typedef struct MechContext MechContext;
+
+/* Version and error text. */
+int32_t mech_abi_version(void);
+const char* mech_last_error(void);
+
+/*
+ * Context with `n_replicas` independent networks, minimized together.
+ * Replaces ForceFieldManager construction + MController::initialize
+ * (Controller/MController.h:97-104); one replica is the plain MEDYAN case.
+ */
+int32_t mech_ctx_create(int32_t precision, int32_t device, MechContext** out);
+int32_t mech_ctx_destroy(MechContext* ctx);
+
+/*
+ * Load networks: serializeDof + ForceFieldManager::vectorizeAllForceFields
+ * (Structure/DofSerializer.hpp:64-187, Mechanics/ForceField/ForceFieldManager.cpp:35-93).
+ * Rebuilds the neighbor lists at the given coordinates.
+ */
+int32_t mech_set_networks(MechContext* ctx, int32_t n_replicas, const MechNetwork* nets);
+
+/* Replace the coordinates of replica r (caller bead order); lists are kept. */
+int32_t mech_set_coords(MechContext* ctx, int32_t replica, const double* coord);
+int32_t mech_get_coords(MechContext* ctx, int32_t replica, double* coord);
+
+/*
+ * SubSystem::resetNeighborLists for the hot path (Structure/SubSystem.cpp:193-206):
+ * HybridCylinderCylinderNL (HybridNeighborListImpl.cpp:527-556) and
+ * BoundaryCylinderNL (NeighborListImpl.cpp:801-809), at the current coordinates.
+ * cell_size <= 0 lets the library choose the bin edge (any edge >= rMax gives
+ * the same list).
+ */
+int32_t mech_rebuild_neighbors(MechContext* ctx, double cell_size, MechListInfo* info);
+
+/*
+ * The sorted cylinder pair list of replica r as (c, n) cylinder indices,
+ * id_c > id_n, ordered by c then n.  Writes min(cap, count) pairs; *count
+ * receives the total.
+ */
+int32_t mech_get_pairs(MechContext* ctx, int32_t replica, int32_t* pairs, int64_t cap, int64_t* count);
+
+/*
+ * ForceFieldManager::computeIndividualEnergies and ::computeEnergy
+ * (ForceFieldManager.cpp:96-227) at `coord` (NULL: current coordinates).
+ * per_ff receives MECH_NUM_FF energies; *total the plain sum and *energy the
+ * computeEnergy value (+inf when a force field reports failure).
+ */
+int32_t mech_energy(MechContext* ctx, int32_t replica, const double* coord, double* per_ff, double* total,
+                    double* energy);
+
+/* ForceFieldManager::computeForces (ForceFieldManager.cpp:242-290): f_out is
+ * overwritten with the total force at `coord` (NULL: current coordinates). */
+int32_t mech_forces(MechContext* ctx, int32_t replica, const double* coord, double* f_out);
+
+/*
+ * CGMethod::minimize (CGMethod.hpp:826-1743) with MController's recovery move
+ * (MController.h:273-339), on every replica at once, starting from the current
+ * coordinates.  results[r] is filled per replica; the final coordinates stay in
+ * the context (mech_get_coords) and the final forces can be read with
+ * mech_get_forces.
+ */
+int32_t mech_minimize(MechContext* ctx, const MechCGParams* params, MechResult* results);
+int32_t mech_get_forces(MechContext* ctx, int32_t replica, double* f_out);
+
+/*
+ * Per-linker stretch forces of the last force evaluation
+ * (LinkerStretching::assignforcemags, LinkerStretching.cpp:117-123; motors alike).
+ */
+int32_t mech_get_stretch_forces(MechContext* ctx, int32_t replica, double* linker_f, double* motor_f);
+
+/* Device time of the kernels of the last mech_minimize, by kernel family
+ * (milliseconds, CUDA events), and the number of kernel launches. */
+typedef struct MechTiming {
+    double ms_total;
+    double ms_line_search;
+    double ms_force;
+    double ms_direction;
+    double ms_rebuild;
+    int64_t launches;
+    int64_t graph_launches;
+} MechTiming;
+int32_t mech_get_timing(MechContext* ctx, MechTiming* t);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* MEDYAN_MECH_H */

@@ -1,0 +1,463 @@
+// Cylinder-cylinder excluded volume: the analytic double integral of 1/r^4
+// over two segments (CylinderExclVolRepulsion.cpp:330-882, paths relative to
+// medyan-5.4.0/src), with the reference's composite-Simpson fallbacks
+// (:884-1254) for pairs whose analytic value is not usable.
+//
+// This file is compiled once per precision (MECH_EXVOL_REAL = double or
+// float).  The FP64 object is built without FMA contraction: the formula is
+// ill-conditioned for nearly coplanar pairs, and rounding each operation as
+// written keeps the GPU within a few ulps of the CPU restatement there.  In
+// mixed precision the pair geometry is single precision; pairs whose
+// coplanarity measure |n . v3| falls under kMixedFp64Coplanar are evaluated in
+// FP64, because the 1/JJ * (sum) form loses about 1/|n.v3|^2 of its relative
+// accuracy, and the reference's own coplanar move (|n . v3| < 0.1) is then
+// always decided in FP64.
+#include <cuda_runtime.h>
+
+#include "mech_device.cuh"
+
+#ifndef MECH_EXVOL_REAL
+#define MECH_EXVOL_REAL double
+#endif
+
+namespace mech {
+
+constexpr float kMixedFp64Coplanar = 0.3f;
+constexpr int kFbNodesEnergy = 400;       // Simpson intervals, energy (:929-930)
+constexpr int kFbNodesForce = 10000;      // Simpson intervals, forces (:1041-1042)
+
+template <typename T>
+struct PairInv {
+    T a, b, c, d, e, F, g, h, I, D2, E2;
+    T AA, BB, CC, DD, EE, FF, GG, HH, JJ;
+    T ATG1, ATG2, ATG3, ATG4;
+};
+
+template <typename T>
+__device__ __forceinline__ T dot3(const T* u, const T* v) {
+    return u[0] * v[0] + u[1] * v[1] + u[2] * v[2];
+}
+
+// Scalar products and the AA..JJ terms (:355-420).  Differences of positions
+// are taken in double, then rounded to T.
+template <typename T>
+__device__ __forceinline__ void pair_inv(const double* c1, const double* c2, const double* c3, const double* c4,
+                                         PairInv<T>& p) {
+    T v12[3], v34[3], v31[3], v14[3], v32[3];
+#pragma unroll
+    for (int k = 0; k < 3; ++k) {
+        v12[k] = (T)(c2[k] - c1[k]);
+        v34[k] = (T)(c4[k] - c3[k]);
+        v31[k] = (T)(c1[k] - c3[k]);
+        v14[k] = (T)(c4[k] - c1[k]);
+        v32[k] = (T)(c2[k] - c3[k]);
+    }
+    p.a = dot3(v12, v12);
+    p.b = dot3(v34, v34);
+    p.c = dot3(v31, v31);
+    p.d = dot3(v12, v34);
+    p.e = dot3(v12, v31);
+    p.F = dot3(v34, v31);
+    p.g = dot3(v12, v14);
+    p.h = dot3(v34, v32);
+    p.I = dot3(v34, v14);
+    p.D2 = dot3(v14, v14);
+    p.E2 = dot3(v32, v32);
+    const T ac = sqrt(p.a * p.c), bc = sqrt(p.b * p.c), aD = sqrt(p.a * p.D2), bE = sqrt(p.b * p.E2);
+    p.AA = sqrt(fmax((T)0, (ac + p.e) * (ac - p.e)));
+    p.BB = sqrt(fmax((T)0, (bc + p.F) * (bc - p.F)));
+    p.CC = p.d * p.e - p.a * p.F;
+    p.DD = p.b * p.e - p.d * p.F;
+    p.EE = sqrt(fmax((T)0, (aD + p.g) * (aD - p.g)));
+    p.FF = sqrt(fmax((T)0, (bE + p.h) * (bE - p.h)));
+    p.GG = p.d * p.g - p.a * p.I;
+    p.HH = p.CC + p.GG - p.DD;
+    // (c1 - c2) x (c3 - c4) . (c3 - c1) = (v12 x v34) . v31 up to sign; squared
+    const T cx = v12[1] * v34[2] - v12[2] * v34[1];
+    const T cy = v12[2] * v34[0] - v12[0] * v34[2];
+    const T cz = v12[0] * v34[1] - v12[1] * v34[0];
+    const T trip = cx * v31[0] + cy * v31[1] + cz * v31[2];
+    p.JJ = -trip * trip;
+    p.ATG1 = atan((p.a + p.e) / p.AA) - atan(p.e / p.AA);
+    p.ATG2 = atan((p.a + p.e - p.d) / p.EE) - atan((p.e - p.d) / p.EE);
+    p.ATG3 = atan((p.F) / p.BB) - atan((p.F - p.b) / p.BB);
+    p.ATG4 = atan((p.d + p.F) / p.FF) - atan((p.d + p.F - p.b) / p.FF);
+}
+
+template <typename T>
+__device__ __forceinline__ bool bad_value(T x) { return !(fabs(x) < (T)(1.0 / 0.0)); }
+
+// Analytic pair energy (:427-436); returns NaN when unusable (inf, NaN or < -1).
+template <typename T>
+__device__ double pair_energy(const double* c1, const double* c2, const double* c3, const double* c4, T kRepScaled) {
+    PairInv<T> p;
+    pair_inv<T>(c1, c2, c3, c4, p);
+    const T U = (T)0.5 * kRepScaled / p.JJ *
+                (p.CC / p.AA * p.ATG1 + p.GG / p.EE * p.ATG2 + p.DD / p.BB * p.ATG3 + p.HH / p.FF * p.ATG4);
+    if (bad_value(U) || U < (T)-1) return __longlong_as_double(0x7ff8000000000000ULL);
+    return (double)U;
+}
+
+// |n_hat . v3_hat| of areInPlane (MathFunctions.h:1101-1134), n = (c2-c1) x (c3-c1), v3 = c4 - c1.
+template <typename T>
+__device__ __forceinline__ T coplanarity(const double* c1, const double* c2, const double* c3, const double* c4) {
+    T v1[3], v2[3], v3[3];
+#pragma unroll
+    for (int k = 0; k < 3; ++k) {
+        v1[k] = (T)(c2[k] - c1[k]);
+        v2[k] = (T)(c3[k] - c1[k]);
+        v3[k] = (T)(c4[k] - c1[k]);
+    }
+    T n[3] = {v1[1] * v2[2] - v1[2] * v2[1], v1[2] * v2[0] - v1[0] * v2[2], v1[0] * v2[1] - v1[1] * v2[0]};
+    const T nn = sqrt(n[0] * n[0] + n[1] * n[1] + n[2] * n[2]);
+    n[0] = n[0] / nn; n[1] = n[1] / nn; n[2] = n[2] / nn;
+    const T vv = sqrt(v3[0] * v3[0] + v3[1] * v3[1] + v3[2] * v3[2]);
+    v3[0] = v3[0] / vv; v3[1] = v3[1] / vv; v3[2] = v3[2] / vv;
+    return fabs(n[0] * v3[0] + n[1] * v3[1] + n[2] * v3[2] - (T)0);
+}
+
+// c2 moved 0.01 nm along the unit normal of (c1, c2, c3) (MathFunctions.h:1221-1273)
+__device__ __forceinline__ void push_c2(const double* c1, const double* c2, const double* c3, double* out) {
+    double v1[3], v2[3];
+    for (int k = 0; k < 3; ++k) { v1[k] = c2[k] - c1[k]; v2[k] = c3[k] - c1[k]; }
+    double n[3] = {v1[1] * v2[2] - v1[2] * v2[1], v1[2] * v2[0] - v1[0] * v2[2], v1[0] * v2[1] - v1[1] * v2[0]};
+    const double nn = sqrt(n[0] * n[0] + n[1] * n[1] + n[2] * n[2]);
+    for (int k = 0; k < 3; ++k) out[k] = (c2[k] + (n[k] / nn) * 0.01);
+}
+__device__ __forceinline__ void push_c1(const double* c1, const double* c2, const double* c3, double* out) {
+    double v1[3], v2[3];
+    for (int k = 0; k < 3; ++k) { v1[k] = c2[k] - c1[k]; v2[k] = c3[k] - c1[k]; }
+    double n[3] = {v1[1] * v2[2] - v1[2] * v2[1], v1[2] * v2[0] - v1[0] * v2[2], v1[0] * v2[1] - v1[1] * v2[0]};
+    const double nn = sqrt(n[0] * n[0] + n[1] * n[1] + n[2] * n[2]);
+    for (int k = 0; k < 3; ++k) out[k] = (c1[k] + (n[k] / nn) * 0.01);
+}
+
+// Analytic forces (:597-860) on the given (possibly moved) beads; returns
+// false when a component is not finite.
+template <typename T>
+__device__ bool pair_forces(const double* c1, const double* c2, const double* c3, const double* c4, T kRepScaled,
+                            T out[4][3]) {
+    PairInv<T> p;
+    pair_inv<T>(c1, c2, c3, c4, p);
+    const T a = p.a, b = p.b, c = p.c, d = p.d, e = p.e, F = p.F;
+    const T AA = p.AA, BB = p.BB, CC = p.CC, DD = p.DD, EE = p.EE, FF = p.FF, GG = p.GG, HH = p.HH;
+    const T invJJ = (T)1 / p.JJ;
+    const T S = CC / AA * p.ATG1 + GG / EE * p.ATG2 + DD / BB * p.ATG3 + HH / FF * p.ATG4;
+    const T pref = kRepScaled * invJJ / (T)2;
+    const T A1 = AA * AA / (AA * AA + (a + e) * (a + e));
+    const T A2 = AA * AA / (AA * AA + e * e);
+    const T E1 = EE * EE / (EE * EE + (a + e - d) * (a + e - d));
+    const T E2 = EE * EE / (EE * EE + (e - d) * (e - d));
+    const T B1 = BB * BB / (BB * BB + F * F);
+    const T B2 = BB * BB / (BB * BB + (F - b) * (F - b));
+    const T F1 = FF * FF / (FF * FF + (d + F) * (d + F));
+    const T F2 = FF * FF / (FF * FF + (d + F - b) * (d + F - b));
+    // partials of the four terms of S in their own arguments
+    const T tA_C = p.ATG1 / AA;
+    const T tA_X = -(p.ATG1 * CC) / (AA * AA) + (-A1 * (a + e) + A2 * e) * CC / (AA * AA * AA);
+    const T tA_e = ((A1 - A2) * CC) / (AA * AA);
+    const T tA_a = (A1 * CC) / (AA * AA);
+    const T tE_G = p.ATG2 / EE;
+    const T tE_X = -(p.ATG2 * GG) / (EE * EE) + (-E1 * (a + e - d) + E2 * (e - d)) * GG / (EE * EE * EE);
+    const T tE_em = ((E1 - E2) * GG) / (EE * EE);
+    const T tE_a = (E1 * GG) / (EE * EE);
+    const T tB_D = p.ATG3 / BB;
+    const T tB_X = -(p.ATG3 * DD) / (BB * BB) + (-B1 * F + B2 * (F - b)) * DD / (BB * BB * BB);
+    const T tB_fm = ((B1 - B2) * DD) / (BB * BB);
+    const T tB_b = (B1 * DD) / (BB * BB);
+    const T tF_H = p.ATG4 / FF;
+    const T tF_X = -(p.ATG4 * HH) / (FF * FF) + (-F1 * (d + F) + F2 * (d + F - b)) * HH / (FF * FF * FF);
+    const T tF_dfm = ((F1 - F2) * HH) / (FF * FF);
+    const T tF_b = (F1 * HH) / (FF * FF);
+    T G[3][3];
+    G[0][0] = tA_C * (-2 * F) + tA_X * (c / AA) + tA_a * 2 + tE_G * (2 * (F - b)) + tE_X * ((b + c - 2 * F) / EE) +
+              tE_a * 2 + tF_H * (-2 * b) + tF_X * (b / FF);
+    G[0][1] = tA_C * e + tE_G * (2 * d - e) + tE_X * ((e - d) / EE) + tE_em * (-1) + tB_D * (-F) + tF_H * (2 * d + F) +
+              tF_X * (-(d + F) / FF) + tF_dfm;
+    G[0][2] = tA_C * d + tA_X * (-e / AA) + tA_e + tE_G * (-d) + tE_X * (-(e - d) / EE) + tE_em + tB_D * b +
+              tF_H * (-b) + tF_X * (b / FF);
+    G[1][0] = G[0][1];
+    G[1][1] = tE_G * (-2 * a) + tE_X * (a / EE) + tB_D * (2 * e) + tB_X * (c / BB) + tB_fm * (-2) + tB_b * 2 +
+              tF_H * (-2 * (a + e)) + tF_X * ((a + c + 2 * e) / FF) + tF_dfm * (-2) + tF_b * 2;
+    G[1][2] = tA_C * (-a) + tE_G * a + tE_X * (-a / EE) + tB_D * (-d) + tB_X * (-F / BB) + tB_fm + tF_H * d +
+              tF_X * (-(d + F) / FF) + tF_dfm;
+    G[2][0] = G[0][2];
+    G[2][1] = G[1][2];
+    G[2][2] = tA_X * (a / AA) + tE_X * (a / EE) + tB_X * (b / BB) + tF_X * (b / FF);
+    T J[3][3];
+    J[0][0] = 2 * (-b * c + F * F);
+    J[0][1] = 2 * (c * d - e * F);
+    J[0][2] = 2 * (b * e - d * F);
+    J[1][0] = J[0][1];
+    J[1][1] = 2 * (-a * c + e * e);
+    J[1][2] = 2 * (-d * e + a * F);
+    J[2][0] = J[0][2];
+    J[2][1] = J[1][2];
+    J[2][2] = 2 * (d * d - a * b);
+    T v1[3], v2[3], v3[3];
+#pragma unroll
+    for (int k = 0; k < 3; ++k) {
+        v1[k] = (T)(c2[k] - c1[k]);
+        v2[k] = (T)(c4[k] - c3[k]);
+        v3[k] = (T)(c1[k] - c3[k]);
+    }
+    bool ok = true;
+    T dv[4][3];
+#pragma unroll
+    for (int y = 0; y < 3; ++y) {
+        dv[0][y] = pref * (-invJJ * S * (J[2][y] - J[0][y]) + (G[2][y] - G[0][y]));
+        dv[1][y] = pref * (-invJJ * S * (J[0][y]) + (G[0][y]));
+        dv[2][y] = pref * (-invJJ * S * (-J[2][y] - J[1][y]) + (-G[2][y] - G[1][y]));
+        dv[3][y] = pref * (-invJJ * S * (J[1][y]) + (G[1][y]));
+    }
+#pragma unroll
+    for (int q = 0; q < 4; ++q)
+#pragma unroll
+        for (int k = 0; k < 3; ++k) {
+            out[q][k] = -(dv[q][0] * v1[k] + dv[q][1] * v2[k] + dv[q][2] * v3[k]);
+            if (bad_value(out[q][k])) ok = false;
+        }
+    return ok;
+}
+
+// ---------------------------------------------------------------------------
+// composite-Simpson fallbacks (FP64, whatever the engine precision)
+// ---------------------------------------------------------------------------
+struct Quad {
+    double a, b, c, d, e, F;
+};
+__device__ __forceinline__ Quad quad_of(const double* c1, const double* c2, const double* c3, const double* c4) {
+    Quad q;
+    double v12[3], v34[3], v31[3];
+    for (int k = 0; k < 3; ++k) { v12[k] = c2[k] - c1[k]; v34[k] = c4[k] - c3[k]; v31[k] = c1[k] - c3[k]; }
+    q.a = dot3(v12, v12); q.b = dot3(v34, v34); q.c = dot3(v31, v31);
+    q.d = dot3(v12, v34); q.e = dot3(v12, v31); q.F = dot3(v34, v31);
+    return q;
+}
+__device__ __forceinline__ double r2_at(const Quad& q, double s, double t) {
+    return q.c + 2 * s * q.e + s * s * q.a - 2 * t * q.F - 2 * s * t * q.d + t * t * q.b;
+}
+// Node i of N: endpoints 0 and 1; interior nodes at (i+1)/N, the positions
+// the reference's loop visits (its node counter is advanced before use).
+__device__ __forceinline__ double node(int i, int N) { return i == 0 ? 0.0 : (i == N ? 1.0 : (double)(i + 1) / N); }
+__device__ __forceinline__ double weight(int i, int N) { return (i == 0 || i == N) ? 1.0 : ((i & 1) ? 4.0 : 2.0); }
+
+template <typename Real>
+__global__ void __launch_bounds__(kBlock) k_exvol_fb_energy(DevNet<Real> n) {
+    __shared__ double sh[32];
+    const int cnt = min(*n.ev_fb_count, kExvolFallbackCap);
+    for (int k = blockIdx.x; k < cnt; k += gridDim.x) {
+        const int pr = n.ev_fb_list[2 * k + 1];
+        const int4 bs = n.ev_bead[pr];
+        const CGState& S = n.st[n.ev_fb_list[2 * k]];
+        // positions of this evaluation (trial flag stored in the list entry's sign bit of the count is not
+        // needed: the list is filled by the same launch sequence, with lambda stored alongside)
+        const double lam = __longlong_as_double(((const long long*)n.ev_fb_energy)[kExvolFallbackCap + k]);
+        const bool tr = lam != 0.0;
+        double c1[3], c2[3], c3[3], c4[3];
+        bead_pos(n.x[S.xbuf], n.d, bs.x, tr, lam, c1);
+        bead_pos(n.x[S.xbuf], n.d, bs.y, tr, lam, c2);
+        bead_pos(n.x[S.xbuf], n.d, bs.z, tr, lam, c3);
+        bead_pos(n.x[S.xbuf], n.d, bs.w, tr, lam, c4);
+        const Quad q = quad_of(c1, c2, c3, c4);
+        const int N = kFbNodesEnergy;
+        double acc = 0.0;
+        for (int w = threadIdx.x; w < (N + 1) * (N + 1); w += blockDim.x) {
+            const int i = w / (N + 1), j = w % (N + 1);
+            const double r2 = r2_at(q, node(i, N), node(j, N));
+            acc += weight(i, N) * weight(j, N) * (1.0 / (r2 * r2));
+        }
+        acc = block_sum(acc, sh);
+        if (threadIdx.x == 0) {
+            const double kRepScaled = (double)n.ev_k[pr] * (double)n.ev_la[pr] * (double)n.ev_lb[pr];
+            const double ds = 1.0 / N;
+            const double U = kRepScaled * (ds * ds / 9.0) * acc;
+            n.ev_fb_energy[k] = (bad_value(U) || U < -1.0) ? -1.0 : U;
+        }
+        __syncthreads();
+    }
+}
+
+// numeric forces: partial moments of (entry, chunk), combined by the last chunk
+template <typename Real>
+__global__ void __launch_bounds__(kBlock) k_exvol_fb_force(DevNet<Real> n, double* moments, int* tickets) {
+    __shared__ double sh[32];
+    __shared__ int s_last;
+    const int cnt = min(*n.ev_fb_count, kExvolFallbackCap);
+    const int N = kFbNodesForce;
+    for (int wi = blockIdx.x; wi < cnt * kFbChunks; wi += gridDim.x) {
+        const int k = wi / kFbChunks, ch = wi % kFbChunks;
+        const int pr = n.ev_fb_list[2 * k + 1];
+        const int4 bs = n.ev_bead[pr];
+        const CGState& S = n.st[n.ev_fb_list[2 * k]];
+        const double* X = n.x[S.xbuf];
+        double c1[3], c2[3], c3[3], c4[3];
+        bead_pos<Real>(X, nullptr, bs.x, false, 0.0, c1);
+        bead_pos<Real>(X, nullptr, bs.y, false, 0.0, c2);
+        bead_pos<Real>(X, nullptr, bs.z, false, 0.0, c3);
+        bead_pos<Real>(X, nullptr, bs.w, false, 0.0, c4);
+        const Quad q = quad_of(c1, c2, c3, c4);
+        const int i0 = (int)((long long)(N + 1) * ch / kFbChunks), i1 = (int)((long long)(N + 1) * (ch + 1) / kFbChunks);
+        double m[6] = {0, 0, 0, 0, 0, 0};
+        for (int i = i0; i < i1; ++i) {
+            const double s = node(i, N), ws = weight(i, N);
+            for (int j = threadIdx.x; j <= N; j += blockDim.x) {
+                const double t = node(j, N), w = ws * weight(j, N);
+                const double r2 = r2_at(q, s, t);
+                const double x = w * (1.0 / (r2 * r2 * r2));
+                m[0] += x; m[1] += s * x; m[2] += s * s * x; m[3] += s * t * x; m[4] += t * x; m[5] += t * t * x;
+            }
+        }
+        for (int qd = 0; qd < 6; ++qd) {
+            const double v = block_sum(m[qd], sh);
+            if (threadIdx.x == 0) moments[((size_t)k * kFbChunks + ch) * 6 + qd] = v;
+        }
+        __syncthreads();
+        if (threadIdx.x == 0) {
+            __threadfence();
+            const int tk = atomicAdd(tickets + k, 1);
+            s_last = (tk == kFbChunks - 1);
+            if (s_last) tickets[k] = 0;
+        }
+        __syncthreads();
+        if (s_last && threadIdx.x == 0) {
+            __threadfence();
+            double I[6] = {0, 0, 0, 0, 0, 0};
+            for (int cc = 0; cc < kFbChunks; ++cc)
+                for (int qd = 0; qd < 6; ++qd) I[qd] += __ldcg(moments + ((size_t)k * kFbChunks + cc) * 6 + qd);
+            const double ds = 1.0 / N;
+            for (int qd = 0; qd < 6; ++qd) I[qd] *= (ds * ds / 9.0);
+            const double kRepScaled = (double)n.ev_k[pr] * (double)n.ev_la[pr] * (double)n.ev_lb[pr];
+            double vA[3], vB[3], vC[3], out[4][3];
+            for (int kk = 0; kk < 3; ++kk) { vA[kk] = c1[kk] - c2[kk]; vB[kk] = c3[kk] - c4[kk]; vC[kk] = c3[kk] - c1[kk]; }
+            bool ok = true;
+            for (int kk = 0; kk < 3; ++kk) {
+                out[0][kk] = 4.0 * kRepScaled * (-I[0] * vC[kk] + I[1] * (vC[kk] - vA[kk]) + I[2] * vA[kk] + I[4] * vB[kk] - I[3] * vB[kk]);
+                out[1][kk] = 4.0 * kRepScaled * (-I[1] * vC[kk] - I[2] * vA[kk] + I[3] * vB[kk]);
+                out[2][kk] = 4.0 * kRepScaled * (I[0] * vC[kk] + I[1] * vA[kk] - I[4] * (vB[kk] + vC[kk]) - I[3] * vA[kk] + I[5] * vB[kk]);
+                out[3][kk] = 4.0 * kRepScaled * (I[4] * vC[kk] + I[3] * vA[kk] - I[5] * vB[kk]);
+            }
+            for (int a = 0; a < 4; ++a)
+                for (int kk = 0; kk < 3; ++kk) ok = ok && !bad_value(out[a][kk]);
+            if (!ok) {
+                // Nothing finite is left to use: the reference exits the process
+                // here (CylinderExclVolRepulsion.cpp:1195-1254).
+                atomicOr(n.err, 1u);
+                for (int a = 0; a < 4; ++a)
+                    for (int kk = 0; kk < 3; ++kk) out[a][kk] = __longlong_as_double(0x7ff8000000000000ULL);
+            }
+            Real* cdst = n.contrib + 3 * (size_t)(n.slot_base[K_EXVOL] + 4 * pr);
+            for (int a = 0; a < 4; ++a)
+                for (int kk = 0; kk < 3; ++kk) cdst[3 * a + kk] = (Real)out[a][kk];
+        }
+        __syncthreads();
+    }
+}
+
+// ---------------------------------------------------------------------------
+// main pair kernel (energy partials or force contributions)
+// ---------------------------------------------------------------------------
+template <typename Real>
+__device__ __forceinline__ void flag_fallback(const DevNet<Real>& n, int r, int pr, double lam) {
+    const int k = atomicAdd(n.ev_fb_count, 1);
+    if (k < kExvolFallbackCap) {
+        n.ev_fb_list[2 * k] = r;
+        n.ev_fb_list[2 * k + 1] = pr;
+        ((long long*)n.ev_fb_energy)[kExvolFallbackCap + k] = __double_as_longlong(lam);
+    } else {
+        atomicOr(n.err, 2u);
+    }
+}
+
+template <typename Real>
+__global__ void __launch_bounds__(kBlock) k_exvol(DevNet<Real> n, int want, int trial, int force, int tile_off) {
+    __shared__ double sh[32];
+    __shared__ int s_go, s_xb;
+    __shared__ double s_lam;
+    const int ti = tile_off + blockIdx.x;
+    const Tile t = n.stile[ti];
+    const int r = t.replica;
+    if (threadIdx.x == 0) {
+        const CGState& S = n.st[r];
+        s_go = want < 0 ? (S.active != 0) : (S.phase == want);
+        s_xb = S.xbuf;
+        s_lam = S.lambda;
+    }
+    __syncthreads();
+    if (!s_go) return;
+    const double* X = n.x[s_xb];
+    const bool tr = trial != 0;
+    const int i = t.begin + threadIdx.x;
+    double e = 0.0;
+    if (i < t.end) {
+        const int4 bs = n.ev_bead[i];
+        double c1[3], c2[3], c3[3], c4[3];
+        bead_pos(X, n.d, bs.x, tr, s_lam, c1);
+        bead_pos(X, n.d, bs.y, tr, s_lam, c2);
+        bead_pos(X, n.d, bs.z, tr, s_lam, c3);
+        bead_pos(X, n.d, bs.w, tr, s_lam, c4);
+        const double kRep = (double)n.ev_k[i] * (double)n.ev_la[i] * (double)n.ev_lb[i];
+        const bool fp32 = sizeof(Real) == 4 && coplanarity<float>(c1, c2, c3, c4) >= kMixedFp64Coplanar;
+        if (!force) {
+            const double u = fp32 ? pair_energy<float>(c1, c2, c3, c4, (float)kRep) : pair_energy<double>(c1, c2, c3, c4, kRep);
+            if (u != u) flag_fallback(n, r, i, tr ? s_lam : 0.0);
+            else e = u;
+        } else {
+            Real* cdst = n.contrib + 3 * (size_t)(n.slot_base[K_EXVOL] + 4 * i);
+            bool ok;
+            if (fp32) {
+                float out[4][3];
+                ok = pair_forces<float>(c1, c2, c3, c4, (float)kRep, out);
+                for (int a = 0; a < 4; ++a)
+                    for (int k = 0; k < 3; ++k) cdst[3 * a + k] = (Real)out[a][k];
+            } else {
+                double moved[3];
+                const double* cc2 = c2;
+                if (coplanarity<double>(c1, c2, c3, c4) < 0.1) {   // force path only (:610-626)
+                    push_c2(c1, c2, c3, moved);
+                    cc2 = moved;
+                }
+                double out[4][3];
+                ok = pair_forces<double>(c1, cc2, c3, c4, kRep, out);
+                for (int a = 0; a < 4; ++a)
+                    for (int k = 0; k < 3; ++k) cdst[3 * a + k] = (Real)out[a][k];
+            }
+            if (!ok) flag_fallback(n, r, i, 0.0);
+        }
+    }
+    if (!force) {
+        e = block_sum(e, sh);
+        if (threadIdx.x == 0) n.part_sp[ti] = e;
+    }
+}
+
+template <typename Real>
+static inline int ev_tiles_of(const DevNet<Real>& n, int* off) {
+    *off = n.sp_tiles[K_LINKER] + n.sp_tiles[K_MOTOR];
+    return n.sp_tiles[K_EXVOL];
+}
+
+template <typename Real>
+int launch_exvol_energy(const DevNet<Real>& n, int want, int trial, cudaStream_t s) {
+    int off = 0;
+    const int nt = ev_tiles_of(n, &off);
+    if (nt == 0) return 0;
+    k_exvol<Real><<<nt, kBlock, 0, s>>>(n, want, trial, 0, off);
+    k_exvol_fb_energy<Real><<<64, kBlock, 0, s>>>(n);
+    return 2;
+}
+
+template <typename Real>
+int launch_exvol_forces(const DevNet<Real>& n, int want, cudaStream_t s) {
+    int off = 0;
+    const int nt = ev_tiles_of(n, &off);
+    if (nt == 0) return 0;
+    k_exvol<Real><<<nt, kBlock, 0, s>>>(n, want, 0, 1, off);
+    k_exvol_fb_force<Real><<<4 * 152, kBlock, 0, s>>>(n, n.fb_moments, n.fb_tickets);
+    return 2;
+}
+
+template int launch_exvol_energy<MECH_EXVOL_REAL>(const DevNet<MECH_EXVOL_REAL>&, int, int, cudaStream_t);
+template int launch_exvol_forces<MECH_EXVOL_REAL>(const DevNet<MECH_EXVOL_REAL>&, int, cudaStream_t);
+
+}  // namespace mech

@@ -1,0 +1,685 @@
+// Filament, linker/motor and boundary force-field kernels, the CG vector
+// kernels and the per-replica finalizers of the device-resident minimizer.
+//
+// Reference behaviour restated here (paths relative to medyan-5.4.0/src):
+//   FilamentStretchingHarmonic.cpp:185-275, FilamentBendingCosine.cpp:199-345,
+//   LinkerStretchingHarmonic.cpp:191-293, MotorGhostStretchingHarmonic.cpp:234-340,
+//   BoundaryCylinderRepulsionExp.cpp:27-110, ForceFieldManager.cpp:96-290,
+//   CGMethod.hpp:238-373 and :826-1743, CGMethod.cpp:317-360,
+//   MController.h:273-339 (recovery move).
+//
+// Filament forces are computed owner-side: a block loads its 256 beads plus a
+// two-bead halo into shared memory, evaluates every cylinder and bending
+// triple touching its beads once, and each bead sums its own terms in the
+// reference's order (stretching, then bending, then the sparse force fields
+// through the CSR gather), so no floating-point atomics are used and FP64
+// forces follow the reference's per-bead summation order.
+#include <cuda_runtime.h>
+
+#include "mech_device.cuh"
+
+namespace mech {
+
+// ---------------------------------------------------------------------------
+// helpers
+// ---------------------------------------------------------------------------
+template <typename Real>
+__device__ __forceinline__ double bead_dot(Real a0, Real a1, Real a2, Real b0, Real b1, Real b2) {
+    if (sizeof(Real) == 8) return (double)(a0 * b0 + a1 * b1 + a2 * b2);
+    // single precision: the three products of one bead are summed with fused
+    // multiply-adds, the sum over beads is carried in double
+    return (double)fmaf((float)a2, (float)b2, fmaf((float)a1, (float)b1, (float)a0 * (float)b0));
+}
+
+__device__ __forceinline__ bool replica_selected(const CGState& S, int want) {
+    return want < 0 ? (S.active != 0) : (S.phase == want);
+}
+
+// Whole-grid ticket: the last block to arrive clears the exvol fallback list
+// (used by the excluded-volume kernels of this evaluation).
+template <typename Real>
+__device__ __forceinline__ void grid_done(const DevNet<Real>& n) {
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        __threadfence();
+        const int t = atomicAdd(n.gticket, 1);
+        if (t == (int)gridDim.x - 1) {
+            *n.ev_fb_count = 0;
+            *n.gticket = 0;
+            __threadfence();
+        }
+    }
+}
+
+// ---------------------------------------------------------------------------
+// finalizers (run by the whole last block of a replica)
+// ---------------------------------------------------------------------------
+template <typename Real>
+__device__ void finalize_energy(const DevNet<Real>& n, int r, int trial, double* sh) {
+    const RepTiles rt = n.rt[r];
+    double e[MECH_NUM_FF];
+    e[MECH_FF_STRETCHING] = sum_slots(n.part_fil, 4, 0, rt.fil_begin, rt.fil_end, sh);
+    e[MECH_FF_BENDING] = sum_slots(n.part_fil, 4, 1, rt.fil_begin, rt.fil_end, sh);
+    e[MECH_FF_LINKER] = sum_slots(n.part_sp, 1, 0, rt.sp_begin[K_LINKER], rt.sp_end[K_LINKER], sh);
+    e[MECH_FF_MOTOR] = sum_slots(n.part_sp, 1, 0, rt.sp_begin[K_MOTOR], rt.sp_end[K_MOTOR], sh);
+    e[MECH_FF_EXVOL] = sum_slots(n.part_sp, 1, 0, rt.sp_begin[K_EXVOL], rt.sp_end[K_EXVOL], sh);
+    e[MECH_FF_BOUNDARY] = sum_slots(n.part_sp, 1, 0, rt.sp_begin[K_BOUNDARY], rt.sp_end[K_BOUNDARY], sh);
+    if (threadIdx.x != 0) return;
+    // Pairs whose analytic energy was not usable were evaluated numerically;
+    // add them in pair order.  A failed pair makes the force field report -1
+    // (CylinderExclVolRepulsion.cpp:442-481).
+    const int cnt = min(__ldcg(n.ev_fb_count), kExvolFallbackCap);
+    int last = -1;
+    bool ev_failed = false;
+    for (;;) {
+        int best = -1, bestPair = 0x7fffffff;
+        for (int k = 0; k < cnt; ++k) {
+            const int rep = __ldcg(n.ev_fb_list + 2 * k), pr = __ldcg(n.ev_fb_list + 2 * k + 1);
+            if (rep == r && pr > last && pr < bestPair) { best = k; bestPair = pr; }
+        }
+        if (best < 0) break;
+        const double u = __ldcg(n.ev_fb_energy + best);
+        if (u == -1.0) ev_failed = true;
+        else e[MECH_FF_EXVOL] += u;
+        last = bestPair;
+    }
+    if (ev_failed) e[MECH_FF_EXVOL] = -1.0;
+    CGState& S = n.st[r];
+    double tot = 0.0;
+    bool failed = false;
+    for (int k = 0; k < MECH_NUM_FF; ++k) {
+        S.eval[k] = e[k];
+        tot += e[k];
+        if (e[k] <= -1) failed = true;
+    }
+    S.eval[MECH_NUM_FF] = tot;
+    S.evalFailed = failed;
+    S.numEnergyEval++;
+    const double E = failed ? (1.0 / 0.0) : tot;
+    if (trial && S.phase == PH_LS_TRIAL) {
+        S.Etrial = E;
+        line_search_step(S, E);
+    } else if (S.phase == PH_RECOVER_ENERGY) {
+        S.E0 = E;
+        S.phase = PH_RESET;
+    } else {
+        S.E0 = E;
+    }
+}
+
+template <typename Real>
+__device__ void finalize_force(const DevNet<Real>& n, int r, double* sh) {
+    const RepTiles rt = n.rt[r];
+    const double mx = max_slots(n.part_fil, 4, 0, rt.fil_begin, rt.fil_end, sh);
+    const double ff = sum_slots(n.part_fil, 4, 1, rt.fil_begin, rt.fil_end, sh);
+    const double ffp = sum_slots(n.part_fil, 4, 2, rt.fil_begin, rt.fil_end, sh);
+    if (threadIdx.x != 0) return;
+    CGState& S = n.st[r];
+    const int ph = S.phase;
+    if (ph == PH_FORCE || ph == PH_RECOVER_FORCE) S.numForceCall++;
+    S.maxF = mx;
+    S.FdotF = ff;
+    S.fbuf ^= 1;
+    if (!isfinite(mx)) {   // CGMethod::maxF throws (CGMethod.hpp:207-210)
+        S.status = MECH_ERR_NONFINITE;
+        S.phase = PH_ERROR;
+        return;
+    }
+    if (ph == PH_FORCE) {
+        S.energyRelChange = fabs(S.newEnergy - S.prevEnergy) / fabs(S.prevEnergy);
+        S.prevEnergy = S.newEnergy;
+        double beta = 0.0;
+        if (S.method == 1) {
+            S.newGrad = ff;
+            beta = S.newGrad / S.lastFdotF;
+        } else if (S.method == 2) {
+            S.newGrad = ff;
+            S.prevGrad = ffp;
+            beta = fmax(0.0, (S.newGrad - S.prevGrad) / S.lastFdotF);
+        }
+        S.beta = beta;
+        // minimum-energy backup once past half the call limit (CGMethod.hpp:1564-1566)
+        if (mx <= 10 * S.gradTol && S.numIter > S.forceCallLimit / 2 && S.totalEnergy <= S.minimumE) {
+            S.minimumE = S.totalEnergy;
+            S.backupPending = 1;
+        }
+        S.phase = PH_DIR;
+    } else if (ph == PH_RECOVER_FORCE) {
+        S.phase = PH_RECOVER_ENERGY;
+    }
+}
+
+// ---------------------------------------------------------------------------
+// filament energy: stretching + bending of the tile's own cylinders/triples
+// ---------------------------------------------------------------------------
+template <typename Real>
+__global__ void __launch_bounds__(kBlock) k_fil_energy(DevNet<Real> n, int want, int trial) {
+    __shared__ double xs[(kFilTile + 4) * 3];
+    __shared__ double sh[32];
+    __shared__ int s_go, s_xb, s_flag;
+    __shared__ double s_lam;
+    const Tile t = n.ftile[blockIdx.x];
+    const int r = t.replica;
+    if (threadIdx.x == 0) {
+        const CGState& S = n.st[r];
+        s_go = replica_selected(S, want);
+        s_xb = S.xbuf;
+        s_lam = S.lambda;
+    }
+    __syncthreads();
+    if (s_go) {
+        const int T = t.end - t.begin;
+        const double* X = n.x[s_xb];
+        const bool tr = trial != 0;
+        for (int i = threadIdx.x; i < T + 4; i += blockDim.x) {
+            const int b = t.begin - 2 + i;
+            double p[3] = {0.0, 0.0, 0.0};
+            if (b >= 0 && b < n.nb) bead_pos(X, n.d, b, tr, s_lam, p);
+            xs[3 * i] = p[0];
+            xs[3 * i + 1] = p[1];
+            xs[3 * i + 2] = p[2];
+        }
+        __syncthreads();
+        double es = 0.0, eb = 0.0;
+        const int i = threadIdx.x;
+        if (i < T) {
+            const int j = t.begin + i;
+            const int fl = n.bflag[j];
+            const double* pm = xs + 3 * (i + 1);
+            const double* p0 = xs + 3 * (i + 2);
+            const double* pp = xs + 3 * (i + 3);
+            if (tr) {   // materialize the trial coordinates of the owned bead
+                double* XT = n.x[s_xb ^ 1] + 3 * (size_t)j;
+                XT[0] = p0[0];
+                XT[1] = p0[1];
+                XT[2] = p0[2];
+            }
+            if (fl & 1) {
+                const Real r2[3] = {(Real)(pp[0] - p0[0]), (Real)(pp[1] - p0[1]), (Real)(pp[2] - p0[2])};
+                es = stretch_energy<Real>(r2[0], r2[1], r2[2], n.kstr[j], n.l0[j]);
+                if (fl & 2) {
+                    const Real r1[3] = {(Real)(p0[0] - pm[0]), (Real)(p0[1] - pm[1]), (Real)(p0[2] - pm[2])};
+                    eb = bend_energy<Real>(r1, r2, n.kbend[j], n.t0[j]);
+                }
+            }
+        }
+        es = block_sum(es, sh);
+        eb = block_sum(eb, sh);
+        if (threadIdx.x == 0) {
+            n.part_fil[4 * (size_t)blockIdx.x + 0] = es;
+            n.part_fil[4 * (size_t)blockIdx.x + 1] = eb;
+        }
+        const RepTiles rt = n.rt[r];
+        if (last_tile(n.ticket, r, rt.fil_end - rt.fil_begin, &s_flag)) finalize_energy(n, r, trial, sh);
+    }
+    grid_done(n);
+}
+
+// ---------------------------------------------------------------------------
+// filament forces + CSR gather of the sparse contributions + CG partials
+// ---------------------------------------------------------------------------
+template <typename Real>
+__global__ void __launch_bounds__(kBlock) k_fil_force(DevNet<Real> n, int want) {
+    __shared__ double xs[(kFilTile + 4) * 3];
+    __shared__ Real fs[(kFilTile + 2) * 3];    // stretch force on the second bead
+    __shared__ Real f1[(kFilTile + 2) * 3];    // bending Fr1
+    __shared__ Real f2[(kFilTile + 2) * 3];    // bending Fr2
+    __shared__ double sh[32];
+    __shared__ int s_go, s_xb, s_fb, s_flag;
+    const Tile t = n.ftile[blockIdx.x];
+    const int r = t.replica;
+    if (threadIdx.x == 0) {
+        const CGState& S = n.st[r];
+        s_go = replica_selected(S, want);
+        s_xb = S.xbuf;
+        s_fb = S.fbuf;
+    }
+    __syncthreads();
+    if (s_go) {
+        const int T = t.end - t.begin;
+        const double* X = n.x[s_xb];
+        for (int i = threadIdx.x; i < T + 4; i += blockDim.x) {
+            const int b = t.begin - 2 + i;
+            double p[3] = {0.0, 0.0, 0.0};
+            if (b >= 0 && b < n.nb) bead_pos<Real>(X, nullptr, b, false, 0.0, p);
+            xs[3 * i] = p[0];
+            xs[3 * i + 1] = p[1];
+            xs[3 * i + 2] = p[2];
+        }
+        __syncthreads();
+        // interaction slots s in [0, T + 2): bead j = begin - 1 + s, shared index s + 1
+        for (int s = threadIdx.x; s < T + 2; s += blockDim.x) {
+            const int j = t.begin - 1 + s;
+            Real a[3] = {0, 0, 0}, b1[3] = {0, 0, 0}, b2[3] = {0, 0, 0};
+            if (j >= 0 && j < n.nb) {
+                const int fl = n.bflag[j];
+                const double* pm = xs + 3 * s;
+                const double* p0 = xs + 3 * (s + 1);
+                const double* pp = xs + 3 * (s + 2);
+                if (fl & 1) {
+                    const Real r2[3] = {(Real)(pp[0] - p0[0]), (Real)(pp[1] - p0[1]), (Real)(pp[2] - p0[2])};
+                    stretch_force<Real>(r2[0], r2[1], r2[2], n.kstr[j], n.l0[j], a);
+                    if (fl & 2) {
+                        const Real r1[3] = {(Real)(p0[0] - pm[0]), (Real)(p0[1] - pm[1]), (Real)(p0[2] - pm[2])};
+                        bend_force<Real>(r1, r2, n.kbend[j], n.t0[j], b1, b2);
+                    }
+                }
+            }
+#pragma unroll
+            for (int q = 0; q < 3; ++q) {
+                fs[3 * s + q] = a[q];
+                f1[3 * s + q] = b1[q];
+                f2[3 * s + q] = b2[q];
+            }
+        }
+        __syncthreads();
+        double mx = 0.0, ff = 0.0, ffp = 0.0;
+        const int i = threadIdx.x;
+        if (i < T) {
+            const int b = t.begin + i;
+            Real F[3];
+#pragma unroll
+            for (int q = 0; q < 3; ++q) {
+                // stretching: cylinder (b-1, b) then (b, b+1); bending: triples
+                // centred on b-1, b, b+1 (the reference's interaction order)
+                Real v = fs[3 * i + q];
+                v += -fs[3 * (i + 1) + q];
+                v += f2[3 * i + q];
+                v += f1[3 * (i + 1) + q] - f2[3 * (i + 1) + q];
+                v += -f1[3 * (i + 2) + q];
+                F[q] = v;
+            }
+            const int c0 = n.csr_off[b], c1 = n.csr_off[b + 1];
+            for (int c = c0; c < c1; ++c) {
+                const int sl = n.csr_slot[c];
+                F[0] += n.contrib[3 * (size_t)sl];
+                F[1] += n.contrib[3 * (size_t)sl + 1];
+                F[2] += n.contrib[3 * (size_t)sl + 2];
+            }
+            Real* Fo = n.f[s_fb ^ 1] + 3 * (size_t)b;
+            const Real* Fp = n.f[s_fb] + 3 * (size_t)b;
+            Fo[0] = F[0];
+            Fo[1] = F[1];
+            Fo[2] = F[2];
+            mx = fmax(fmax(fabs((double)F[0]), fabs((double)F[1])), fabs((double)F[2]));
+            ff = bead_dot<Real>(F[0], F[1], F[2], F[0], F[1], F[2]);
+            ffp = bead_dot<Real>(F[0], F[1], F[2], Fp[0], Fp[1], Fp[2]);
+        }
+        mx = block_max(mx, sh);
+        ff = block_sum(ff, sh);
+        ffp = block_sum(ffp, sh);
+        if (threadIdx.x == 0) {
+            n.part_fil[4 * (size_t)blockIdx.x + 0] = mx;
+            n.part_fil[4 * (size_t)blockIdx.x + 1] = ff;
+            n.part_fil[4 * (size_t)blockIdx.x + 2] = ffp;
+        }
+        const RepTiles rt = n.rt[r];
+        if (last_tile(n.ticket, r, rt.fil_end - rt.fil_begin, &s_flag)) finalize_force(n, r, sh);
+    }
+    grid_done(n);
+}
+
+// ---------------------------------------------------------------------------
+// linker, motor and boundary interactions (energy or force contributions)
+// ---------------------------------------------------------------------------
+template <typename Real>
+__global__ void __launch_bounds__(kBlock) k_bond_bnd(DevNet<Real> n, int want, int trial, int force, int n_lm_tiles,
+                                                     int ev_tiles) {
+    __shared__ double sh[32];
+    __shared__ int s_go, s_xb;
+    __shared__ double s_lam;
+    const int ti = blockIdx.x < n_lm_tiles ? blockIdx.x : blockIdx.x + ev_tiles;
+    const Tile t = n.stile[ti];
+    const int kind = n.stile_kind[ti];
+    const int r = t.replica;
+    if (threadIdx.x == 0) {
+        const CGState& S = n.st[r];
+        s_go = replica_selected(S, want);
+        s_xb = S.xbuf;
+        s_lam = S.lambda;
+    }
+    __syncthreads();
+    if (!s_go) return;
+    const double* X = n.x[s_xb];
+    const bool tr = trial != 0;
+    const int i = t.begin + threadIdx.x;
+    double e = 0.0;
+    if (i < t.end) {
+        if (kind == K_BOUNDARY) {
+            const int b = n.bb_bead[i];
+            const double* pl = n.planes + 4 * n.bb_plane[i];
+            double p[3];
+            bead_pos(X, n.d, b, tr, s_lam, p);
+            const double rr = plane_dist(pl, p);
+            const Real K = n.bb_k[i], sl = n.bb_slen[i];
+            const Real R = (Real)(-rr / (double)sl);
+            const Real ex = exp(R);
+            if (!force) {
+                e = (double)(K * ex);
+            } else {
+                const Real f0 = K * ex / sl;
+                Real* c = n.contrib + 3 * (size_t)(n.slot_base[K_BOUNDARY] + i);
+                c[0] = f0 * (Real)pl[0];
+                c[1] = f0 * (Real)pl[1];
+                c[2] = f0 * (Real)pl[2];
+            }
+        } else {
+            const bool lk = kind == K_LINKER;
+            const int4 bs = lk ? n.lk_bead[i] : n.mt_bead[i];
+            const Real k = lk ? n.lk_k[i] : n.mt_k[i];
+            const Real l0 = lk ? n.lk_l0[i] : n.mt_l0[i];
+            const Real s1 = lk ? n.lk_s1[i] : n.mt_s1[i];
+            const Real s2 = lk ? n.lk_s2[i] : n.mt_s2[i];
+            double c1[3], c2[3], c3[3], c4[3], v1[3], v2[3];
+            bead_pos(X, n.d, bs.x, tr, s_lam, c1);
+            bead_pos(X, n.d, bs.y, tr, s_lam, c2);
+            bead_pos(X, n.d, bs.z, tr, s_lam, c3);
+            bead_pos(X, n.d, bs.w, tr, s_lam, c4);
+            lerp3(c1, c2, (double)s1, v1);
+            lerp3(c3, c4, (double)s2, v2);
+            const Real lx = (Real)(v2[0] - v1[0]), ly = (Real)(v2[1] - v1[1]), lz = (Real)(v2[2] - v1[2]);
+            const Real dist = sqrt(lx * lx + ly * ly + lz * lz);
+            if (!force) {
+                const Real dd = dist - l0;
+                e = (double)((Real)0.5 * k * dd * dd);
+            } else {
+                const Real invL = (Real)1 / dist;
+                const Real f0 = k * (dist - l0) * invL;
+                const Real Fl[3] = {-f0 * lx, -f0 * ly, -f0 * lz};
+                Real* c = n.contrib + 3 * (size_t)(n.slot_base[kind] + 4 * i);
+#pragma unroll
+                for (int q = 0; q < 3; ++q) {
+                    c[q] = -Fl[q] * ((Real)1 - s1);
+                    c[3 + q] = -Fl[q] * (s1);
+                    c[6 + q] = Fl[q] * ((Real)1 - s2);
+                    c[9 + q] = Fl[q] * (s2);
+                }
+                (lk ? n.lk_sf : n.mt_sf)[i] = (double)(f0 / invL);
+            }
+        }
+    }
+    if (!force) {
+        e = block_sum(e, sh);
+        if (threadIdx.x == 0) n.part_sp[ti] = e;
+    }
+}
+
+// ---------------------------------------------------------------------------
+// direction update d = F + beta d, conjugacy check, backup copy
+// ---------------------------------------------------------------------------
+template <typename Real>
+__global__ void __launch_bounds__(kBlock) k_direction(DevNet<Real> n) {
+    __shared__ double sh[32];
+    __shared__ int s_go, s_fb, s_xb, s_bk, s_flag;
+    __shared__ double s_beta;
+    const Tile t = n.ftile[blockIdx.x];
+    const int r = t.replica;
+    if (threadIdx.x == 0) {
+        const CGState& S = n.st[r];
+        s_go = S.phase == PH_DIR;
+        s_fb = S.fbuf;
+        s_xb = S.xbuf;
+        s_bk = S.backupPending;
+        s_beta = S.beta;
+    }
+    __syncthreads();
+    if (!s_go) return;
+    const int b = t.begin + threadIdx.x;
+    double dF = 0.0;
+    if (b < t.end) {
+        const Real* F = n.f[s_fb] + 3 * (size_t)b;
+        Real* D = n.d + 3 * (size_t)b;
+        const Real beta = (Real)s_beta;
+        const Real d0 = F[0] + beta * D[0], d1 = F[1] + beta * D[1], d2 = F[2] + beta * D[2];
+        D[0] = d0;
+        D[1] = d1;
+        D[2] = d2;
+        dF = bead_dot<Real>(d0, d1, d2, F[0], F[1], F[2]);
+        if (s_bk) {
+            const double* X = n.x[s_xb] + 3 * (size_t)b;
+            double* B = n.xbest + 3 * (size_t)b;
+            B[0] = X[0];
+            B[1] = X[1];
+            B[2] = X[2];
+        }
+    }
+    dF = block_sum(dF, sh);
+    if (threadIdx.x == 0) n.part_fil[4 * (size_t)blockIdx.x + 3] = dF;
+    const RepTiles rt = n.rt[r];
+    if (last_tile(n.ticket, r, rt.fil_end - rt.fil_begin, &s_flag)) {
+        const double slope = sum_slots(n.part_fil, 4, 3, rt.fil_begin, rt.fil_end, sh);
+        if (threadIdx.x == 0) {
+            CGState& S = n.st[r];
+            if (S.backupPending) {
+                S.backupValid = 1;
+                S.backupPending = 0;
+            }
+            if (slope <= 0) {          // conjugacy lost: reset to steepest descent
+                S.phase = PH_RESET;
+            } else {
+                S.slope = slope;
+                if (S.method >= 1) S.lastFdotF = S.newGrad;
+                begin_iteration(S);
+            }
+        }
+    }
+}
+
+// d = F (resetCGParams, CGMethod.hpp:963-972); the new slope d.F is F.F
+template <typename Real>
+__global__ void __launch_bounds__(kBlock) k_reset(DevNet<Real> n) {
+    __shared__ int s_go, s_fb, s_flag;
+    const Tile t = n.ftile[blockIdx.x];
+    const int r = t.replica;
+    if (threadIdx.x == 0) {
+        const CGState& S = n.st[r];
+        s_go = S.phase == PH_RESET;
+        s_fb = S.fbuf;
+    }
+    __syncthreads();
+    if (!s_go) return;
+    const int b = t.begin + threadIdx.x;
+    if (b < t.end) {
+        const Real* F = n.f[s_fb] + 3 * (size_t)b;
+        Real* D = n.d + 3 * (size_t)b;
+        D[0] = F[0];
+        D[1] = F[1];
+        D[2] = F[2];
+    }
+    const RepTiles rt = n.rt[r];
+    if (last_tile(n.ticket, r, rt.fil_end - rt.fil_begin, &s_flag)) {
+        if (threadIdx.x == 0) {
+            CGState& S = n.st[r];
+            S.slope = S.FdotF;
+            S.lastFdotF = S.FdotF;
+            begin_iteration(S);
+        }
+    }
+}
+
+// lambda = 0 after a line search (CGMethod.hpp:1337-1367)
+__global__ void k_dispatch_failed(CGState* st, int R) {
+    const int r = blockIdx.x * blockDim.x + threadIdx.x;
+    if (r >= R) return;
+    CGState& S = st[r];
+    if (S.phase != PH_FAILED) return;
+    if (!S.tryToRecover) {
+        S.errorFlags |= 1u;
+        S.status = MECH_ERR_LINESEARCH;
+        S.phase = PH_DONE;
+    } else if (!S.safeMode) {
+        S.safeMode = 1;
+        S.numSafeMode++;
+        S.phase = PH_RESET;
+    } else {
+        S.safeMode = 0;
+        S.numRecover++;
+        S.phase = PH_RECOVER;
+    }
+}
+
+// Recovery move: step = maxDist / max_i |d_i|, x += step d (MController.h:273-339).
+template <typename Real>
+__global__ void __launch_bounds__(kBlock) k_recover_maxabs(DevNet<Real> n) {
+    __shared__ double sh[32];
+    __shared__ int s_go, s_flag;
+    const Tile t = n.ftile[blockIdx.x];
+    const int r = t.replica;
+    if (threadIdx.x == 0) s_go = n.st[r].phase == PH_RECOVER;
+    __syncthreads();
+    if (!s_go) return;
+    const int b = t.begin + threadIdx.x;
+    double m = 0.0;
+    if (b < t.end) {
+        const Real* D = n.d + 3 * (size_t)b;
+        m = fmax(fmax(fabs((double)D[0]), fabs((double)D[1])), fabs((double)D[2]));
+    }
+    m = block_max(m, sh);
+    if (threadIdx.x == 0) n.part_fil[4 * (size_t)blockIdx.x + 3] = m;
+    const RepTiles rt = n.rt[r];
+    if (last_tile(n.ticket, r, rt.fil_end - rt.fil_begin, &s_flag)) {
+        const double mx = max_slots(n.part_fil, 4, 3, rt.fil_begin, rt.fil_end, sh);
+        if (threadIdx.x == 0) {
+            CGState& S = n.st[r];
+            const double step = S.maxDist / mx;
+            if (!(step < (1.0 / 0.0))) {   // "step size is infinity" (MController.h:311-316)
+                S.status = MECH_ERR_NONFINITE;
+                S.phase = PH_ERROR;
+            } else {
+                S.lambda = step;
+                S.phase = PH_RECOVER_MOVE;
+            }
+        }
+    }
+}
+
+template <typename Real>
+__global__ void __launch_bounds__(kBlock) k_recover_move(DevNet<Real> n) {
+    __shared__ int s_go, s_xb, s_flag;
+    __shared__ double s_step;
+    const Tile t = n.ftile[blockIdx.x];
+    const int r = t.replica;
+    if (threadIdx.x == 0) {
+        const CGState& S = n.st[r];
+        s_go = S.phase == PH_RECOVER_MOVE;
+        s_xb = S.xbuf;
+        s_step = S.lambda;
+    }
+    __syncthreads();
+    if (!s_go) return;
+    const int b = t.begin + threadIdx.x;
+    if (b < t.end) {
+        double* X = n.x[s_xb] + 3 * (size_t)b;
+        const Real* D = n.d + 3 * (size_t)b;
+        X[0] += s_step * (double)D[0];
+        X[1] += s_step * (double)D[1];
+        X[2] += s_step * (double)D[2];
+    }
+    const RepTiles rt = n.rt[r];
+    if (last_tile(n.ticket, r, rt.fil_end - rt.fil_begin, &s_flag)) {
+        if (threadIdx.x == 0) n.st[r].phase = PH_RECOVER_FORCE;
+    }
+}
+
+template <typename Real>
+__global__ void __launch_bounds__(kBlock) k_backup_restore(DevNet<Real> n) {
+    const Tile t = n.ftile[blockIdx.x];
+    const CGState& S = n.st[t.replica];
+    if (!S.restore) return;
+    const int b = t.begin + threadIdx.x;
+    if (b < t.end) {
+        double* X = n.x[S.xbuf] + 3 * (size_t)b;
+        const double* B = n.xbest + 3 * (size_t)b;
+        X[0] = B[0];
+        X[1] = B[1];
+        X[2] = B[2];
+    }
+}
+
+// ---------------------------------------------------------------------------
+// launchers
+// ---------------------------------------------------------------------------
+template <typename Real>
+static int n_lm_tiles(const DevNet<Real>& n, int* ev_tiles, int* bb_tiles) {
+    *ev_tiles = n.sp_tiles[K_EXVOL];
+    *bb_tiles = n.sp_tiles[K_BOUNDARY];
+    return n.sp_tiles[K_LINKER] + n.sp_tiles[K_MOTOR];
+}
+
+template <typename Real>
+int launch_energy(const DevNet<Real>& n, int want, int trial, cudaStream_t s) {
+    int ev_t = 0, bb_t = 0;
+    const int lm = n_lm_tiles(n, &ev_t, &bb_t);
+    int launched = 0;
+    if (lm + bb_t > 0) {
+        k_bond_bnd<Real><<<lm + bb_t, kBlock, 0, s>>>(n, want, trial, 0, lm, ev_t);
+        ++launched;
+    }
+    launched += launch_exvol_energy<Real>(n, want, trial, s);
+    k_fil_energy<Real><<<n.n_ftiles, kBlock, 0, s>>>(n, want, trial);
+    return launched + 1;
+}
+
+template <typename Real>
+int launch_forces(const DevNet<Real>& n, int want, cudaStream_t s) {
+    int ev_t = 0, bb_t = 0;
+    const int lm = n_lm_tiles(n, &ev_t, &bb_t);
+    int launched = 0;
+    if (lm + bb_t > 0) {
+        k_bond_bnd<Real><<<lm + bb_t, kBlock, 0, s>>>(n, want, 0, 1, lm, ev_t);
+        ++launched;
+    }
+    launched += launch_exvol_forces<Real>(n, want, s);
+    k_fil_force<Real><<<n.n_ftiles, kBlock, 0, s>>>(n, want);
+    return launched + 1;
+}
+
+template <typename Real>
+int launch_direction(const DevNet<Real>& n, cudaStream_t s) {
+    k_direction<Real><<<n.n_ftiles, kBlock, 0, s>>>(n);
+    return 1;
+}
+
+template <typename Real>
+int launch_reset(const DevNet<Real>& n, cudaStream_t s) {
+    k_reset<Real><<<n.n_ftiles, kBlock, 0, s>>>(n);
+    return 1;
+}
+
+template <typename Real>
+int launch_dispatch_failed(const DevNet<Real>& n, cudaStream_t s) {
+    k_dispatch_failed<<<(n.R + 127) / 128, 128, 0, s>>>(n.st, n.R);
+    return 1;
+}
+
+template <typename Real>
+int launch_recover(const DevNet<Real>& n, cudaStream_t s) {
+    int k = 0;
+    k_recover_maxabs<Real><<<n.n_ftiles, kBlock, 0, s>>>(n);
+    k_recover_move<Real><<<n.n_ftiles, kBlock, 0, s>>>(n);
+    k += 2;
+    k += launch_forces<Real>(n, PH_RECOVER_FORCE, s);
+    k += launch_energy<Real>(n, PH_RECOVER_ENERGY, 0, s);
+    k += launch_reset<Real>(n, s);
+    return k;
+}
+
+template <typename Real>
+int launch_backup_restore(const DevNet<Real>& n, cudaStream_t s) {
+    k_backup_restore<Real><<<n.n_ftiles, kBlock, 0, s>>>(n);
+    return 1;
+}
+
+#define MECH_INSTANTIATE(R)                                                             \
+    template int launch_energy<R>(const DevNet<R>&, int, int, cudaStream_t);            \
+    template int launch_forces<R>(const DevNet<R>&, int, cudaStream_t);                 \
+    template int launch_direction<R>(const DevNet<R>&, cudaStream_t);                   \
+    template int launch_reset<R>(const DevNet<R>&, cudaStream_t);                       \
+    template int launch_dispatch_failed<R>(const DevNet<R>&, cudaStream_t);             \
+    template int launch_recover<R>(const DevNet<R>&, cudaStream_t);                     \
+    template int launch_backup_restore<R>(const DevNet<R>&, cudaStream_t);
+MECH_INSTANTIATE(double)
+MECH_INSTANTIATE(float)
+#undef MECH_INSTANTIATE
+
+}  // namespace mech

@@ -1,0 +1,1069 @@
+// Host side of the engine: the context, network upload (serializeDof +
+// vectorizeAllForceFields), neighbor-list rebuild orchestration, the CUDA-graph
+// driven minimizer loop, and the C ABI of include/medyan_mech.h.
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <chrono>
+#include <cmath>
+#include <cstdio>
+#include <cstring>
+#include <limits>
+#include <mutex>
+#include <string>
+#include <vector>
+
+#include "mech_internal.cuh"
+#include "mech_nl.cuh"
+
+namespace mech {
+
+static thread_local std::string g_last_error;
+
+static int set_err(int code, const std::string& msg) {
+    g_last_error = msg;
+    return code;
+}
+
+#define CU(call)                                                                                   \
+    do {                                                                                           \
+        cudaError_t _e = (call);                                                                   \
+        if (_e != cudaSuccess)                                                                     \
+            return set_err(MECH_ERR_CUDA, std::string(#call) + ": " + cudaGetErrorString(_e));     \
+    } while (0)
+
+struct ReplicaHost {
+    int nb = 0, bead_begin = 0;
+    int ncyl = 0, cyl_begin = 0;
+    int nfil = 0;
+    int nlk = 0, lk_begin = 0, nmt = 0, mt_begin = 0;
+    int nplanes = 0, plane_begin = 0;
+    std::vector<int> perm;     // caller bead -> internal local index
+    std::vector<int> inv;      // internal local index -> caller bead
+    double box[3] = {0, 0, 0};
+    double rmax = 0, bcut = 0;
+    // set by the last rebuild
+    long long nev = 0, ev_begin = 0, nbb = 0, bb_begin = 0, nbcyl = 0;
+    double cell = 0;
+    int gx = 1, gy = 1, gz = 1;
+    long long cell_off = 0;
+};
+
+}  // namespace mech
+
+using namespace mech;
+
+struct MechContext {
+    int device = 0;
+    int precision = MECH_PREC_FP64;
+    cudaStream_t stream = nullptr;
+    int R = 0;
+    int nb = 0, ncyl = 0, nlk = 0, nmt = 0, nplanes = 0;
+    long long nev = 0, nbb = 0;
+    std::vector<ReplicaHost> reps;
+    bool have_net = false, have_lists = false;
+    // beads
+    DeviceBuffer x[2], f[2], d, xbest, bflag, kstr, l0, kbend, t0;
+    // cylinders
+    DeviceBuffer cyl_b1, cyl_id, cyl_fil, cyl_pos, cyl_rep, cyl_minus, cyl_kex, cyl_type, cyl_l0;
+    // linkers / motors
+    DeviceBuffer lk_bead, lk_k, lk_l0, lk_s1, lk_s2, lk_sf, mt_bead, mt_k, mt_l0, mt_s1, mt_s2, mt_sf;
+    // boundary
+    DeviceBuffer planes, plane_k, plane_slen, bb_k, bb_slen;
+    // excluded volume
+    DeviceBuffer ev_bead, ev_k, ev_la, ev_lb;
+    // tiles, partials, state
+    DeviceBuffer ftile, stile, stile_kind, rt, part_fil, part_sp, st, ticket, gticket, err;
+    DeviceBuffer contrib, ev_fb_count, ev_fb_list, ev_fb_energy, fb_moments, fb_tickets;
+    // rebuild scratch
+    PairBuild pb;
+    BndBuild bbuild;
+    CsrBuild cb;
+    DeviceBuffer rep_cell, rep_dims, rep_rmax2, rep_rmin2, rep_margin, rep_q, rep_ncyl, rep_plane, rep_cyl, rep_bcut,
+        gather_idx, gather_out;
+    int n_ftiles = 0, n_stiles = 0;
+    int sp_tiles[K_NUM_SPARSE] = {0, 0, 0, 0};
+    int slot_base[K_NUM_SPARSE + 1] = {0, 0, 0, 0, 0};
+    std::vector<RepTiles> h_rt;
+    CGState* h_st = nullptr;   // pinned mirror of the states
+    unsigned* h_err = nullptr;
+    MechTiming timing{};
+    std::vector<int32_t> cyl_local_first;   // replica-local cylinder -> internal global first bead
+
+    ~MechContext() {
+        if (h_st) cudaFreeHost(h_st);
+        if (h_err) cudaFreeHost(h_err);
+        if (stream) cudaStreamDestroy(stream);
+    }
+};
+
+namespace {
+
+template <typename T>
+int upload(DeviceBuffer& b, const std::vector<T>& v, cudaStream_t s) {
+    CU(b.ensure(sizeof(T) * std::max<size_t>(v.size(), 1)));
+    if (!v.empty()) CU(cudaMemcpyAsync(b.p, v.data(), sizeof(T) * v.size(), cudaMemcpyHostToDevice, s));
+    return MECH_OK;
+}
+
+template <typename Real>
+DevNet<Real> make_devnet(MechContext* c) {
+    DevNet<Real> n{};
+    n.nb = c->nb;
+    n.R = c->R;
+    n.x[0] = c->x[0].as<double>();
+    n.x[1] = c->x[1].as<double>();
+    n.f[0] = c->f[0].as<Real>();
+    n.f[1] = c->f[1].as<Real>();
+    n.d = c->d.as<Real>();
+    n.xbest = c->xbest.as<double>();
+    n.bflag = c->bflag.as<uint8_t>();
+    n.kstr = c->kstr.as<Real>();
+    n.l0 = c->l0.as<Real>();
+    n.kbend = c->kbend.as<Real>();
+    n.t0 = c->t0.as<Real>();
+    n.n_ftiles = c->n_ftiles;
+    n.ftile = c->ftile.as<Tile>();
+    n.n_lk = c->nlk;
+    n.n_mt = c->nmt;
+    n.n_ev = (int)c->nev;
+    n.n_bb = (int)c->nbb;
+    n.lk_bead = c->lk_bead.as<int4>();
+    n.lk_k = c->lk_k.as<Real>();
+    n.lk_l0 = c->lk_l0.as<Real>();
+    n.lk_s1 = c->lk_s1.as<Real>();
+    n.lk_s2 = c->lk_s2.as<Real>();
+    n.mt_bead = c->mt_bead.as<int4>();
+    n.mt_k = c->mt_k.as<Real>();
+    n.mt_l0 = c->mt_l0.as<Real>();
+    n.mt_s1 = c->mt_s1.as<Real>();
+    n.mt_s2 = c->mt_s2.as<Real>();
+    n.ev_bead = c->ev_bead.as<int4>();
+    n.ev_k = c->ev_k.as<Real>();
+    n.ev_la = c->ev_la.as<Real>();
+    n.ev_lb = c->ev_lb.as<Real>();
+    n.bb_bead = c->bbuild.bead.as<int>();
+    n.bb_plane = c->bbuild.plane.as<int>();
+    n.planes = c->planes.as<double>();
+    n.bb_k = c->bb_k.as<Real>();
+    n.bb_slen = c->bb_slen.as<Real>();
+    n.n_stiles = c->n_stiles;
+    n.stile = c->stile.as<Tile>();
+    n.stile_kind = c->stile_kind.as<int>();
+    for (int k = 0; k < K_NUM_SPARSE; ++k) n.sp_tiles[k] = c->sp_tiles[k];
+    n.contrib = c->contrib.as<Real>();
+    for (int k = 0; k <= K_NUM_SPARSE; ++k) n.slot_base[k] = c->slot_base[k];
+    n.csr_off = c->cb.off.as<int>();
+    n.csr_slot = c->cb.slots.as<int>();
+    n.lk_sf = c->lk_sf.as<double>();
+    n.mt_sf = c->mt_sf.as<double>();
+    n.ev_fb_count = c->ev_fb_count.as<int>();
+    n.ev_fb_list = c->ev_fb_list.as<int>();
+    n.ev_fb_energy = c->ev_fb_energy.as<double>();
+    n.fb_moments = c->fb_moments.as<double>();
+    n.fb_tickets = c->fb_tickets.as<int>();
+    n.part_fil = c->part_fil.as<double>();
+    n.part_sp = c->part_sp.as<double>();
+    n.st = c->st.as<CGState>();
+    n.rt = c->rt.as<RepTiles>();
+    n.ticket = c->ticket.as<int>();
+    n.gticket = c->gticket.as<int>();
+    n.err = c->err.as<unsigned>();
+    return n;
+}
+
+// Precision-typed upload of a double vector.
+int upload_real(MechContext* c, DeviceBuffer& b, const std::vector<double>& v) {
+    if (c->precision == MECH_PREC_FP64) return upload(b, v, c->stream);
+    std::vector<float> w(v.begin(), v.end());
+    return upload(b, w, c->stream);
+}
+
+size_t real_size(const MechContext* c) { return c->precision == MECH_PREC_FP64 ? 8 : 4; }
+
+// Fill the per-interaction boundary constants and the exvol interaction
+// arrays after a rebuild.
+template <typename Real>
+__global__ void k_ev_build(const int2* pairs, long long P, const int* cyl_b1, const double* kex, const int* type,
+                           const double* l0, int4* ev_bead, Real* ev_k, Real* ev_la, Real* ev_lb) {
+    const long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= P) return;
+    const int2 pr = pairs[i];
+    const int bc = cyl_b1[pr.x], bn = cyl_b1[pr.y];
+    ev_bead[i] = make_int4(bc, bc + 1, bn, bn + 1);
+    // VolumeK of the cylinder, the larger of the two for mixed types (CylinderExclVolume.cpp:113-121)
+    const double k = type[pr.x] == type[pr.y] ? kex[pr.x] : fmax(kex[pr.x], kex[pr.y]);
+    ev_k[i] = (Real)k;
+    ev_la[i] = (Real)l0[pr.x];
+    ev_lb[i] = (Real)l0[pr.y];
+}
+
+template <typename Real>
+__global__ void k_bb_build(const int* bb_plane, long long n, const double* pk, const double* ps, Real* bk, Real* bs) {
+    const long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    bk[i] = (Real)pk[bb_plane[i]];
+    bs[i] = (Real)ps[bb_plane[i]];
+}
+
+__global__ void k_gather_i32(const int* src, const long long* idx, int n, long long* out) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < n) out[i] = src[idx[i]];
+}
+
+// caller order <-> internal order of one replica's coordinates / forces
+__global__ void k_scatter_coords(const double* in, const int* perm, int nb, int base, double* out) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= nb) return;
+    const int j = base + perm[i];
+    out[3 * (size_t)j] = in[3 * (size_t)i];
+    out[3 * (size_t)j + 1] = in[3 * (size_t)i + 1];
+    out[3 * (size_t)j + 2] = in[3 * (size_t)i + 2];
+}
+
+template <typename Real>
+__global__ void k_gather_coords(const Real* in, const int* perm, int nb, int base, double* out) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= nb) return;
+    const int j = base + perm[i];
+    out[3 * (size_t)i] = (double)in[3 * (size_t)j];
+    out[3 * (size_t)i + 1] = (double)in[3 * (size_t)j + 1];
+    out[3 * (size_t)i + 2] = (double)in[3 * (size_t)j + 2];
+}
+
+__global__ void k_cg_init(CGState* st, int R) {
+    const int r = blockIdx.x * blockDim.x + threadIdx.x;
+    if (r >= R) return;
+    CGState& S = st[r];
+    if (!S.active) return;
+    S.numEnergyCall = 1;
+    S.numForceCall = 1;
+    S.prevEnergy = S.eval[MECH_NUM_FF];   // energiesBefore.total
+    if (!isfinite(S.maxF)) {
+        S.status = MECH_ERR_NONFINITE;
+        S.phase = PH_ERROR;
+        return;
+    }
+    S.phase = PH_RESET;                   // resetCGParams, then the loop head
+}
+
+int ensure_perm_buffer(MechContext* c, int r, DeviceBuffer& buf) {
+    const ReplicaHost& h = c->reps[r];
+    return upload(buf, h.perm, c->stream);
+}
+
+}  // namespace
+
+// ===========================================================================
+// network upload
+// ===========================================================================
+static int set_networks(MechContext* c, int R, const MechNetwork* nets) {
+    if (R <= 0 || !nets) return set_err(MECH_ERR_ARG, "no networks");
+    c->reps.assign(R, ReplicaHost());
+    c->R = R;
+    int nb = 0, ncyl = 0, nlk = 0, nmt = 0, npl = 0;
+    std::vector<double> x, kstr, l0b, kbend, t0, cyl_kex, cyl_l0, lkk, lkl, lks1, lks2, mtk, mtl, mts1, mts2, planes,
+        pk, ps;
+    std::vector<uint8_t> flags, minus;
+    std::vector<int> cyl_b1, cyl_fil, cyl_pos, cyl_rep, cyl_type;
+    std::vector<int64_t> cyl_id;
+    std::vector<int4> lkb, mtb;
+    c->cyl_local_first.clear();
+    for (int r = 0; r < R; ++r) {
+        const MechNetwork& N = nets[r];
+        ReplicaHost& h = c->reps[r];
+        if (N.n_beads <= 0 || !N.coord || N.n_filaments <= 0 || !N.fil_cyl_start || N.n_cylinders <= 0 || !N.cyl_bead)
+            return set_err(MECH_ERR_ARG, "replica " + std::to_string(r) + ": empty network");
+        if (N.fil_cyl_start[0] != 0 || N.fil_cyl_start[N.n_filaments] != N.n_cylinders)
+            return set_err(MECH_ERR_ARG, "fil_cyl_start does not cover the cylinders");
+        h.nb = N.n_beads;
+        h.bead_begin = nb;
+        h.ncyl = N.n_cylinders;
+        h.cyl_begin = ncyl;
+        h.nfil = N.n_filaments;
+        h.perm.assign(N.n_beads, -1);
+        h.inv.assign(N.n_beads, -1);
+        for (int k = 0; k < 3; ++k) h.box[k] = N.box[k];
+        h.rmax = N.exvol_cutoff;
+        h.bcut = N.boundary_cutoff;
+        // internal bead order: filament by filament, minus end first
+        int li = 0;
+        std::vector<int> first_local(N.n_cylinders, -1);
+        for (int f = 0; f < N.n_filaments; ++f) {
+            const int cs = N.fil_cyl_start[f], ce = N.fil_cyl_start[f + 1];
+            if (ce <= cs) return set_err(MECH_ERR_TOPOLOGY, "filament without cylinders");
+            for (int cc = cs; cc < ce; ++cc) {
+                const int b1 = N.cyl_bead[2 * cc], b2 = N.cyl_bead[2 * cc + 1];
+                if (b1 < 0 || b2 < 0 || b1 >= N.n_beads || b2 >= N.n_beads)
+                    return set_err(MECH_ERR_ARG, "cylinder bead out of range");
+                if (cc == cs) {
+                    if (h.perm[b1] != -1) return set_err(MECH_ERR_TOPOLOGY, "bead shared between filaments");
+                    h.perm[b1] = li;
+                    h.inv[li] = b1;
+                    ++li;
+                } else if (N.cyl_bead[2 * (cc - 1) + 1] != b1) {
+                    return set_err(MECH_ERR_TOPOLOGY, "cylinders of a filament do not chain");
+                }
+                first_local[cc] = li - 1;
+                if (h.perm[b2] != -1) return set_err(MECH_ERR_TOPOLOGY, "bead used twice");
+                h.perm[b2] = li;
+                h.inv[li] = b2;
+                ++li;
+            }
+        }
+        if (li != N.n_beads) return set_err(MECH_ERR_TOPOLOGY, "beads outside filaments");
+        // bead arrays in internal order
+        const size_t xoff = x.size();
+        x.resize(xoff + 3 * (size_t)N.n_beads);
+        flags.resize(nb + N.n_beads, 0);
+        kstr.resize(nb + N.n_beads, 0.0);
+        l0b.resize(nb + N.n_beads, 0.0);
+        kbend.resize(nb + N.n_beads, 0.0);
+        t0.resize(nb + N.n_beads, 0.0);
+        for (int b = 0; b < N.n_beads; ++b)
+            for (int k = 0; k < 3; ++k) x[xoff + 3 * (size_t)h.perm[b] + k] = N.coord[3 * (size_t)b + k];
+        for (int f = 0; f < N.n_filaments; ++f) {
+            const int cs = N.fil_cyl_start[f], ce = N.fil_cyl_start[f + 1];
+            for (int cc = cs; cc < ce; ++cc) {
+                const int j = nb + first_local[cc];   // slot of the cylinder's first bead
+                flags[j] |= 1;
+                flags[j + 1] |= 2;
+                kstr[j] = N.cyl_k_stretch[cc];
+                l0b[j] = N.cyl_eq_length[cc];
+                // the bending triple centred on j uses the constants of cylinder (j, j+1)
+                kbend[j] = N.cyl_k_bend[cc];
+                t0[j] = N.cyl_eq_theta ? N.cyl_eq_theta[cc] : 0.0;
+            }
+        }
+        for (int cc = 0; cc < N.n_cylinders; ++cc) {
+            cyl_b1.push_back(nb + first_local[cc]);
+            cyl_id.push_back(N.cyl_id[cc]);
+            cyl_fil.push_back(N.cyl_filament_id[cc]);
+            cyl_pos.push_back(N.cyl_position[cc]);
+            cyl_rep.push_back(r);
+            cyl_type.push_back(N.cyl_type ? N.cyl_type[cc] : 0);
+            cyl_kex.push_back(N.cyl_k_exvol[cc]);
+            cyl_l0.push_back(N.cyl_eq_length[cc]);
+            c->cyl_local_first.push_back(nb + first_local[cc]);
+        }
+        minus.resize(ncyl + N.n_cylinders, 0);
+        for (int f = 0; f < N.n_filaments; ++f) minus[ncyl + N.fil_cyl_start[f]] = 1;
+        // linkers / motors
+        auto bonds = [&](int n, const int32_t* cyl, const double* pos, const double* k, const double* eql,
+                         std::vector<int4>& bead, std::vector<double>& kk, std::vector<double>& ll,
+                         std::vector<double>& s1, std::vector<double>& s2) -> int {
+            for (int i = 0; i < n; ++i) {
+                const int c1 = cyl[2 * i], c2 = cyl[2 * i + 1];
+                if (c1 < 0 || c2 < 0 || c1 >= N.n_cylinders || c2 >= N.n_cylinders) return MECH_ERR_ARG;
+                const int a = nb + first_local[c1], b = nb + first_local[c2];
+                bead.push_back(make_int4(a, a + 1, b, b + 1));
+                kk.push_back(k[i]);
+                ll.push_back(eql[i]);
+                s1.push_back(pos[2 * i]);
+                s2.push_back(pos[2 * i + 1]);
+            }
+            return MECH_OK;
+        };
+        h.lk_begin = nlk;
+        h.nlk = N.n_linkers;
+        if (N.n_linkers > 0 && bonds(N.n_linkers, N.lk_cyl, N.lk_pos, N.lk_k, N.lk_eq_length, lkb, lkk, lkl, lks1, lks2))
+            return set_err(MECH_ERR_ARG, "linker cylinder out of range");
+        h.mt_begin = nmt;
+        h.nmt = N.n_motors;
+        if (N.n_motors > 0 && bonds(N.n_motors, N.mt_cyl, N.mt_pos, N.mt_k, N.mt_eq_length, mtb, mtk, mtl, mts1, mts2))
+            return set_err(MECH_ERR_ARG, "motor cylinder out of range");
+        h.plane_begin = npl;
+        h.nplanes = N.n_planes;
+        for (int p = 0; p < N.n_planes; ++p) {
+            for (int k = 0; k < 4; ++k) planes.push_back(N.planes[4 * p + k]);
+            pk.push_back(N.plane_k[p]);
+            ps.push_back(N.plane_screen[p]);
+        }
+        nb += N.n_beads;
+        ncyl += N.n_cylinders;
+        nlk += N.n_linkers;
+        nmt += N.n_motors;
+        npl += N.n_planes;
+    }
+    c->nb = nb;
+    c->ncyl = ncyl;
+    c->nlk = nlk;
+    c->nmt = nmt;
+    c->nplanes = npl;
+    cudaStream_t s = c->stream;
+    const size_t rs = real_size(c);
+    int rc;
+    if ((rc = upload(c->x[0], x, s))) return rc;
+    CU(c->x[1].ensure(sizeof(double) * x.size()));
+    CU(cudaMemcpyAsync(c->x[1].p, c->x[0].p, sizeof(double) * x.size(), cudaMemcpyDeviceToDevice, s));
+    CU(c->xbest.ensure(sizeof(double) * x.size()));
+    CU(c->f[0].ensure(rs * x.size()));
+    CU(c->f[1].ensure(rs * x.size()));
+    CU(c->d.ensure(rs * x.size()));
+    CU(cudaMemsetAsync(c->f[0].p, 0, rs * x.size(), s));
+    CU(cudaMemsetAsync(c->f[1].p, 0, rs * x.size(), s));
+    CU(cudaMemsetAsync(c->d.p, 0, rs * x.size(), s));
+    if ((rc = upload(c->bflag, flags, s))) return rc;
+    if ((rc = upload_real(c, c->kstr, kstr)) || (rc = upload_real(c, c->l0, l0b)) || (rc = upload_real(c, c->kbend, kbend)) ||
+        (rc = upload_real(c, c->t0, t0)))
+        return rc;
+    if ((rc = upload(c->cyl_b1, cyl_b1, s)) || (rc = upload(c->cyl_id, cyl_id, s)) || (rc = upload(c->cyl_fil, cyl_fil, s)) ||
+        (rc = upload(c->cyl_pos, cyl_pos, s)) || (rc = upload(c->cyl_rep, cyl_rep, s)) || (rc = upload(c->cyl_type, cyl_type, s)) ||
+        (rc = upload(c->cyl_kex, cyl_kex, s)) || (rc = upload(c->cyl_l0, cyl_l0, s)) || (rc = upload(c->cyl_minus, minus, s)))
+        return rc;
+    if ((rc = upload(c->lk_bead, lkb, s)) || (rc = upload_real(c, c->lk_k, lkk)) || (rc = upload_real(c, c->lk_l0, lkl)) ||
+        (rc = upload_real(c, c->lk_s1, lks1)) || (rc = upload_real(c, c->lk_s2, lks2)))
+        return rc;
+    if ((rc = upload(c->mt_bead, mtb, s)) || (rc = upload_real(c, c->mt_k, mtk)) || (rc = upload_real(c, c->mt_l0, mtl)) ||
+        (rc = upload_real(c, c->mt_s1, mts1)) || (rc = upload_real(c, c->mt_s2, mts2)))
+        return rc;
+    CU(c->lk_sf.ensure(sizeof(double) * std::max(nlk, 1)));
+    CU(c->mt_sf.ensure(sizeof(double) * std::max(nmt, 1)));
+    if ((rc = upload(c->planes, planes, s)) || (rc = upload(c->plane_k, pk, s)) || (rc = upload(c->plane_slen, ps, s)))
+        return rc;
+    // filament tiles (static)
+    std::vector<Tile> ft;
+    c->h_rt.assign(R, RepTiles{});
+    for (int r = 0; r < R; ++r) {
+        const ReplicaHost& h = c->reps[r];
+        c->h_rt[r].fil_begin = (int)ft.size();
+        for (int b = 0; b < h.nb; b += kFilTile)
+            ft.push_back(Tile{r, h.bead_begin + b, h.bead_begin + std::min(h.nb, b + kFilTile), 0});
+        c->h_rt[r].fil_end = (int)ft.size();
+    }
+    c->n_ftiles = (int)ft.size();
+    if ((rc = upload(c->ftile, ft, s))) return rc;
+    CU(c->part_fil.ensure(sizeof(double) * 4 * ft.size()));
+    // states
+    CU(c->st.ensure(sizeof(CGState) * R));
+    CU(cudaMemsetAsync(c->st.p, 0, sizeof(CGState) * R, s));
+    CU(c->ticket.ensure(sizeof(int) * R));
+    CU(cudaMemsetAsync(c->ticket.p, 0, sizeof(int) * R, s));
+    CU(c->gticket.ensure(sizeof(int) * 4));
+    CU(cudaMemsetAsync(c->gticket.p, 0, sizeof(int) * 4, s));
+    CU(c->err.ensure(sizeof(unsigned) * 4));
+    CU(cudaMemsetAsync(c->err.p, 0, sizeof(unsigned) * 4, s));
+    CU(c->ev_fb_count.ensure(sizeof(int) * 4));
+    CU(cudaMemsetAsync(c->ev_fb_count.p, 0, sizeof(int) * 4, s));
+    CU(c->ev_fb_list.ensure(sizeof(int) * 2 * kExvolFallbackCap));
+    CU(c->ev_fb_energy.ensure(sizeof(double) * 2 * kExvolFallbackCap));
+    CU(c->fb_moments.ensure(sizeof(double) * 6 * kFbChunks * (size_t)kExvolFallbackCap));
+    CU(c->fb_tickets.ensure(sizeof(int) * kExvolFallbackCap));
+    CU(cudaMemsetAsync(c->fb_tickets.p, 0, sizeof(int) * kExvolFallbackCap, s));
+    if (c->h_st) cudaFreeHost(c->h_st);
+    CU(cudaMallocHost(&c->h_st, sizeof(CGState) * R));
+    if (!c->h_err) CU(cudaMallocHost(&c->h_err, sizeof(unsigned) * 4));
+    CU(cudaStreamSynchronize(s));
+    c->have_net = true;
+    c->have_lists = false;
+    return MECH_OK;
+}
+
+// ===========================================================================
+// neighbor lists
+// ===========================================================================
+static int rebuild(MechContext* c, double cell_req, MechListInfo* info) {
+    if (!c->have_net) return set_err(MECH_ERR_STATE, "no network");
+    cudaStream_t s = c->stream;
+    const int R = c->R;
+    // per replica grid
+    std::vector<double> rcell(R), rmax2(R), rmin2(R), bcut(R);
+    std::vector<int4> dims(R);
+    std::vector<float> margin(R);
+    long long ncells = 0;
+    for (int r = 0; r < R; ++r) {
+        ReplicaHost& h = c->reps[r];
+        double cell = cell_req;
+        const double vol = std::max(1.0, h.box[0] * h.box[1] * h.box[2]);
+        if (cell <= 0) {
+            // about half a cylinder per cell; never below the reference's 1.125 rMax
+            cell = std::max(1.125 * h.rmax, std::cbrt(vol / std::max(1, h.ncyl)) * 0.7937);
+        }
+        cell = std::max(cell, h.rmax);
+        auto g = [&](double L) { return std::max(1, (int)std::ceil(std::max(L, cell) / cell)); };
+        h.gx = g(h.box[0]);
+        h.gy = g(h.box[1]);
+        h.gz = g(h.box[2]);
+        // keep the cell array bounded: grow the edge until cells <= 8 * cylinders + 4096
+        while ((long long)h.gx * h.gy * h.gz > 8LL * h.ncyl + 4096) {
+            cell *= 1.25;
+            h.gx = g(h.box[0]);
+            h.gy = g(h.box[1]);
+            h.gz = g(h.box[2]);
+        }
+        h.cell = cell;
+        h.cell_off = ncells;
+        ncells += (long long)h.gx * h.gy * h.gz;
+        rcell[r] = cell;
+        dims[r] = make_int4(h.gx, h.gy, h.gz, (int)h.cell_off);
+        rmax2[r] = (double)(float)(h.rmax * h.rmax);
+        rmin2[r] = 0.0;
+        bcut[r] = h.bcut;
+        // float-midpoint prefilter slack (coordinates up to a few boxes from the origin)
+        const double M = 4.0 * std::max(h.box[0], std::max(h.box[1], h.box[2])) + 1e4;
+        const double delta = (2.0 * M + h.rmax) * 6.0e-8;
+        margin[r] = (float)(2.0 * h.rmax * std::sqrt(3.0) * delta + 3.0 * delta * delta + 4e-7 * h.rmax * h.rmax + 1e-2);
+    }
+    if (ncells > 2000000000LL) return set_err(MECH_ERR_CAPACITY, "bin grid too large");
+    int rc;
+    if ((rc = upload(c->rep_cell, rcell, s)) || (rc = upload(c->rep_dims, dims, s)) || (rc = upload(c->rep_rmax2, rmax2, s)) ||
+        (rc = upload(c->rep_rmin2, rmin2, s)) || (rc = upload(c->rep_margin, margin, s)) || (rc = upload(c->rep_bcut, bcut, s)))
+        return rc;
+    NLInput in{};
+    in.ncyl = c->ncyl;
+    in.cyl_b1 = c->cyl_b1.as<int>();
+    in.cyl_id = c->cyl_id.as<int64_t>();
+    in.cyl_fil = c->cyl_fil.as<int>();
+    in.cyl_pos = c->cyl_pos.as<int>();
+    in.cyl_rep = c->cyl_rep.as<int>();
+    // current coordinates: replica buffers may differ; gather them into x[0] first
+    in.x = nullptr;
+    in.rep_cell = c->rep_cell.as<double>();
+    in.rep_dims = c->rep_dims.as<int4>();
+    in.rep_rmax2 = c->rep_rmax2.as<double>();
+    in.rep_rmin2 = c->rep_rmin2.as<double>();
+    in.R = R;
+    in.ncells = ncells;
+    // Current coordinates live in x[xbuf] per replica; canonicalize them to
+    // x[0] (and reset xbuf) so the lists read one array.
+    CU(cudaMemcpyAsync(c->h_st, c->st.p, sizeof(CGState) * R, cudaMemcpyDeviceToHost, s));
+    CU(cudaStreamSynchronize(s));
+    bool moved = false;
+    for (int r = 0; r < R; ++r) {
+        if (c->h_st[r].xbuf) {
+            const ReplicaHost& h = c->reps[r];
+            CU(cudaMemcpyAsync(c->x[0].as<double>() + 3 * (size_t)h.bead_begin, c->x[1].as<double>() + 3 * (size_t)h.bead_begin,
+                               sizeof(double) * 3 * h.nb, cudaMemcpyDeviceToDevice, s));
+            c->h_st[r].xbuf = 0;
+            moved = true;
+        }
+    }
+    if (moved) CU(cudaMemcpyAsync(c->st.p, c->h_st, sizeof(CGState) * R, cudaMemcpyHostToDevice, s));
+    in.x = c->x[0].as<double>();
+    long long P = 0;
+    CU(build_pairs(in, c->pb, c->rep_margin.as<float>(), &P, s));
+    c->nev = P;
+    // per replica pair ranges: pair offsets at the replicas' first cylinders
+    {
+        std::vector<long long> idx(R + 1);
+        for (int r = 0; r < R; ++r) idx[r] = c->reps[r].cyl_begin;
+        idx[R] = c->ncyl;
+        if ((rc = upload(c->gather_idx, idx, s))) return rc;
+        CU(c->gather_out.ensure(sizeof(long long) * (R + 1)));
+        k_gather_i32<<<(R + 1 + 127) / 128, 128, 0, s>>>(c->pb.off.as<int>(), c->gather_idx.as<long long>(), R + 1,
+                                                      c->gather_out.as<long long>());
+        std::vector<long long> o(R + 1);
+        CU(cudaMemcpyAsync(o.data(), c->gather_out.p, sizeof(long long) * (R + 1), cudaMemcpyDeviceToHost, s));
+        CU(cudaStreamSynchronize(s));
+        for (int r = 0; r < R; ++r) {
+            c->reps[r].ev_begin = o[r];
+            c->reps[r].nev = o[r + 1] - o[r];
+        }
+    }
+    const size_t rs = real_size(c);
+    CU(c->ev_bead.ensure(sizeof(int4) * std::max<long long>(P, 1)));
+    CU(c->ev_k.ensure(rs * std::max<long long>(P, 1)));
+    CU(c->ev_la.ensure(rs * std::max<long long>(P, 1)));
+    CU(c->ev_lb.ensure(rs * std::max<long long>(P, 1)));
+    if (P > 0) {
+        const unsigned nbk = (unsigned)((P + 255) / 256);
+        if (c->precision == MECH_PREC_FP64)
+            k_ev_build<double><<<nbk, 256, 0, s>>>(c->pb.pairs.as<int2>(), P, c->cyl_b1.as<int>(), c->cyl_kex.as<double>(),
+                                                   c->cyl_type.as<int>(), c->cyl_l0.as<double>(), c->ev_bead.as<int4>(),
+                                                   c->ev_k.as<double>(), c->ev_la.as<double>(), c->ev_lb.as<double>());
+        else
+            k_ev_build<float><<<nbk, 256, 0, s>>>(c->pb.pairs.as<int2>(), P, c->cyl_b1.as<int>(), c->cyl_kex.as<double>(),
+                                                  c->cyl_type.as<int>(), c->cyl_l0.as<double>(), c->ev_bead.as<int4>(),
+                                                  c->ev_k.as<float>(), c->ev_la.as<float>(), c->ev_lb.as<float>());
+    }
+    // boundary lists
+    {
+        std::vector<long long> rq(R);
+        std::vector<int> rnc(R), rpl(R), rcy(R);
+        long long nq = 0;
+        for (int r = 0; r < R; ++r) {
+            rq[r] = nq;
+            rnc[r] = c->reps[r].ncyl;
+            rpl[r] = c->reps[r].plane_begin;
+            rcy[r] = c->reps[r].cyl_begin;
+            nq += (long long)c->reps[r].nplanes * c->reps[r].ncyl;
+        }
+        if ((rc = upload(c->rep_q, rq, s)) || (rc = upload(c->rep_ncyl, rnc, s)) || (rc = upload(c->rep_plane, rpl, s)) ||
+            (rc = upload(c->rep_cyl, rcy, s)))
+            return rc;
+        BndInput bi{};
+        bi.nq = nq;
+        bi.R = R;
+        bi.rep_q = c->rep_q.as<long long>();
+        bi.rep_ncyl = c->rep_ncyl.as<int>();
+        bi.rep_plane = c->rep_plane.as<int>();
+        bi.rep_cyl = c->rep_cyl.as<int>();
+        bi.cutoff = c->rep_bcut.as<double>();
+        bi.planes = c->planes.as<double>();
+        bi.cyl_b1 = c->cyl_b1.as<int>();
+        bi.cyl_minus = c->cyl_minus.as<uint8_t>();
+        long long nbb = 0;
+        CU(build_boundary(bi, c->pb.mid.as<double>(), c->bbuild, &nbb, s));
+        c->nbb = nbb;
+        std::vector<long long> idx(R + 1);
+        for (int r = 0; r < R; ++r) idx[r] = rq[r];
+        idx[R] = nq;
+        if ((rc = upload(c->gather_idx, idx, s))) return rc;
+        k_gather_i32<<<(R + 1 + 127) / 128, 128, 0, s>>>(c->bbuild.off.as<int>(), c->gather_idx.as<long long>(), R + 1,
+                                                      c->gather_out.as<long long>());
+        std::vector<long long> o(R + 1);
+        CU(cudaMemcpyAsync(o.data(), c->gather_out.p, sizeof(long long) * (R + 1), cudaMemcpyDeviceToHost, s));
+        CU(cudaStreamSynchronize(s));
+        for (int r = 0; r < R; ++r) {
+            c->reps[r].bb_begin = o[r];
+            c->reps[r].nbb = o[r + 1] - o[r];
+        }
+        CU(c->bb_k.ensure(rs * std::max<long long>(nbb, 1)));
+        CU(c->bb_slen.ensure(rs * std::max<long long>(nbb, 1)));
+        if (nbb > 0) {
+            const unsigned nbk = (unsigned)((nbb + 255) / 256);
+            if (c->precision == MECH_PREC_FP64)
+                k_bb_build<double><<<nbk, 256, 0, s>>>(c->bbuild.plane.as<int>(), nbb, c->plane_k.as<double>(),
+                                                       c->plane_slen.as<double>(), c->bb_k.as<double>(), c->bb_slen.as<double>());
+            else
+                k_bb_build<float><<<nbk, 256, 0, s>>>(c->bbuild.plane.as<int>(), nbb, c->plane_k.as<double>(),
+                                                      c->plane_slen.as<double>(), c->bb_k.as<float>(), c->bb_slen.as<float>());
+        }
+    }
+    // sparse tiles: linker, motor, exvol, boundary; each replica's interactions tiled separately
+    {
+        std::vector<Tile> st;
+        std::vector<int> kind;
+        for (int k = 0; k < K_NUM_SPARSE; ++k) {
+            const int t0 = (int)st.size();
+            for (int r = 0; r < R; ++r) {
+                const ReplicaHost& h = c->reps[r];
+                long long b = 0, n = 0;
+                if (k == K_LINKER) { b = h.lk_begin; n = h.nlk; }
+                if (k == K_MOTOR) { b = h.mt_begin; n = h.nmt; }
+                if (k == K_EXVOL) { b = h.ev_begin; n = h.nev; }
+                if (k == K_BOUNDARY) { b = h.bb_begin; n = h.nbb; }
+                c->h_rt[r].sp_begin[k] = (int)st.size();
+                for (long long i = 0; i < n; i += kSparseTile) {
+                    st.push_back(Tile{r, (int)(b + i), (int)(b + std::min<long long>(n, i + kSparseTile)), 0});
+                    kind.push_back(k);
+                }
+                c->h_rt[r].sp_end[k] = (int)st.size();
+            }
+            c->sp_tiles[k] = (int)st.size() - t0;
+        }
+        c->n_stiles = (int)st.size();
+        if ((rc = upload(c->stile, st, s)) || (rc = upload(c->stile_kind, kind, s)) || (rc = upload(c->rt, c->h_rt, s)))
+            return rc;
+        CU(c->part_sp.ensure(sizeof(double) * std::max<size_t>(st.size(), 1)));
+    }
+    // contribution slots and the gather index
+    c->slot_base[K_LINKER] = 0;
+    c->slot_base[K_MOTOR] = 4 * c->nlk;
+    c->slot_base[K_EXVOL] = 4 * c->nlk + 4 * c->nmt;
+    c->slot_base[K_BOUNDARY] = (int)(c->slot_base[K_EXVOL] + 4 * P);
+    c->slot_base[K_NUM_SPARSE] = (int)(c->slot_base[K_BOUNDARY] + c->nbb);
+    CU(c->contrib.ensure(rs * 3 * std::max(1, c->slot_base[K_NUM_SPARSE])));
+    CU(cudaMemsetAsync(c->contrib.p, 0, rs * 3 * std::max(1, c->slot_base[K_NUM_SPARSE]), s));
+    {
+        CsrInput ci{};
+        ci.nb = c->nb;
+        for (int k = 0; k <= K_NUM_SPARSE; ++k) ci.base[k] = c->slot_base[k];
+        ci.lk = c->lk_bead.as<int4>();
+        ci.mt = c->mt_bead.as<int4>();
+        ci.ev = c->ev_bead.as<int4>();
+        ci.bb = c->bbuild.bead.as<int>();
+        CU(build_csr(ci, c->cb, s));
+    }
+    CU(cudaStreamSynchronize(s));
+    CU(cudaGetLastError());
+    c->have_lists = true;
+    if (info) {
+        info->n_exvol_pairs = P;
+        info->n_boundary_beads = c->nbb;
+        info->n_boundary_cyl = 0;
+        info->cell_size = c->reps[0].cell;
+        info->n_cells = ncells;
+    }
+    return MECH_OK;
+}
+
+// ===========================================================================
+// evaluation and minimization
+// ===========================================================================
+static int pull_states(MechContext* c) {
+    CU(cudaMemcpyAsync(c->h_st, c->st.p, sizeof(CGState) * c->R, cudaMemcpyDeviceToHost, c->stream));
+    CU(cudaMemcpyAsync(c->h_err, c->err.p, sizeof(unsigned), cudaMemcpyDeviceToHost, c->stream));
+    CU(cudaStreamSynchronize(c->stream));
+    return MECH_OK;
+}
+static int push_states(MechContext* c) {
+    CU(cudaMemcpyAsync(c->st.p, c->h_st, sizeof(CGState) * c->R, cudaMemcpyHostToDevice, c->stream));
+    return MECH_OK;
+}
+
+template <typename Real>
+static int eval_energy(MechContext* c, int replica) {
+    int rc;
+    if ((rc = pull_states(c))) return rc;
+    for (int r = 0; r < c->R; ++r) c->h_st[r].active = (replica < 0 || r == replica);
+    if ((rc = push_states(c))) return rc;
+    const DevNet<Real> n = make_devnet<Real>(c);
+    c->timing.launches += launch_energy<Real>(n, -1, 0, c->stream);
+    CU(cudaGetLastError());
+    return pull_states(c);
+}
+
+template <typename Real>
+static int eval_forces(MechContext* c, int replica) {
+    int rc;
+    if ((rc = pull_states(c))) return rc;
+    for (int r = 0; r < c->R; ++r) c->h_st[r].active = (replica < 0 || r == replica);
+    if ((rc = push_states(c))) return rc;
+    const DevNet<Real> n = make_devnet<Real>(c);
+    c->timing.launches += launch_forces<Real>(n, -1, c->stream);
+    CU(cudaGetLastError());
+    return pull_states(c);
+}
+
+static constexpr int kBlocksPerGraph = 8;
+static constexpr int kTrialsPerBlock = 2;
+
+template <typename Real>
+static int capture_iteration_graph(MechContext* c, cudaGraphExec_t* exec, int* nlaunch) {
+    const DevNet<Real> n = make_devnet<Real>(c);
+    cudaGraph_t g = nullptr;
+    CU(cudaStreamBeginCapture(c->stream, cudaStreamCaptureModeThreadLocal));
+    int k = 0;
+    for (int b = 0; b < kBlocksPerGraph; ++b) {
+        for (int t = 0; t < kTrialsPerBlock; ++t) k += launch_energy<Real>(n, PH_LS_TRIAL, 1, c->stream);
+        k += launch_forces<Real>(n, PH_FORCE, c->stream);
+        k += launch_direction<Real>(n, c->stream);
+        k += launch_dispatch_failed<Real>(n, c->stream);
+        k += launch_reset<Real>(n, c->stream);
+    }
+    cudaError_t e = cudaStreamEndCapture(c->stream, &g);
+    if (e != cudaSuccess) return set_err(MECH_ERR_CUDA, std::string("graph capture: ") + cudaGetErrorString(e));
+    e = cudaGraphInstantiate(exec, g, 0);
+    cudaGraphDestroy(g);
+    if (e != cudaSuccess) return set_err(MECH_ERR_CUDA, std::string("graph instantiate: ") + cudaGetErrorString(e));
+    *nlaunch = k;
+    return MECH_OK;
+}
+
+template <typename Real>
+static int minimize_impl(MechContext* c, const MechCGParams* p, MechResult* res) {
+    if (!c->have_lists) {
+        int rc = rebuild(c, 0.0, nullptr);
+        if (rc) return rc;
+    }
+    auto t_start = std::chrono::steady_clock::now();
+    cudaStream_t s = c->stream;
+    int rc;
+    if ((rc = pull_states(c))) return rc;
+    for (int r = 0; r < c->R; ++r) {
+        CGState& S = c->h_st[r];
+        const int xb = S.xbuf, fb = S.fbuf;
+        std::memset(&S, 0, sizeof(S));
+        S.xbuf = xb;
+        S.fbuf = fb;
+        S.method = p->method;
+        S.maxDist = p->max_dist;
+        S.lambdaMax = p->lambda_max;
+        S.gradTol = p->grad_tol;
+        S.energyRelTol = p->energy_rel_tol;
+        S.energyCallLimit = p->energy_call_limit;
+        S.forceCallLimit = std::max(p->force_call_limit, 3 * c->reps[r].nb);
+        S.tryToRecover = p->try_to_recover;
+        S.minimumE = std::numeric_limits<double>::infinity();
+        S.maxF = std::numeric_limits<double>::infinity();
+        S.energyRelChange = std::numeric_limits<double>::infinity();
+        S.active = 1;
+        S.phase = PH_IDLE;
+    }
+    if ((rc = push_states(c))) return rc;
+    CU(cudaMemsetAsync(c->err.p, 0, sizeof(unsigned), s));
+    const DevNet<Real> n = make_devnet<Real>(c);
+    cudaEvent_t e0, e1;
+    CU(cudaEventCreate(&e0));
+    CU(cudaEventCreate(&e1));
+    CU(cudaEventRecord(e0, s));
+    // energiesBefore, initial forces, resetCGParams, loop head
+    long long launches = 0;
+    launches += launch_energy<Real>(n, -1, 0, s);
+    launches += launch_forces<Real>(n, -1, s);
+    k_cg_init<<<(c->R + 127) / 128, 128, 0, s>>>(n.st, c->R);
+    launches += 1 + launch_reset<Real>(n, s);
+    CU(cudaGetLastError());
+    if ((rc = pull_states(c))) return rc;
+    std::vector<std::vector<double>> before(c->R);
+    for (int r = 0; r < c->R; ++r) before[r].assign(c->h_st[r].eval, c->h_st[r].eval + MECH_NUM_FF + 1);
+    cudaGraphExec_t exec = nullptr;
+    int per_graph = 0;
+    if ((rc = capture_iteration_graph<Real>(c, &exec, &per_graph))) return rc;
+    long long graphs = 0;
+    long long max_graphs = 0;
+    for (int r = 0; r < c->R; ++r)
+        max_graphs = std::max<long long>(max_graphs, 4LL * c->h_st[r].forceCallLimit / kBlocksPerGraph + 1000);
+    int status = MECH_OK;
+    for (;;) {
+        CU(cudaGraphLaunch(exec, s));
+        ++graphs;
+        launches += per_graph;
+        if ((rc = pull_states(c))) { cudaGraphExecDestroy(exec); return rc; }
+        if (*c->h_err) {
+            status = set_err(MECH_ERR_NONFINITE, "excluded-volume numeric fallback failed");
+            break;
+        }
+        bool all_done = true, recover = false;
+        for (int r = 0; r < c->R; ++r) {
+            const int ph = c->h_st[r].phase;
+            if (ph != PH_DONE && ph != PH_ERROR) all_done = false;
+            if (ph == PH_RECOVER) recover = true;
+        }
+        if (all_done) break;
+        if (recover) {
+            launches += launch_recover<Real>(n, s);
+            CU(cudaGetLastError());
+        }
+        if (graphs > max_graphs) {
+            status = set_err(MECH_ERR_ITER_LIMIT, "minimizer loop exceeded its iteration cap");
+            break;
+        }
+    }
+    cudaGraphExecDestroy(exec);
+    // call-limit exit restores the minimum-energy backup (CGMethod.hpp:1589-1610)
+    bool restore = false;
+    for (int r = 0; r < c->R; ++r) {
+        CGState& S = c->h_st[r];
+        const bool limit = (S.energyCallLimit != 0 && S.numEnergyCall > S.energyCallLimit) ||
+                           (S.forceCallLimit != 0 && S.numForceCall > S.forceCallLimit);
+        S.restore = (p->report_on_call_limit && limit && S.backupValid) ? 1 : 0;
+        restore = restore || S.restore;
+        S.active = 1;
+    }
+    if ((rc = push_states(c))) return rc;
+    if (restore) launches += launch_backup_restore<Real>(n, s);
+    launches += launch_energy<Real>(n, -1, 0, s);   // energiesAfter
+    CU(cudaEventRecord(e1, s));
+    if ((rc = pull_states(c))) return rc;
+    float ms = 0.f;
+    cudaEventElapsedTime(&ms, e0, e1);
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    const double secs = std::chrono::duration<double>(std::chrono::steady_clock::now() - t_start).count();
+    c->timing.ms_total = ms;
+    c->timing.launches = launches;
+    c->timing.graph_launches = graphs;
+    for (int r = 0; r < c->R; ++r) {
+        const CGState& S = c->h_st[r];
+        MechResult& o = res[r];
+        std::memset(&o, 0, sizeof(o));
+        o.error_flags = (uint32_t)S.errorFlags;
+        o.status = status != MECH_OK ? status : (S.phase == PH_ERROR ? S.status : (S.errorFlags ? MECH_ERR_LINESEARCH : MECH_OK));
+        o.num_energy_call = S.numEnergyCall + 1;
+        o.energy_call_limit = S.energyCallLimit;
+        o.num_force_call = S.numForceCall;
+        o.force_call_limit = S.forceCallLimit;
+        o.num_iter = S.numIter;
+        o.num_safe_mode = S.numSafeMode;
+        o.num_recover = S.numRecover;
+        o.num_line_search_trials = S.numTrials;
+        o.num_energy_eval = S.numEnergyEval;
+        o.used_backup = S.restore;
+        o.grad_inf_norm = S.maxF;
+        o.grad_tol = S.gradTol;
+        o.energy_rel_change = S.energyRelChange;
+        o.energy_rel_tol = S.energyRelTol;
+        for (int k = 0; k <= MECH_NUM_FF; ++k) {
+            o.energies_before[k] = before[r][k];
+            o.energies_after[k] = S.eval[k];
+        }
+        o.seconds = secs;
+    }
+    return status;
+}
+
+// ===========================================================================
+// C ABI
+// ===========================================================================
+extern "C" {
+
+int32_t mech_abi_version(void) { return MECH_ABI_VERSION; }
+const char* mech_last_error(void) { return g_last_error.c_str(); }
+
+int32_t mech_ctx_create(int32_t precision, int32_t device, MechContext** out) {
+    if (!out) return set_err(MECH_ERR_ARG, "out is null");
+    if (precision != MECH_PREC_FP64 && precision != MECH_PREC_MIXED) return set_err(MECH_ERR_ARG, "bad precision");
+    int ndev = 0;
+    if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev == 0) {
+        cudaGetLastError();
+        return set_err(MECH_ERR_NO_DEVICE, "no CUDA device");
+    }
+    if (device < 0 || device >= ndev) return set_err(MECH_ERR_ARG, "bad device");
+    CU(cudaSetDevice(device));
+    MechContext* c = new MechContext();
+    c->device = device;
+    c->precision = precision;
+    cudaError_t e = cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking);
+    if (e != cudaSuccess) {
+        delete c;
+        return set_err(MECH_ERR_CUDA, cudaGetErrorString(e));
+    }
+    *out = c;
+    return MECH_OK;
+}
+
+int32_t mech_ctx_destroy(MechContext* ctx) {
+    if (!ctx) return MECH_OK;
+    cudaSetDevice(ctx->device);
+    cudaStreamSynchronize(ctx->stream);
+    delete ctx;
+    return MECH_OK;
+}
+
+int32_t mech_set_networks(MechContext* ctx, int32_t n_replicas, const MechNetwork* nets) {
+    if (!ctx) return set_err(MECH_ERR_ARG, "null context");
+    CU(cudaSetDevice(ctx->device));
+    const int rc = set_networks(ctx, n_replicas, nets);
+    if (rc) return rc;
+    return rebuild(ctx, 0.0, nullptr);
+}
+
+static int check_replica(MechContext* ctx, int32_t r) {
+    if (!ctx) return set_err(MECH_ERR_ARG, "null context");
+    if (!ctx->have_net) return set_err(MECH_ERR_STATE, "no network");
+    if (r < 0 || r >= ctx->R) return set_err(MECH_ERR_ARG, "bad replica");
+    return MECH_OK;
+}
+
+int32_t mech_set_coords(MechContext* ctx, int32_t r, const double* coord) {
+    int rc = check_replica(ctx, r);
+    if (rc) return rc;
+    if (!coord) return set_err(MECH_ERR_ARG, "null coord");
+    CU(cudaSetDevice(ctx->device));
+    if ((rc = pull_states(ctx))) return rc;
+    const ReplicaHost& h = ctx->reps[r];
+    DeviceBuffer tmp, perm;
+    CU(tmp.ensure(sizeof(double) * 3 * h.nb));
+    CU(cudaMemcpyAsync(tmp.p, coord, sizeof(double) * 3 * h.nb, cudaMemcpyHostToDevice, ctx->stream));
+    if ((rc = ensure_perm_buffer(ctx, r, perm))) return rc;
+    double* X = ctx->x[ctx->h_st[r].xbuf].as<double>();
+    k_scatter_coords<<<(h.nb + 255) / 256, 256, 0, ctx->stream>>>(tmp.as<double>(), perm.as<int>(), h.nb, h.bead_begin, X);
+    CU(cudaGetLastError());
+    CU(cudaStreamSynchronize(ctx->stream));
+    return MECH_OK;
+}
+
+int32_t mech_get_coords(MechContext* ctx, int32_t r, double* coord) {
+    int rc = check_replica(ctx, r);
+    if (rc) return rc;
+    if (!coord) return set_err(MECH_ERR_ARG, "null coord");
+    CU(cudaSetDevice(ctx->device));
+    if ((rc = pull_states(ctx))) return rc;
+    const ReplicaHost& h = ctx->reps[r];
+    DeviceBuffer tmp, perm;
+    CU(tmp.ensure(sizeof(double) * 3 * h.nb));
+    if ((rc = ensure_perm_buffer(ctx, r, perm))) return rc;
+    const double* X = ctx->x[ctx->h_st[r].xbuf].as<double>();
+    k_gather_coords<double><<<(h.nb + 255) / 256, 256, 0, ctx->stream>>>(X, perm.as<int>(), h.nb, h.bead_begin, tmp.as<double>());
+    CU(cudaMemcpyAsync(coord, tmp.p, sizeof(double) * 3 * h.nb, cudaMemcpyDeviceToHost, ctx->stream));
+    CU(cudaStreamSynchronize(ctx->stream));
+    return MECH_OK;
+}
+
+int32_t mech_get_forces(MechContext* ctx, int32_t r, double* f_out) {
+    int rc = check_replica(ctx, r);
+    if (rc) return rc;
+    if (!f_out) return set_err(MECH_ERR_ARG, "null output");
+    CU(cudaSetDevice(ctx->device));
+    if ((rc = pull_states(ctx))) return rc;
+    const ReplicaHost& h = ctx->reps[r];
+    DeviceBuffer tmp, perm;
+    CU(tmp.ensure(sizeof(double) * 3 * h.nb));
+    if ((rc = ensure_perm_buffer(ctx, r, perm))) return rc;
+    const int fb = ctx->h_st[r].fbuf;
+    if (ctx->precision == MECH_PREC_FP64)
+        k_gather_coords<double><<<(h.nb + 255) / 256, 256, 0, ctx->stream>>>(ctx->f[fb].as<double>(), perm.as<int>(), h.nb,
+                                                                           h.bead_begin, tmp.as<double>());
+    else
+        k_gather_coords<float><<<(h.nb + 255) / 256, 256, 0, ctx->stream>>>(ctx->f[fb].as<float>(), perm.as<int>(), h.nb,
+                                                                          h.bead_begin, tmp.as<double>());
+    CU(cudaMemcpyAsync(f_out, tmp.p, sizeof(double) * 3 * h.nb, cudaMemcpyDeviceToHost, ctx->stream));
+    CU(cudaStreamSynchronize(ctx->stream));
+    return MECH_OK;
+}
+
+int32_t mech_rebuild_neighbors(MechContext* ctx, double cell_size, MechListInfo* info) {
+    if (!ctx) return set_err(MECH_ERR_ARG, "null context");
+    CU(cudaSetDevice(ctx->device));
+    return rebuild(ctx, cell_size, info);
+}
+
+int32_t mech_get_pairs(MechContext* ctx, int32_t r, int32_t* pairs, int64_t cap, int64_t* count) {
+    int rc = check_replica(ctx, r);
+    if (rc) return rc;
+    if (!ctx->have_lists) return set_err(MECH_ERR_STATE, "no lists");
+    const ReplicaHost& h = ctx->reps[r];
+    if (count) *count = h.nev;
+    const long long n = std::min<long long>(cap, h.nev);
+    if (n > 0 && pairs) {
+        CU(cudaMemcpy(pairs, ctx->pb.pairs.as<int2>() + h.ev_begin, sizeof(int2) * n, cudaMemcpyDeviceToHost));
+        for (long long i = 0; i < 2 * n; ++i) pairs[i] -= h.cyl_begin;
+    }
+    return MECH_OK;
+}
+
+int32_t mech_energy(MechContext* ctx, int32_t r, const double* coord, double* per_ff, double* total, double* energy) {
+    int rc = check_replica(ctx, r);
+    if (rc) return rc;
+    if (coord && (rc = mech_set_coords(ctx, r, coord))) return rc;
+    if (!ctx->have_lists && (rc = rebuild(ctx, 0.0, nullptr))) return rc;
+    rc = ctx->precision == MECH_PREC_FP64 ? eval_energy<double>(ctx, r) : eval_energy<float>(ctx, r);
+    if (rc) return rc;
+    const CGState& S = ctx->h_st[r];
+    if (per_ff)
+        for (int k = 0; k < MECH_NUM_FF; ++k) per_ff[k] = S.eval[k];
+    if (total) *total = S.eval[MECH_NUM_FF];
+    if (energy) *energy = S.E0;
+    return MECH_OK;
+}
+
+int32_t mech_forces(MechContext* ctx, int32_t r, const double* coord, double* f_out) {
+    int rc = check_replica(ctx, r);
+    if (rc) return rc;
+    if (coord && (rc = mech_set_coords(ctx, r, coord))) return rc;
+    if (!ctx->have_lists && (rc = rebuild(ctx, 0.0, nullptr))) return rc;
+    rc = ctx->precision == MECH_PREC_FP64 ? eval_forces<double>(ctx, r) : eval_forces<float>(ctx, r);
+    if (rc) return rc;
+    if (*ctx->h_err) return set_err(MECH_ERR_NONFINITE, "excluded-volume numeric fallback failed");
+    return f_out ? mech_get_forces(ctx, r, f_out) : MECH_OK;
+}
+
+int32_t mech_minimize(MechContext* ctx, const MechCGParams* params, MechResult* results) {
+    if (!ctx || !params || !results) return set_err(MECH_ERR_ARG, "null argument");
+    if (!ctx->have_net) return set_err(MECH_ERR_STATE, "no network");
+    if (params->method < 0 || params->method > 2) return set_err(MECH_ERR_ARG, "bad method");
+    CU(cudaSetDevice(ctx->device));
+    return ctx->precision == MECH_PREC_FP64 ? minimize_impl<double>(ctx, params, results)
+                                            : minimize_impl<float>(ctx, params, results);
+}
+
+int32_t mech_get_stretch_forces(MechContext* ctx, int32_t r, double* linker_f, double* motor_f) {
+    int rc = check_replica(ctx, r);
+    if (rc) return rc;
+    const ReplicaHost& h = ctx->reps[r];
+    if (linker_f && h.nlk > 0)
+        CU(cudaMemcpy(linker_f, ctx->lk_sf.as<double>() + h.lk_begin, sizeof(double) * h.nlk, cudaMemcpyDeviceToHost));
+    if (motor_f && h.nmt > 0)
+        CU(cudaMemcpy(motor_f, ctx->mt_sf.as<double>() + h.mt_begin, sizeof(double) * h.nmt, cudaMemcpyDeviceToHost));
+    return MECH_OK;
+}
+
+int32_t mech_get_timing(MechContext* ctx, MechTiming* t) {
+    if (!ctx || !t) return set_err(MECH_ERR_ARG, "null argument");
+    *t = ctx->timing;
+    return MECH_OK;
+}
+
+}  // extern "C"

@@ -1,0 +1,184 @@
+// Internal declarations shared by the engine's translation units.
+//
+// Layout in HBM (one context, R replica networks concatenated):
+//   beads     internal order = filament by filament, minus end first, replica
+//             after replica; coordinates x[2][3*nb] double (AoS, current and
+//             trial buffer), forces f[2][3*nb] Real (current and previous),
+//             search direction d[3*nb] Real.
+//   per bead  flag byte (bit0: cylinder to the next bead, bit1: cylinder from
+//             the previous bead); the cylinder (i, i+1) keeps its k_str, l0 at
+//             slot i; the bending triple centred on i keeps the constants of
+//             the cylinder (i, i+1) at slot i.
+//   sparse    linkers, motors, excluded-volume pairs and boundary beads as
+//             interaction lists of internal bead indices; their force
+//             contributions go to a slot buffer and every bead gathers its own
+//             slots through a CSR index, in a fixed order (no float atomics).
+//   tiles     every kernel works on tiles that never straddle replicas; each
+//             tile writes its partial sums to a fixed slot and the last tile of
+//             a replica (atomic ticket) reduces the slots in order, so every
+//             sum is deterministic.
+#pragma once
+
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include <string>
+#include <vector>
+
+#include "../../include/medyan_mech.h"
+
+namespace mech {
+
+constexpr int kFilTile = 256;     // beads per filament tile (one block)
+constexpr int kSparseTile = 256;  // interactions per sparse tile (one block)
+constexpr int kExvolFallbackCap = 4096;
+constexpr int kFbChunks = 64;       // work split of one numeric force fallback
+
+enum Kind : int { K_LINKER = 0, K_MOTOR = 1, K_EXVOL = 2, K_BOUNDARY = 3, K_NUM_SPARSE = 4 };
+
+enum Phase : int {
+    PH_IDLE = 0,
+    PH_LS_TRIAL = 1,   // a line-search trial energy is pending
+    PH_FORCE = 2,      // trial accepted: forces at the new coordinates pending
+    PH_DIR = 3,        // forces, beta ready: direction update pending
+    PH_RESET = 4,      // conjugacy lost: d = F pending
+    PH_FAILED = 5,     // line search returned lambda = 0: host decides
+    PH_DONE = 6,       // converged or call limit
+    PH_ERROR = 7,      // non-finite max force or other fatal condition
+    PH_RECOVER = 8,         // safe-mode failure: recovery move pending (MController.h:273-339)
+    PH_RECOVER_MOVE = 9,
+    PH_RECOVER_FORCE = 10,
+    PH_RECOVER_ENERGY = 11,
+};
+
+// Per-replica minimizer state, resident in device memory.
+struct CGState {
+    // line search
+    double lambda;
+    double E0;             // energy at the current coordinates (computeEnergy value)
+    double Etrial;
+    double reducedSlope;
+    double slope;          // d . F
+    // convergence bookkeeping
+    double maxF;           // gradInfNorm
+    double FdotF;          // F . F of the current forces
+    double lastFdotF;
+    double newGrad, prevGrad, beta;
+    double prevEnergy;
+    double energyRelChange;
+    double newEnergy;
+    double minimumE;
+    double totalEnergy;
+    // parameters
+    double maxDist, lambdaMax, gradTol, energyRelTol;
+    int method, energyCallLimit, forceCallLimit, tryToRecover;
+    // energies of the last evaluation: per FF, then the plain total
+    double eval[MECH_NUM_FF + 1];
+    int evalFailed;        // an FF reported failure in the last evaluation
+    int phase;
+    int safeMode;
+    int xbuf, fbuf;
+    int numIter, numEnergyCall, numForceCall, numEnergyEval, numTrials, numSafeMode, numRecover;
+    int backupValid, backupPending;
+    int errorFlags, status;
+    int active;            // replica participates in the current minimization
+    int restore;           // copy the backup coordinates back (host request)
+};
+
+// Tile of consecutive items of one replica.
+struct Tile {
+    int replica;
+    int begin;
+    int end;
+    int pad;
+};
+
+// Per-replica tile ranges, by tile family.
+struct RepTiles {
+    int fil_begin, fil_end;          // filament (bead) tiles
+    int sp_begin[K_NUM_SPARSE], sp_end[K_NUM_SPARSE];
+};
+
+// Everything the kernels read, passed by value.
+template <typename Real>
+struct DevNet {
+    int nb;                 // beads, all replicas
+    int R;
+    double* x[2];
+    Real* f[2];
+    Real* d;
+    double* xbest;
+    const uint8_t* bflag;
+    const Real* kstr;       // per bead slot
+    const Real* l0;
+    const Real* kbend;
+    const Real* t0;
+    // filament tiles
+    int n_ftiles;
+    const Tile* ftile;
+    // sparse interactions (internal bead indices)
+    int n_lk, n_mt, n_ev, n_bb;
+    const int4* lk_bead; const Real* lk_k; const Real* lk_l0; const Real* lk_s1; const Real* lk_s2;
+    const int4* mt_bead; const Real* mt_k; const Real* mt_l0; const Real* mt_s1; const Real* mt_s2;
+    const int4* ev_bead; const Real* ev_k; const Real* ev_la; const Real* ev_lb;
+    const int* bb_bead; const int* bb_plane;     // plane index into planes
+    const double* planes;                         // [4 * n_planes_total] a, b, c, d
+    const Real* bb_k; const Real* bb_slen;
+    // sparse tiles
+    int n_stiles;
+    const Tile* stile;      // concatenated: linker, motor, exvol, boundary tiles
+    const int* stile_kind;
+    int sp_tiles[K_NUM_SPARSE];   // tiles per kind
+    // contributions and gather index
+    Real* contrib;          // [3 * n_slots]
+    int slot_base[K_NUM_SPARSE + 1];
+    const int* csr_off;     // [nb + 1]
+    const int* csr_slot;
+    // stretch forces of linkers / motors (assignforcemags)
+    double* lk_sf; double* mt_sf;
+    // exvol numeric fallback list: count, (replica, pair) entries, energies
+    // [cap] followed by the lambda of each entry [cap]; force-fallback scratch
+    int* ev_fb_count; int* ev_fb_list; double* ev_fb_energy;
+    double* fb_moments;     // [cap * kFbChunks * 6]
+    int* fb_tickets;        // [cap]
+    // partial sums
+    double* part_fil;       // [n_ftiles * 4]
+    double* part_sp;        // [n_stiles]
+    // per replica
+    CGState* st;
+    const RepTiles* rt;
+    int* ticket;            // [R] last-tile tickets
+    int* gticket;           // whole-grid ticket
+    unsigned* err;          // device error word
+};
+
+// ---- kernels (mech_ff.cu) -------------------------------------------------
+// mode: 0 = line-search trial at x + lambda d (replicas in PH_LS_TRIAL),
+//       1 = plain evaluation at x (replicas with active != 0)
+// `want` selects the replicas a launch works on: replicas whose phase equals
+// `want`, or every replica with active != 0 when want < 0.  `trial` evaluates
+// at x + lambda d instead of x.  Each returns the number of kernels launched.
+template <typename Real> int launch_energy(const DevNet<Real>& n, int want, int trial, cudaStream_t s);
+template <typename Real> int launch_forces(const DevNet<Real>& n, int want, cudaStream_t s);
+template <typename Real> int launch_direction(const DevNet<Real>& n, cudaStream_t s);
+template <typename Real> int launch_reset(const DevNet<Real>& n, cudaStream_t s);
+template <typename Real> int launch_dispatch_failed(const DevNet<Real>& n, cudaStream_t s);
+template <typename Real> int launch_recover(const DevNet<Real>& n, cudaStream_t s);
+template <typename Real> int launch_backup_restore(const DevNet<Real>& n, cudaStream_t s);
+// excluded-volume kernels (mech_exvol.cu, one object per precision)
+template <typename Real> int launch_exvol_energy(const DevNet<Real>& n, int want, int trial, cudaStream_t s);
+template <typename Real> int launch_exvol_forces(const DevNet<Real>& n, int want, cudaStream_t s);
+
+struct DeviceBuffer {
+    void* p = nullptr;
+    size_t bytes = 0;
+    cudaError_t ensure(size_t nbytes);
+    void release();
+    ~DeviceBuffer() { release(); }
+    template <typename T> T* as() const { return static_cast<T*>(p); }
+};
+
+// exclusive scan of n int32 values into out (n + 1 entries, out[n] = total)
+cudaError_t exclusive_scan_i32(const int* in, int* out, long long n, DeviceBuffer& tmp, cudaStream_t s);
+
+}  // namespace mech

@@ -1,0 +1,141 @@
+"""GPU path against the oracle, through the C ABI.
+
+Tolerances (FP64 path):
+* energies: per force field |E_gpu - E_oracle| <= 1e-12 * |E_oracle| + 1e-10 pN nm;
+* forces: per component |F_gpu - F_oracle| <= 1e-12 * S + 1e-9 pN, with S the
+  sum over force fields of that component's magnitude (the oracle evaluated one
+  force field at a time), i.e. relative to the contributions' scale;
+* neighbor lists: the sorted cylinder-pair set is integer-exact.
+"""
+import numpy as np
+import pytest
+
+import oracle
+from picgo_gb300 import Engine, cg_params, jitter, make_network
+
+pytestmark = pytest.mark.gpu
+
+FF_FIELDS = ("n_stretch", "n_bend", "n_linker", "n_motor", "n_exvol", "n_planes")
+
+
+def per_ff_force_scale(vec, coord):
+    S = np.zeros_like(coord)
+    for keep in FF_FIELDS:
+        s2 = oracle.System.from_buffer_copy(vec.system)
+        for nm in FF_FIELDS:
+            if nm != keep:
+                setattr(s2, nm, 0)
+        vv = oracle.Vectorized(vec.arrays, s2, vec.ndof, vec.nbeads, vec.pairs, vec.bnd_cyl, vec.bnd_nn)
+        S += np.abs(oracle.forces(vv, coord))
+    return S
+
+
+def check_energies(per_gpu, per_orc):
+    for k in range(6):
+        assert abs(per_gpu[k] - per_orc[k]) <= 1e-12 * abs(per_orc[k]) + 1e-10, (k, per_gpu[k], per_orc[k])
+
+
+def check_forces(f_gpu, f_orc, scale):
+    err = np.abs(f_gpu - f_orc)
+    tol = 1e-12 * scale + 1e-9
+    bad = err > tol
+    assert not bad.any(), (err[bad][:5], tol[bad][:5], np.argwhere(bad)[:5])
+
+
+NETS = {
+    "c1": dict(config="c1"),
+    "c1_shuffled": dict(config="c1", shuffle_beads=True, shuffle_ids=True, seed=11),
+    "small_motors": dict(config="c1", n_filaments=60, n_cyl_per_filament=12, box=1500.0, n_linkers=80, n_motors=40,
+                         seed=3),
+}
+
+
+def _net(name, sigma=0.0):
+    kw = dict(NETS[name])
+    cfg = kw.pop("config")
+    net = make_network(cfg, **kw)
+    return jitter(net, sigma, seed=7) if sigma else net
+
+
+@pytest.mark.parametrize("name", list(NETS))
+@pytest.mark.parametrize("sigma", [0.0, 0.7])
+def test_fp64_energies_and_forces_match_oracle(name, sigma):
+    net = _net(name, sigma)
+    vec = oracle.vectorize(net)
+    with Engine("fp64") as eng:
+        eng.set_network(net)
+        assert np.array_equal(eng.pairs(), vec.pairs)
+        per, tot, en = eng.energies()
+        o_tot, o_per = oracle.energies(vec, net.coord)
+        check_energies(per, o_per)
+        assert en == oracle.energy(vec, net.coord) or abs(en - o_tot) <= 1e-12 * abs(o_tot)
+        f = eng.forces()
+        check_forces(f, oracle.forces(vec, net.coord), per_ff_force_scale(vec, net.coord))
+
+
+@pytest.mark.parametrize("cell", [0.0, 27.0, 30.375, 55.0, 140.0])
+def test_pair_list_is_exact_for_any_bin_edge(cell):
+    net = _net("c1_shuffled", 2.0)
+    ref = oracle.cyl_pairs(net)
+    with Engine("fp64") as eng:
+        eng.set_network(net)
+        info = eng.rebuild(cell)
+        assert info["n_exvol_pairs"] == ref.shape[0]
+        assert np.array_equal(eng.pairs(), ref)
+
+
+def test_coordinates_round_trip_in_caller_order():
+    net = _net("c1_shuffled")
+    with Engine("fp64") as eng:
+        eng.set_network(net)
+        assert np.array_equal(eng.coords(), net.coord)
+        x2 = net.coord + 0.25
+        eng.set_coords(x2)
+        assert np.array_equal(eng.coords(), x2)
+
+
+def test_fp64_minimizer_tracks_oracle_for_first_iterations():
+    """Same decisions in the first CG iterations: coordinates agree to round-off."""
+    net = _net("small_motors", 0.3)
+    vec = oracle.vectorize(net)
+    prm = dict(energy_call_limit=40)
+    x_o, f_o, r_o = oracle.minimize(vec, net.coord, oracle.cg_params(energyCallLimit=40))
+    with Engine("fp64") as eng:
+        eng.set_network(net)
+        r = eng.minimize(cg_params(**prm))[0]
+        x = eng.coords()
+    assert r["num_iter"] == r_o.numIter
+    assert r["num_force_call"] == r_o.numForceCall
+    assert r["num_energy_call"] == r_o.numEnergyCall
+    assert np.abs(x - x_o).max() <= 1e-9 * (1 + np.abs(x_o).max())
+    assert abs(r["energies_after"][6] - r_o.energiesAfter[6]) <= 1e-10 * abs(r_o.energiesAfter[6])
+
+
+def test_fp64_minimizer_converges_like_oracle():
+    net = _net("small_motors")
+    vec = oracle.vectorize(net)
+    x_o, f_o, r_o = oracle.minimize(vec, net.coord)
+    with Engine("fp64") as eng:
+        eng.set_network(net)
+        r = eng.minimize(cg_params())[0]
+        f = eng.last_forces()
+    assert r["status"] == 0 and r["error_flags"] == 0
+    assert r["grad_inf_norm"] < r["grad_tol"] or r["energy_rel_change"] < r["energy_rel_tol"]
+    assert np.isclose(np.abs(f).max(), r["grad_inf_norm"])
+    # both descend from the same start to a nearby stationary state
+    assert r["energies_after"][6] < r["energies_before"][6]
+    assert abs(r["energies_after"][6] - r_o.energiesAfter[6]) <= 2e-2 * abs(r_o.energiesAfter[6])
+
+
+def test_mixed_energy_error_against_fp64():
+    net = _net("c1", 0.5)
+    vec = oracle.vectorize(net)
+    o_tot, o_per = oracle.energies(vec, net.coord)
+    fo = oracle.forces(vec, net.coord)
+    with Engine("mixed") as eng:
+        eng.set_network(net)
+        per, tot, _ = eng.energies()
+        f = eng.forces()
+    assert abs(tot - o_tot) <= 1e-6 * abs(o_tot), (tot, o_tot)
+    scale = per_ff_force_scale(vec, net.coord)
+    assert np.all(np.abs(f - fo) <= 1e-4 * scale + 1e-3)
