@@ -1,0 +1,341 @@
+#!/usr/bin/env python
+"""Benchmark of the mechanical-equilibration path on one GB300.
+
+Workload: 20,000 actin filaments x 50 cylinders (1,000,000 cylinders, 1,020,000
+beads) in a 10 um box with 50,000 linkers and 5,000 motors (rest lengths
+175-225 nm), seeded synthetic network.  One step = one neighbor-list rebuild
+plus one Polak-Ribiere CG minimization from the seeded start until
+max|F| < 1 pN (energy-change criterion disabled so that the force criterion
+decides), through the C ABI.
+
+Printed line: value = CG force evaluations per second in mixed precision
+(force evaluations of the minimizer divided by its time); the time to 1 pN,
+the FP64 path's figures and the CPU oracle's are beside it.
+
+--impl reference: the oracle (a loop-for-loop CPU restatement of MEDYAN's
+minimizer; MEDYAN itself cannot be built here) on a bounded sample of the
+same workload, same metric.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import tempfile
+import time
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+if ROOT not in sys.path:
+    sys.path.insert(0, ROOT)
+
+METRIC = "CG time to 1 pN and force evals/s at 1M cylinders: mixed vs FP64, one GB300"
+UNIT = "force_evals/s"
+SEED = 20261203 + 2
+CONFIG_NAME = "c2"
+
+
+def cg(**kw):
+    from picgo_gb300 import cg_params
+    base = dict(method=2, max_dist=1.0, lambda_max=0.01, grad_tol=1.0, energy_rel_tol=0.0,
+                force_call_limit=1_000_000, energy_call_limit=0)
+    base.update(kw)
+    return cg_params(**base)
+
+
+def workload():
+    from picgo_gb300 import make_network
+    return make_network(CONFIG_NAME, seed=SEED)
+
+
+class Clocks:
+    """nvidia-smi sampling of SM clocks and throttle reasons during the timed region."""
+    Q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,clocks_event_reasons.hw_slowdown,"
+         "clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown,"
+         "clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, device: int):
+        self.device = device
+        self.proc = None
+        self.path = None
+
+    def __enter__(self):
+        fd, self.path = tempfile.mkstemp(suffix=".csv")
+        os.close(fd)
+        try:
+            self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.device), "--query-gpu=" + self.Q,
+                                          "--format=csv,noheader,nounits", "-lms", "200"],
+                                         stdout=open(self.path, "w"), stderr=subprocess.DEVNULL)
+        except OSError:
+            self.proc = None
+        return self
+
+    def __exit__(self, *exc):
+        if self.proc:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except subprocess.TimeoutExpired:
+                self.proc.kill()
+
+    def summary(self) -> dict:
+        sm, mx, reasons = [], None, set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        try:
+            for line in open(self.path):
+                f = [x.strip() for x in line.split(",")]
+                if len(f) < 9:
+                    continue
+                try:
+                    sm.append(float(f[1]))
+                    mx = float(f[2])
+                except ValueError:
+                    continue
+                for nm, v in zip(names, f[5:9]):
+                    if v.lower() in ("active", "1"):
+                        reasons.add(nm)
+        except OSError:
+            pass
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": mx, "reasons": sorted(reasons),
+                "samples": len(sm)}
+
+
+def flush_l2(torch, dev):
+    buf = torch.empty(64 * 1024 * 1024, dtype=torch.float32, device=dev)   # 256 MB > 129 MB L2
+    buf.zero_()
+    del buf
+
+
+def run_ours(args, rank, world, dist):
+    import numpy as np
+    import torch
+    from picgo_gb300 import Engine
+
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    torch.cuda.set_device(local)
+    dev = torch.device("cuda", local)
+    net = workload()
+    params = cg()
+
+    def barrier():
+        if dist is not None:
+            dist.barrier()
+        torch.cuda.synchronize()
+
+    eng = Engine(args.precision, local)
+    eng.set_network(net)
+
+    def step():
+        eng.reset_coords()
+        eng.rebuild()
+        return eng.minimize(params)[0]
+
+    for _ in range(args.warmup):
+        step()
+    # ---- timed: device-resident inputs ----
+    results, step_ms, launches = [], [], 0
+    with Clocks(local) as clk:
+        barrier()
+        for _ in range(args.steps):
+            flush_l2(torch, dev)
+            torch.cuda.synchronize()
+            e0 = torch.cuda.Event(enable_timing=True)
+            e1 = torch.cuda.Event(enable_timing=True)
+            e0.record()
+            r = step()
+            e1.record()
+            torch.cuda.synchronize()
+            step_ms.append(e0.elapsed_time(e1))
+            results.append(r)
+            launches += eng.timing()["launches"]
+        barrier()
+    clocks = clk.summary()
+    total_ms = sum(step_ms)
+    if dist is not None:
+        t = torch.tensor([total_ms], device=dev)
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        total_ms = float(t.item())
+    force_calls = sum(r["num_force_call"] for r in results)
+    value_local = force_calls / (total_ms / 1e3)
+    ms_per_step = total_ms / args.steps
+
+    # ---- end to end: pinned host coordinates in, minimized coordinates out ----
+    h_in = torch.empty((net.n_beads, 3), dtype=torch.float64, pin_memory=True)
+    h_in.copy_(torch.from_numpy(net.coord))
+    h_out = torch.empty((net.n_beads, 3), dtype=torch.float64, pin_memory=True)
+    e2e_ms, e2e_calls = [], 0
+    barrier()
+    for _ in range(args.steps):
+        flush_l2(torch, dev)
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        eng.set_coords(h_in.numpy())
+        eng.rebuild()
+        r = eng.minimize(params)[0]
+        h_out.numpy()[:] = eng.coords()
+        e2e_ms.append(1e3 * (time.perf_counter() - t0))
+        e2e_calls += r["num_force_call"]
+    barrier()
+    e2e_value = e2e_calls / (sum(e2e_ms) / 1e3)
+
+    # ---- dominant kernel: per-launch device time with CUDA events on the engine's stream ----
+    eng.reset_coords()
+    eng.rebuild()
+    prof = eng.profile(20)
+    rs = 4 if args.precision == "mixed" else 8
+    nb = prof["n_beads"]
+    # algorithmic bytes per launch (each input read once, each output written once)
+    fil_energy_bytes = nb * (24 + 1 + 4 * rs)                 # x, flags, k_str, l0, k_bend, theta0
+    fil_force_bytes = nb * (24 + 1 + 4 * rs + 4 + rs * 3 + rs * 3) + prof["n_slots"] * (4 + 3 * rs)
+    kernels = {
+        "fil_force": (prof["ms_fil_force"], fil_force_bytes),
+        "fil_energy": (prof["ms_fil_energy"], fil_energy_bytes),
+    }
+    peaks = {}
+    try:
+        peaks = json.load(open(os.path.join(ROOT, "MEASURED_PEAKS.json")))
+    except OSError:
+        pass
+    peak = float(peaks.get("hbm_gbs", 6800.0))
+    name, (ms, nbytes) = max(kernels.items(), key=lambda kv: kv[1][0])
+    achieved = nbytes / (ms * 1e-3) / 1e9
+    roofline = {"bound": "hbm", "kernel": name, "achieved": round(achieved, 1), "peak": peak, "unit": "GB/s",
+                "frac": round(achieved / peak, 4), "traffic": None,
+                "peak_source": "measured" if "hbm_gbs" in peaks else "fallback",
+                "bytes_per_launch": int(nbytes), "ms_per_launch": round(ms, 5),
+                "profile_ms": {k: round(v, 5) for k, v in prof.items() if k.startswith("ms_")}}
+    eng.close()
+
+    out = {
+        "metric": METRIC, "value": value_local * world if dist is None else None, "unit": UNIT, "n_gpus": world,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": round(ms_per_step, 3), "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "f32+f64" if args.precision == "mixed" else "f64",
+        "data": "synthetic (seeded network generator; no dataset)",
+        "config": {"workload": "20,000 filaments x 50 cylinders (1M cylinders), 50k linkers, 5k motors, 10 um box",
+                   "seed": SEED, "precision": args.precision, "cg": "Polak-Ribiere, backtracking, gradTol 1 pN, "
+                   "maxDist 1, lambdaMax 0.01, energyRelTol 0 (run to 1 pN)",
+                   "l2": "flushed (256 MB write) between timed steps", "parallelism": f"replicas x{world}"},
+        "time_to_1pN_s": round(ms_per_step / 1e3, 4),
+        "cg_iterations": results[-1]["num_iter"], "force_calls_per_step": results[-1]["num_force_call"],
+        "final_max_force_pN": results[-1]["grad_inf_norm"],
+        "e2e": {"value": round(e2e_value * world, 2), "unit": UNIT, "h2d_bytes_per_step": int(net.n_beads * 24),
+                "d2h_bytes_per_step": int(net.n_beads * 24)},
+        "gpu_launches": int(launches),
+        "clocks": clocks,
+        "roofline": roofline,
+    }
+    if dist is not None:
+        t = torch.tensor([force_calls], dtype=torch.float64, device=dev)
+        dist.all_reduce(t)
+        out["value"] = float(t.item()) / (total_ms / 1e3)
+    out["value"] = round(out["value"], 2)
+    return out, net
+
+
+def fp64_compare(args, net):
+    """Same step on the plain FP64 path, once (time to 1 pN and evals/s)."""
+    import torch
+    from picgo_gb300 import Engine
+    eng = Engine("fp64", int(os.environ.get("LOCAL_RANK", "0")))
+    eng.set_network(net)
+    eng.rebuild()
+    r0 = eng.minimize(cg(energy_call_limit=200))[0]   # warm-up
+    eng.reset_coords()
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    eng.rebuild()
+    r = eng.minimize(cg())[0]
+    dt = time.perf_counter() - t0
+    eng.close()
+    return {"time_to_1pN_s": round(dt, 4), "force_evals_per_s": round(r["num_force_call"] / dt, 2),
+            "cg_iterations": r["num_iter"], "final_max_force_pN": r["grad_inf_norm"], "status": r["status"],
+            "energy_after": r["energies_after"][6], "warmup_iters": r0["num_iter"]}
+
+
+def cpu_sample(net, seconds: float):
+    """The oracle's CG on the same network, bounded: force evaluations per second on one core."""
+    import oracle
+    t0 = time.perf_counter()
+    vec = oracle.vectorize(net)
+    t_vec = time.perf_counter() - t0
+    limit = 8
+    while True:
+        t0 = time.perf_counter()
+        x, f, res = oracle.minimize(vec, net.coord, oracle.cg_params(energyRelTol=0.0, energyCallLimit=limit,
+                                                                       forceCallLimit=1_000_000))
+        dt = time.perf_counter() - t0
+        if dt >= seconds or limit >= 4096:
+            break
+        limit = int(limit * max(2.0, min(8.0, seconds / max(dt, 1e-3))))
+    return {"value": round(res.numForceCall / dt, 4), "unit": UNIT, "cores": 1, "kind": "port",
+            "sample": f"oracle CG on the same 1M-cylinder network from the same start, first {res.numIter} "
+                      f"iterations ({res.numForceCall} force + {res.numEnergyCall} energy evaluations) in {dt:.1f} s "
+                      f"(vectorize {t_vec:.1f} s excluded); single-threaded like MEDYAN's minimizer",
+            "seconds": round(dt, 2), "energy_evals_per_force_eval": round(res.numEnergyCall / max(1, res.numForceCall), 3)}
+
+
+def run_reference(args, rank, world):
+    if rank != 0:
+        return None
+    net = workload()
+    vals = []
+    for _ in range(args.warmup):
+        pass   # the oracle has no warm-up state; each step is a fresh bounded sample
+    for _ in range(args.steps):
+        s = cpu_sample(net, args.cpu_seconds / max(1, args.steps))
+        vals.append(s)
+    v = sum(s["value"] for s in vals) / len(vals)
+    cpu = dict(vals[-1])
+    cpu["value"] = round(v, 4)
+    return {"metric": METRIC, "value": round(v, 4), "unit": UNIT, "impl": "reference", "n_gpus": world,
+            "steps": args.steps, "warmup": args.warmup, "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": "f64", "data": "synthetic (seeded network generator; no dataset)",
+            "config": {"workload": "20,000 filaments x 50 cylinders (1M cylinders), 50k linkers, 5k motors, 10 um box",
+                       "seed": SEED, "precision": "fp64 (CPU restatement of MEDYAN's minimizer)"},
+            "cpu_baseline": cpu,
+            "e2e": {"value": round(v, 4), "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=3)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
+    ap.add_argument("--precision", choices=["mixed", "fp64"], default="mixed")
+    ap.add_argument("--cpu-seconds", type=float, default=20.0)
+    ap.add_argument("--no-fp64", action="store_true")
+    ap.add_argument("--no-cpu", action="store_true")
+    args = ap.parse_args()
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    dist = None
+    if world > 1:
+        import torch.distributed as tdist
+        tdist.init_process_group("nccl" if args.impl == "ours" else "gloo")
+        dist = tdist
+    if args.impl == "reference":
+        out = run_reference(args, rank, world)
+        if out is not None:
+            print(json.dumps(out))
+        if dist is not None:
+            dist.destroy_process_group()
+        return
+    out, net = run_ours(args, rank, world, dist)
+    if rank == 0:
+        if not args.no_fp64 and args.precision == "mixed":
+            f = fp64_compare(args, net)
+            out["fp64"] = f
+            out["mixed_vs_fp64_time_to_1pN"] = round(f["time_to_1pN_s"] / out["time_to_1pN_s"], 3)
+            out["mixed_vs_fp64_evals_per_s"] = round(out["value"] / max(f["force_evals_per_s"], 1e-9), 3)
+        if not args.no_cpu and world == 1:
+            out["cpu_baseline"] = cpu_sample(net, args.cpu_seconds)
+        print(json.dumps(out))
+    if dist is not None:
+        dist.destroy_process_group()
+
+
+if __name__ == "__main__":
+    main()

@@ -228,6 +228,29 @@ typedef struct MechTiming {
 } MechTiming;
 int32_t mech_get_timing(MechContext* ctx, MechTiming* t);
 
+/* Restore every replica's coordinates to those given at mech_set_networks
+ * (device-to-device; no host transfer). */
+int32_t mech_reset_coords(MechContext* ctx);
+
+/*
+ * Average device time per launch (milliseconds, CUDA events on the context's
+ * stream) of the evaluation kernels at the current coordinates, each launched
+ * `iters` times in plain-evaluation mode: a full energy evaluation, a full
+ * force evaluation, and their parts.
+ */
+typedef struct MechProfile {
+    double ms_energy_eval;         /* all kernels of one energy evaluation */
+    double ms_force_eval;          /* all kernels of one force evaluation */
+    double ms_fil_energy;          /* filament stretching + bending energy */
+    double ms_fil_force;           /* filament forces + sparse gather + CG partials */
+    double ms_bond_energy;         /* linkers, motors, boundary: energy */
+    double ms_bond_force;          /* linkers, motors, boundary: contributions */
+    double ms_exvol_energy;        /* excluded volume (with its fallback check) */
+    double ms_exvol_force;
+    int64_t n_beads, n_exvol_pairs, n_boundary, n_linkers, n_motors, n_slots;
+} MechProfile;
+int32_t mech_profile(MechContext* ctx, int32_t iters, MechProfile* out);
+
 #ifdef __cplusplus
 }
 #endif

@@ -100,6 +100,36 @@ void push_off_plane(const double* p1, const double* p2, const double* p3, const 
 
 inline bool bad(double x) { return std::fabs(x) == std::numeric_limits<double>::infinity() || x != x; }
 
+// When set, force routines accumulate |contribution| instead of the
+// contribution: the per-component scale that parity tolerances refer to.
+bool g_abs = false;
+inline void acc(double& dst, double v) { dst += g_abs ? std::fabs(v) : v; }
+
+// Arctangent from argument reduction and the alternating series, written with
+// + - * / only so that it rounds identically on every IEEE machine compiled
+// without contraction.  atan(x) = -atan(-x); atan(x) = pi/2 - atan(1/x) for
+// x > 1; atan(x) = pi/6 + atan((sqrt(3) x - 1) / (x + sqrt(3))) for
+// x > tan(pi/12); then sum_k (-1)^k x^(2k+1) / (2k+1) to k = 18.
+double series_atan(double x) {
+    const double kPi2 = 1.5707963267948966, kPi6 = 0.52359877559829882, kSqrt3 = 1.7320508075688772,
+                 kTan15 = 0.26794919243112270;
+    const bool neg = x < 0;
+    double a = neg ? -x : x;
+    const bool inv = a > 1.0;
+    if (inv) a = 1.0 / a;
+    const bool red = a > kTan15;
+    if (red) a = (a * kSqrt3 - 1.0) / (a + kSqrt3);
+    const double z = a * a;
+    double p = 1.0 / 37.0;
+    for (int k = 17; k >= 0; --k) p = 1.0 / (2 * k + 1) - z * p;
+    double r = a * p;
+    if (red) r = kPi6 + r;
+    if (inv) r = kPi2 - r;
+    return neg ? -r : r;
+}
+bool g_series_atan = false;
+inline double atan_(double x) { return g_series_atan ? series_atan(x) : std::atan(x); }
+
 }  // namespace
 
 extern "C" {
@@ -129,8 +159,8 @@ void orc_stretch_forces(const double* coord, double* f, int n, const int* bs, co
         double* f1 = f + bs[2 * i];
         double* f2 = f + bs[2 * i + 1];
         const double F[3] = {-f0 * (c2[0] - c1[0]), -f0 * (c2[1] - c1[1]), -f0 * (c2[2] - c1[2])};
-        for (int d = 0; d < 3; ++d) f2[d] += F[d];
-        for (int d = 0; d < 3; ++d) f1[d] += -F[d];
+        for (int d = 0; d < 3; ++d) acc(f2[d], F[d]);
+        for (int d = 0; d < 3; ++d) acc(f1[d], -F[d]);
     }
 }
 
@@ -200,9 +230,9 @@ void orc_bend_forces(const double* coord, double* f, int n, const int* bs, const
         double* f1 = f + bs[3 * i];
         double* f2 = f + bs[3 * i + 1];
         double* f3 = f + bs[3 * i + 2];
-        for (int d = 0; d < 3; ++d) f1[d] += -F1[d];
-        for (int d = 0; d < 3; ++d) f2[d] += F1[d] - F2[d];
-        for (int d = 0; d < 3; ++d) f3[d] += F2[d];
+        for (int d = 0; d < 3; ++d) acc(f1[d], -F1[d]);
+        for (int d = 0; d < 3; ++d) acc(f2[d], F1[d] - F2[d]);
+        for (int d = 0; d < 3; ++d) acc(f3[d], F2[d]);
     }
 }
 
@@ -238,10 +268,10 @@ void orc_bond_forces(const double* coord, double* f, int n, const int* bs, const
         double* f2 = f + bs[4 * i + 1];
         double* f3 = f + bs[4 * i + 2];
         double* f4 = f + bs[4 * i + 3];
-        for (int d = 0; d < 3; ++d) f1[d] += -Fl[d] * (1 - s1[i]);
-        for (int d = 0; d < 3; ++d) f2[d] += -Fl[d] * (s1[i]);
-        for (int d = 0; d < 3; ++d) f3[d] += Fl[d] * (1 - s2[i]);
-        for (int d = 0; d < 3; ++d) f4[d] += Fl[d] * (s2[i]);
+        for (int d = 0; d < 3; ++d) acc(f1[d], -Fl[d] * (1 - s1[i]));
+        for (int d = 0; d < 3; ++d) acc(f2[d], -Fl[d] * (s1[i]));
+        for (int d = 0; d < 3; ++d) acc(f3[d], Fl[d] * (1 - s2[i]));
+        for (int d = 0; d < 3; ++d) acc(f4[d], Fl[d] * (s2[i]));
         if (stretchforce) stretchforce[i] = f0 / invL;
     }
 }
@@ -294,10 +324,10 @@ static void pair_invariants(const double* c1, const double* c2, const double* c3
     cross3(cp, A, Bv);
     const double trip = cp[0] * Cv[0] + cp[1] * Cv[1] + cp[2] * Cv[2];
     p.JJ = -trip * trip;
-    p.ATG1 = std::atan((p.a + p.e) / p.AA) - std::atan(p.e / p.AA);
-    p.ATG2 = std::atan((p.a + p.e - p.d) / p.EE) - std::atan((p.e - p.d) / p.EE);
-    p.ATG3 = std::atan((p.F) / p.BB) - std::atan((p.F - p.b) / p.BB);
-    p.ATG4 = std::atan((p.d + p.F) / p.FF) - std::atan((p.d + p.F - p.b) / p.FF);
+    p.ATG1 = atan_((p.a + p.e) / p.AA) - atan_(p.e / p.AA);
+    p.ATG2 = atan_((p.a + p.e - p.d) / p.EE) - atan_((p.e - p.d) / p.EE);
+    p.ATG3 = atan_((p.F) / p.BB) - atan_((p.F - p.b) / p.BB);
+    p.ATG4 = atan_((p.d + p.F) / p.FF) - atan_((p.d + p.F - p.b) / p.FF);
 }
 
 // 1 / r(s,t)^4 and its r^-6 moments on the two segments (CylinderExclVolRepulsion.h:53-72)
@@ -547,7 +577,7 @@ int orc_exvol_forces(const double* coord, double* f, int n, const int* bs, const
         if (r < 0) return -1;     // the reference exits the process here
         nfallback += r;
         for (int q = 0; q < 4; ++q)
-            for (int k = 0; k < 3; ++k) f[bs[4 * i + q] + k] += out[q][k];
+            for (int k = 0; k < 3; ++k) acc(f[bs[4 * i + q] + k], out[q][k]);
     }
     return nfallback;
 }
@@ -587,9 +617,9 @@ void orc_boundary_forces(const double* coord, double* f, int nplanes, const doub
             const double R = -r / slen[off + j];
             const double f0 = krep[off + j] * std::exp(R) / slen[off + j];
             double* fb = f + bs[off + j];
-            fb[0] += f0 * pl[0];
-            fb[1] += f0 * pl[1];
-            fb[2] += f0 * pl[2];
+            acc(fb[0], f0 * pl[0]);
+            acc(fb[1], f0 * pl[1]);
+            acc(fb[2], f0 * pl[2]);
         }
         off += nn[p];
     }
@@ -600,7 +630,9 @@ void orc_boundary_forces(const double* coord, double* f, int nplanes, const doub
 // ---------------------------------------------------------------------------
 
 // Half cylinder-cylinder list by brute force over all pairs, with the
-// predicate of HybridCylinderCylinderNL::updateNeighborsbin (:413-443):
+// predicate of HybridCylinderCylinderNL::updateNeighborsbin (:413-443)
+// (one search is registered per filament-type pair, CylinderExclVolume.h:94-109,
+// so every type combination is listed):
 // keep (c, n) when id_c > id_n, not (same filament and |pos_c - pos_n| <= 2),
 // and rMin^2 <= d^2 <= rMax^2, d^2 summed from 0 as (m_n - m_c)^2 over x, y, z
 // (Util/Math/Vec.hpp:378-385) and the bounds held as float (HybridNeighborList.h:37).
@@ -615,7 +647,7 @@ int64_t orc_cyl_pairs(int ncyl, const double* mid, const int64_t* id, const int*
         for (int ni = 0; ni < ncyl; ++ni) {
             if (id[ci] <= id[ni]) continue;
             if (fil[ci] == fil[ni] && std::abs(pos[ci] - pos[ni]) <= 2) continue;
-            if (type[ci] != type[ni]) continue;   // one search per type pair; all configured types are 0
+            (void)type;
             double d2 = 0;
             for (int k = 0; k < 3; ++k) d2 += (mid[3 * ni + k] - mid[3 * ci + k]) * (mid[3 * ni + k] - mid[3 * ci + k]);
             if (d2 < rminsq || d2 > rmaxsq) continue;
@@ -651,7 +683,6 @@ int64_t orc_cyl_pairs_binned(int ncyl, const double* mid, const int64_t* id, con
                     for (int ni : bins[(size_t(jx) * G + jy) * G + jz]) {
                         if (id[ci] <= id[ni]) continue;
                         if (fil[ci] == fil[ni] && std::abs(pos[ci] - pos[ni]) <= 2) continue;
-                        if (type[ci] != type[ni]) continue;
                         double d2 = 0;
                         for (int k = 0; k < 3; ++k)
                             d2 += (mid[3 * ni + k] - mid[3 * ci + k]) * (mid[3 * ni + k] - mid[3 * ci + k]);
@@ -1017,5 +1048,17 @@ int orc_minimize_quadratic(int n, const double* w, const double* o, const OrcCGP
 }
 
 int orc_version(void) { return 1; }
+
+// Arctangent used by the excluded-volume formula: 0 = the C library's atan
+// (the reference's), 1 = series_atan above (rounds identically on the GPU).
+void orc_set_series_atan(int on) { g_series_atan = on != 0; }
+double orc_series_atan(double x) { return series_atan(x); }
+
+// Per-component sum of |contribution| over every interaction.
+void orc_system_force_scale(const OrcSystem* s, const double* x, double* scale, int nvar) {
+    g_abs = true;
+    orc_system_forces(s, x, scale, nvar, nullptr, nullptr);
+    g_abs = false;
+}
 
 }  // extern "C"

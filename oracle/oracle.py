@@ -115,6 +115,10 @@ def lib():
             L.orc_boundary_energy.argtypes = [_dp, C.c_int, _dp, _ip, _ip, _dp, _dp]
             L.orc_boundary_forces.argtypes = [_dp, _dp, C.c_int, _dp, _ip, _ip, _dp, _dp]
             L.orc_set_exvol_force_nodes.argtypes = [C.c_int]
+            L.orc_set_series_atan.argtypes = [C.c_int]
+            L.orc_series_atan.restype = C.c_double
+            L.orc_series_atan.argtypes = [C.c_double]
+            L.orc_system_force_scale.argtypes = [C.POINTER(System), _dp, _dp, C.c_int]
             _lib = L
     return _lib
 
@@ -182,7 +186,7 @@ def cyl_pairs_fast(net, coord=None) -> np.ndarray:
     c = np.where(net.cyl_id[i] > net.cyl_id[j], i, j)
     n = np.where(net.cyl_id[i] > net.cyl_id[j], j, i)
     same = (net.cyl_fil[c] == net.cyl_fil[n]) & (np.abs(net.cyl_pos[c] - net.cyl_pos[n]) <= 2)
-    ok = ~same & (net.cyl_type[c] == net.cyl_type[n])
+    ok = ~same
     dx = mid[n] - mid[c]
     d2 = ((0.0 + dx[:, 0] * dx[:, 0]) + dx[:, 1] * dx[:, 1]) + dx[:, 2] * dx[:, 2]
     ok &= (d2 >= 0.0) & (d2 <= rmaxsq)
@@ -318,6 +322,25 @@ def forces(vec: Vectorized, coord: np.ndarray) -> np.ndarray:
     f = np.zeros_like(x)
     lib().orc_system_forces(C.byref(vec.system), _p(x), _p(f), x.size, None, None)
     return f.reshape(-1, 3)
+
+
+def force_scale(vec: Vectorized, coord: np.ndarray) -> np.ndarray:
+    """Per component, the sum over interactions of |contribution|."""
+    x = np.ascontiguousarray(coord, dtype=np.float64).reshape(-1)
+    s = np.zeros_like(x)
+    lib().orc_system_force_scale(C.byref(vec.system), _p(x), _p(s), x.size)
+    return s.reshape(-1, 3)
+
+
+class series_atan_mode:
+    """Context manager: the excluded-volume formula uses the oracle's series
+    arctangent (the one the GPU's FP64 kernel uses) instead of the C library's."""
+    def __enter__(self):
+        lib().orc_set_series_atan(1)
+        return self
+
+    def __exit__(self, *exc):
+        lib().orc_set_series_atan(0)
 
 
 def cg_params(method=2, maxDist=1.0, lambdaMax=0.01, gradTol=1.0, energyRelTol=1e-9, energyCallLimit=0,

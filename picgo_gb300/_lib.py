@@ -32,6 +32,7 @@ EXPORTS = [
     "mech_abi_version", "mech_last_error", "mech_ctx_create", "mech_ctx_destroy", "mech_set_networks",
     "mech_set_coords", "mech_get_coords", "mech_rebuild_neighbors", "mech_get_pairs", "mech_energy",
     "mech_forces", "mech_minimize", "mech_get_forces", "mech_get_stretch_forces", "mech_get_timing",
+    "mech_reset_coords", "mech_profile",
 ]
 
 
@@ -84,6 +85,14 @@ class MechTiming(C.Structure):
                 ("graph_launches", C.c_int64)]
 
 
+class MechProfile(C.Structure):
+    _fields_ = [("ms_energy_eval", C.c_double), ("ms_force_eval", C.c_double), ("ms_fil_energy", C.c_double),
+                ("ms_fil_force", C.c_double), ("ms_bond_energy", C.c_double), ("ms_bond_force", C.c_double),
+                ("ms_exvol_energy", C.c_double), ("ms_exvol_force", C.c_double), ("n_beads", C.c_int64),
+                ("n_exvol_pairs", C.c_int64), ("n_boundary", C.c_int64), ("n_linkers", C.c_int64),
+                ("n_motors", C.c_int64), ("n_slots", C.c_int64)]
+
+
 _lock = threading.Lock()
 _lib = None
 
@@ -122,6 +131,8 @@ def load(build_if_missing: bool = False):
         L.mech_get_forces.argtypes = [vp, C.c_int32, _dp]
         L.mech_get_stretch_forces.argtypes = [vp, C.c_int32, _dp, _dp]
         L.mech_get_timing.argtypes = [vp, C.POINTER(MechTiming)]
+        L.mech_reset_coords.argtypes = [vp]
+        L.mech_profile.argtypes = [vp, C.c_int32, C.POINTER(MechProfile)]
         for name in EXPORTS:
             f = getattr(L, name)
             if f.restype is None or f.restype is C.c_int:

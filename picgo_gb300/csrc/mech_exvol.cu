@@ -33,6 +33,37 @@ struct PairInv {
     T ATG1, ATG2, ATG3, ATG4;
 };
 
+// Arctangent from argument reduction and the alternating series, with + - * /
+// only: compiled without contraction it rounds exactly like the oracle's
+// restatement on the host, which keeps FP64 parity free of libm differences
+// (nearly coplanar pairs amplify a one-ulp arctangent difference ~1e6 times).
+// atan(x) = -atan(-x); = pi/2 - atan(1/x) for x > 1;
+// = pi/6 + atan((sqrt(3) x - 1)/(x + sqrt(3))) for x > tan(pi/12);
+// then sum_k (-1)^k x^(2k+1)/(2k+1), k <= 18.
+__device__ __forceinline__ double series_atan(double x) {
+    constexpr double kPi2 = 1.5707963267948966, kPi6 = 0.52359877559829882, kSqrt3 = 1.7320508075688772,
+                     kTan15 = 0.26794919243112270;
+    constexpr double kInvOdd[19] = {1.0 / 1,  1.0 / 3,  1.0 / 5,  1.0 / 7,  1.0 / 9,  1.0 / 11, 1.0 / 13,
+                                    1.0 / 15, 1.0 / 17, 1.0 / 19, 1.0 / 21, 1.0 / 23, 1.0 / 25, 1.0 / 27,
+                                    1.0 / 29, 1.0 / 31, 1.0 / 33, 1.0 / 35, 1.0 / 37};
+    const bool neg = x < 0;
+    double a = neg ? -x : x;
+    const bool inv = a > 1.0;
+    if (inv) a = 1.0 / a;
+    const bool red = a > kTan15;
+    if (red) a = (a * kSqrt3 - 1.0) / (a + kSqrt3);
+    const double z = a * a;
+    double p = kInvOdd[18];
+#pragma unroll
+    for (int k = 17; k >= 0; --k) p = kInvOdd[k] - z * p;
+    double r = a * p;
+    if (red) r = kPi6 + r;
+    if (inv) r = kPi2 - r;
+    return neg ? -r : r;
+}
+__device__ __forceinline__ double atan_of(double x) { return series_atan(x); }
+__device__ __forceinline__ float atan_of(float x) { return atanf(x); }
+
 template <typename T>
 __device__ __forceinline__ T dot3(const T* u, const T* v) {
     return u[0] * v[0] + u[1] * v[1] + u[2] * v[2];
@@ -78,10 +109,10 @@ __device__ __forceinline__ void pair_inv(const double* c1, const double* c2, con
     const T cz = v12[0] * v34[1] - v12[1] * v34[0];
     const T trip = cx * v31[0] + cy * v31[1] + cz * v31[2];
     p.JJ = -trip * trip;
-    p.ATG1 = atan((p.a + p.e) / p.AA) - atan(p.e / p.AA);
-    p.ATG2 = atan((p.a + p.e - p.d) / p.EE) - atan((p.e - p.d) / p.EE);
-    p.ATG3 = atan((p.F) / p.BB) - atan((p.F - p.b) / p.BB);
-    p.ATG4 = atan((p.d + p.F) / p.FF) - atan((p.d + p.F - p.b) / p.FF);
+    p.ATG1 = atan_of((p.a + p.e) / p.AA) - atan_of(p.e / p.AA);
+    p.ATG2 = atan_of((p.a + p.e - p.d) / p.EE) - atan_of((p.e - p.d) / p.EE);
+    p.ATG3 = atan_of((p.F) / p.BB) - atan_of((p.F - p.b) / p.BB);
+    p.ATG4 = atan_of((p.d + p.F) / p.FF) - atan_of((p.d + p.F - p.b) / p.FF);
 }
 
 template <typename T>

@@ -670,7 +670,21 @@ int launch_backup_restore(const DevNet<Real>& n, cudaStream_t s) {
     return 1;
 }
 
+template <typename Real>
+int launch_part(const DevNet<Real>& n, int which, cudaStream_t s) {
+    int ev_t = 0, bb_t = 0;
+    const int lm = n_lm_tiles(n, &ev_t, &bb_t);
+    switch (which) {
+        case 0: k_fil_energy<Real><<<n.n_ftiles, kBlock, 0, s>>>(n, -1, 0); return 1;
+        case 1: k_fil_force<Real><<<n.n_ftiles, kBlock, 0, s>>>(n, -1); return 1;
+        case 2: if (lm + bb_t > 0) { k_bond_bnd<Real><<<lm + bb_t, kBlock, 0, s>>>(n, -1, 0, 0, lm, ev_t); return 1; } return 0;
+        case 3: if (lm + bb_t > 0) { k_bond_bnd<Real><<<lm + bb_t, kBlock, 0, s>>>(n, -1, 0, 1, lm, ev_t); return 1; } return 0;
+    }
+    return 0;
+}
+
 #define MECH_INSTANTIATE(R)                                                             \
+    template int launch_part<R>(const DevNet<R>&, int, cudaStream_t);                   \
     template int launch_energy<R>(const DevNet<R>&, int, int, cudaStream_t);            \
     template int launch_forces<R>(const DevNet<R>&, int, cudaStream_t);                 \
     template int launch_direction<R>(const DevNet<R>&, cudaStream_t);                   \

@@ -63,7 +63,7 @@ struct MechContext {
     std::vector<ReplicaHost> reps;
     bool have_net = false, have_lists = false;
     // beads
-    DeviceBuffer x[2], f[2], d, xbest, bflag, kstr, l0, kbend, t0;
+    DeviceBuffer x[2], f[2], d, xbest, xinit, bflag, kstr, l0, kbend, t0;
     // cylinders
     DeviceBuffer cyl_b1, cyl_id, cyl_fil, cyl_pos, cyl_rep, cyl_minus, cyl_kex, cyl_type, cyl_l0;
     // linkers / motors
@@ -81,6 +81,7 @@ struct MechContext {
     CsrBuild cb;
     DeviceBuffer rep_cell, rep_dims, rep_rmax2, rep_rmin2, rep_margin, rep_q, rep_ncyl, rep_plane, rep_cyl, rep_bcut,
         gather_idx, gather_out;
+    DeviceBuffer perm_all, stage;   // caller -> internal bead map of all replicas; coordinate staging
     int n_ftiles = 0, n_stiles = 0;
     int sp_tiles[K_NUM_SPARSE] = {0, 0, 0, 0};
     int slot_base[K_NUM_SPARSE + 1] = {0, 0, 0, 0, 0};
@@ -247,10 +248,8 @@ __global__ void k_cg_init(CGState* st, int R) {
     S.phase = PH_RESET;                   // resetCGParams, then the loop head
 }
 
-int ensure_perm_buffer(MechContext* c, int r, DeviceBuffer& buf) {
-    const ReplicaHost& h = c->reps[r];
-    return upload(buf, h.perm, c->stream);
-}
+// the replica's slice of the caller -> internal map (replica-local indices)
+const int* perm_of(MechContext* c, int r) { return c->perm_all.as<int>() + c->reps[r].bead_begin; }
 
 }  // namespace
 
@@ -385,6 +384,14 @@ static int set_networks(MechContext* c, int R, const MechNetwork* nets) {
         nmt += N.n_motors;
         npl += N.n_planes;
     }
+    {
+        std::vector<int> pa;
+        pa.reserve(nb);
+        for (int r = 0; r < R; ++r) pa.insert(pa.end(), c->reps[r].perm.begin(), c->reps[r].perm.end());
+        int rc0 = upload(c->perm_all, pa, c->stream);
+        if (rc0) return rc0;
+        CU(c->stage.ensure(sizeof(double) * 3 * (size_t)std::max(nb, 1)));
+    }
     c->nb = nb;
     c->ncyl = ncyl;
     c->nlk = nlk;
@@ -397,6 +404,8 @@ static int set_networks(MechContext* c, int R, const MechNetwork* nets) {
     CU(c->x[1].ensure(sizeof(double) * x.size()));
     CU(cudaMemcpyAsync(c->x[1].p, c->x[0].p, sizeof(double) * x.size(), cudaMemcpyDeviceToDevice, s));
     CU(c->xbest.ensure(sizeof(double) * x.size()));
+    CU(c->xinit.ensure(sizeof(double) * x.size()));
+    CU(cudaMemcpyAsync(c->xinit.p, c->x[0].p, sizeof(double) * x.size(), cudaMemcpyDeviceToDevice, s));
     CU(c->f[0].ensure(rs * x.size()));
     CU(c->f[1].ensure(rs * x.size()));
     CU(c->d.ensure(rs * x.size()));
@@ -944,12 +953,10 @@ int32_t mech_set_coords(MechContext* ctx, int32_t r, const double* coord) {
     CU(cudaSetDevice(ctx->device));
     if ((rc = pull_states(ctx))) return rc;
     const ReplicaHost& h = ctx->reps[r];
-    DeviceBuffer tmp, perm;
-    CU(tmp.ensure(sizeof(double) * 3 * h.nb));
-    CU(cudaMemcpyAsync(tmp.p, coord, sizeof(double) * 3 * h.nb, cudaMemcpyHostToDevice, ctx->stream));
-    if ((rc = ensure_perm_buffer(ctx, r, perm))) return rc;
+    CU(cudaMemcpyAsync(ctx->stage.p, coord, sizeof(double) * 3 * h.nb, cudaMemcpyHostToDevice, ctx->stream));
     double* X = ctx->x[ctx->h_st[r].xbuf].as<double>();
-    k_scatter_coords<<<(h.nb + 255) / 256, 256, 0, ctx->stream>>>(tmp.as<double>(), perm.as<int>(), h.nb, h.bead_begin, X);
+    k_scatter_coords<<<(h.nb + 255) / 256, 256, 0, ctx->stream>>>(ctx->stage.as<double>(), perm_of(ctx, r), h.nb,
+                                                                  h.bead_begin, X);
     CU(cudaGetLastError());
     CU(cudaStreamSynchronize(ctx->stream));
     return MECH_OK;
@@ -962,12 +969,10 @@ int32_t mech_get_coords(MechContext* ctx, int32_t r, double* coord) {
     CU(cudaSetDevice(ctx->device));
     if ((rc = pull_states(ctx))) return rc;
     const ReplicaHost& h = ctx->reps[r];
-    DeviceBuffer tmp, perm;
-    CU(tmp.ensure(sizeof(double) * 3 * h.nb));
-    if ((rc = ensure_perm_buffer(ctx, r, perm))) return rc;
     const double* X = ctx->x[ctx->h_st[r].xbuf].as<double>();
-    k_gather_coords<double><<<(h.nb + 255) / 256, 256, 0, ctx->stream>>>(X, perm.as<int>(), h.nb, h.bead_begin, tmp.as<double>());
-    CU(cudaMemcpyAsync(coord, tmp.p, sizeof(double) * 3 * h.nb, cudaMemcpyDeviceToHost, ctx->stream));
+    k_gather_coords<double><<<(h.nb + 255) / 256, 256, 0, ctx->stream>>>(X, perm_of(ctx, r), h.nb, h.bead_begin,
+                                                                        ctx->stage.as<double>());
+    CU(cudaMemcpyAsync(coord, ctx->stage.p, sizeof(double) * 3 * h.nb, cudaMemcpyDeviceToHost, ctx->stream));
     CU(cudaStreamSynchronize(ctx->stream));
     return MECH_OK;
 }
@@ -979,17 +984,14 @@ int32_t mech_get_forces(MechContext* ctx, int32_t r, double* f_out) {
     CU(cudaSetDevice(ctx->device));
     if ((rc = pull_states(ctx))) return rc;
     const ReplicaHost& h = ctx->reps[r];
-    DeviceBuffer tmp, perm;
-    CU(tmp.ensure(sizeof(double) * 3 * h.nb));
-    if ((rc = ensure_perm_buffer(ctx, r, perm))) return rc;
     const int fb = ctx->h_st[r].fbuf;
     if (ctx->precision == MECH_PREC_FP64)
-        k_gather_coords<double><<<(h.nb + 255) / 256, 256, 0, ctx->stream>>>(ctx->f[fb].as<double>(), perm.as<int>(), h.nb,
-                                                                           h.bead_begin, tmp.as<double>());
+        k_gather_coords<double><<<(h.nb + 255) / 256, 256, 0, ctx->stream>>>(ctx->f[fb].as<double>(), perm_of(ctx, r), h.nb,
+                                                                           h.bead_begin, ctx->stage.as<double>());
     else
-        k_gather_coords<float><<<(h.nb + 255) / 256, 256, 0, ctx->stream>>>(ctx->f[fb].as<float>(), perm.as<int>(), h.nb,
-                                                                          h.bead_begin, tmp.as<double>());
-    CU(cudaMemcpyAsync(f_out, tmp.p, sizeof(double) * 3 * h.nb, cudaMemcpyDeviceToHost, ctx->stream));
+        k_gather_coords<float><<<(h.nb + 255) / 256, 256, 0, ctx->stream>>>(ctx->f[fb].as<float>(), perm_of(ctx, r), h.nb,
+                                                                          h.bead_begin, ctx->stage.as<double>());
+    CU(cudaMemcpyAsync(f_out, ctx->stage.p, sizeof(double) * 3 * h.nb, cudaMemcpyDeviceToHost, ctx->stream));
     CU(cudaStreamSynchronize(ctx->stream));
     return MECH_OK;
 }
@@ -1058,6 +1060,73 @@ int32_t mech_get_stretch_forces(MechContext* ctx, int32_t r, double* linker_f, d
     if (motor_f && h.nmt > 0)
         CU(cudaMemcpy(motor_f, ctx->mt_sf.as<double>() + h.mt_begin, sizeof(double) * h.nmt, cudaMemcpyDeviceToHost));
     return MECH_OK;
+}
+
+int32_t mech_reset_coords(MechContext* ctx) {
+    if (!ctx) return set_err(MECH_ERR_ARG, "null context");
+    if (!ctx->have_net) return set_err(MECH_ERR_STATE, "no network");
+    CU(cudaSetDevice(ctx->device));
+    int rc;
+    if ((rc = pull_states(ctx))) return rc;
+    for (int r = 0; r < ctx->R; ++r) ctx->h_st[r].xbuf = 0;
+    if ((rc = push_states(ctx))) return rc;
+    CU(cudaMemcpyAsync(ctx->x[0].p, ctx->xinit.p, sizeof(double) * 3 * (size_t)ctx->nb, cudaMemcpyDeviceToDevice,
+                       ctx->stream));
+    CU(cudaStreamSynchronize(ctx->stream));
+    return MECH_OK;
+}
+
+}  // extern "C"
+
+template <typename Real>
+static int profile_impl(MechContext* c, int iters, MechProfile* o) {
+    int rc;
+    if (!c->have_lists && (rc = rebuild(c, 0.0, nullptr))) return rc;
+    if ((rc = pull_states(c))) return rc;
+    for (int r = 0; r < c->R; ++r) c->h_st[r].active = 1;
+    if ((rc = push_states(c))) return rc;
+    const DevNet<Real> n = make_devnet<Real>(c);
+    cudaStream_t s = c->stream;
+    cudaEvent_t e0, e1;
+    CU(cudaEventCreate(&e0));
+    CU(cudaEventCreate(&e1));
+    auto timeit = [&](auto&& fn) -> double {
+        fn();   // warm
+        cudaEventRecord(e0, s);
+        for (int i = 0; i < iters; ++i) fn();
+        cudaEventRecord(e1, s);
+        cudaEventSynchronize(e1);
+        float ms = 0.f;
+        cudaEventElapsedTime(&ms, e0, e1);
+        return ms / iters;
+    };
+    o->ms_energy_eval = timeit([&] { launch_energy<Real>(n, -1, 0, s); });
+    o->ms_force_eval = timeit([&] { launch_forces<Real>(n, -1, s); });
+    o->ms_fil_energy = timeit([&] { launch_part<Real>(n, 0, s); });
+    o->ms_fil_force = timeit([&] { launch_part<Real>(n, 1, s); });
+    o->ms_bond_energy = timeit([&] { launch_part<Real>(n, 2, s); });
+    o->ms_bond_force = timeit([&] { launch_part<Real>(n, 3, s); });
+    o->ms_exvol_energy = timeit([&] { launch_exvol_energy<Real>(n, -1, 0, s); });
+    o->ms_exvol_force = timeit([&] { launch_exvol_forces<Real>(n, -1, s); });
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    CU(cudaGetLastError());
+    o->n_beads = c->nb;
+    o->n_exvol_pairs = c->nev;
+    o->n_boundary = c->nbb;
+    o->n_linkers = c->nlk;
+    o->n_motors = c->nmt;
+    o->n_slots = c->slot_base[K_NUM_SPARSE];
+    return pull_states(c);
+}
+
+extern "C" {
+
+int32_t mech_profile(MechContext* ctx, int32_t iters, MechProfile* out) {
+    if (!ctx || !out || iters <= 0) return set_err(MECH_ERR_ARG, "bad argument");
+    if (!ctx->have_net) return set_err(MECH_ERR_STATE, "no network");
+    CU(cudaSetDevice(ctx->device));
+    return ctx->precision == MECH_PREC_FP64 ? profile_impl<double>(ctx, iters, out) : profile_impl<float>(ctx, iters, out);
 }
 
 int32_t mech_get_timing(MechContext* ctx, MechTiming* t) {

@@ -165,6 +165,9 @@ template <typename Real> int launch_reset(const DevNet<Real>& n, cudaStream_t s)
 template <typename Real> int launch_dispatch_failed(const DevNet<Real>& n, cudaStream_t s);
 template <typename Real> int launch_recover(const DevNet<Real>& n, cudaStream_t s);
 template <typename Real> int launch_backup_restore(const DevNet<Real>& n, cudaStream_t s);
+// single kernel families in plain-evaluation mode, for profiling:
+// 0 filament energy, 1 filament force, 2 bond/boundary energy, 3 bond/boundary force
+template <typename Real> int launch_part(const DevNet<Real>& n, int which, cudaStream_t s);
 // excluded-volume kernels (mech_exvol.cu, one object per precision)
 template <typename Real> int launch_exvol_energy(const DevNet<Real>& n, int want, int trial, cudaStream_t s);
 template <typename Real> int launch_exvol_forces(const DevNet<Real>& n, int want, cudaStream_t s);

@@ -14,7 +14,7 @@ from typing import Sequence
 import numpy as np
 
 from . import _lib
-from ._lib import MechCGParams, MechListInfo, MechNetwork, MechResult, MechTiming, check
+from ._lib import MechCGParams, MechListInfo, MechNetwork, MechProfile, MechResult, MechTiming, check
 
 _dp = C.POINTER(C.c_double)
 _i32p = C.POINTER(C.c_int32)
@@ -176,6 +176,14 @@ class Engine:
         if rc not in (_lib.MECH_OK, -5):
             check(rc)
         return [r.as_dict() for r in res]
+
+    def reset_coords(self) -> None:
+        check(self._L.mech_reset_coords(self._ctx))
+
+    def profile(self, iters: int = 20) -> dict:
+        p = MechProfile()
+        check(self._L.mech_profile(self._ctx, int(iters), C.byref(p)))
+        return {k: getattr(p, k) for k, _ in p._fields_}
 
     def timing(self) -> dict:
         t = MechTiming()

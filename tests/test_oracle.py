@@ -268,3 +268,39 @@ def test_cg_reduces_energy_and_stops_on_a_criterion():
     assert res.energiesAfter[6] < res.energiesBefore[6]
     assert res.gradInfNorm < res.gradTol or res.energyRelChange < res.energyRelTol
     assert np.isclose(np.abs(f).max(), res.gradInfNorm)
+
+
+def test_series_atan_accuracy():
+    """The series arctangent shared with the GPU FP64 kernel is within 3 ulp of numpy's."""
+    L = oracle.lib()
+    xs = np.concatenate([np.linspace(-40, 40, 40001), np.logspace(-300, 300, 4001), -np.logspace(-8, 8, 401),
+                         [0.0, 1.0, np.tan(np.pi / 12), 1e308]])
+    ys = np.array([L.orc_series_atan(float(x)) for x in xs])
+    ref = np.arctan(xs)
+    ulp = np.abs(ys - ref) / np.spacing(np.abs(ref) + 1e-300)
+    assert ulp.max() <= 3.0
+    assert L.orc_series_atan(float("inf")) == np.pi / 2
+
+
+def test_oracle_atan_sensitivity():
+    """C-library vs series arctangent in the excluded-volume formula: the
+    reference's own libm sensitivity (energies ~1e-14, forces up to ~1e-9 of
+    the contribution scale on nearly coplanar pairs)."""
+    net = make_network("c1")
+    v = oracle.vectorize(net)
+    e1, p1 = oracle.energies(v, net.coord)
+    f1 = oracle.forces(v, net.coord)
+    with oracle.series_atan_mode():
+        e2, p2 = oracle.energies(v, net.coord)
+        f2 = oracle.forces(v, net.coord)
+    s = oracle.force_scale(v, net.coord)
+    assert abs(p1[4] - p2[4]) <= 1e-12 * abs(p1[4])
+    assert np.all(np.abs(f1 - f2) <= 1e-8 * s + 1e-9)
+
+
+def test_force_scale_bounds_forces():
+    net = jitter(make_network("c1", n_motors=50), 0.4)
+    v = oracle.vectorize(net)
+    f = oracle.forces(v, net.coord)
+    s = oracle.force_scale(v, net.coord)
+    assert np.all(np.abs(f) <= s * (1 + 1e-12) + 1e-12)
