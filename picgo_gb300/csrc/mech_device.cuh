@@ -59,6 +59,28 @@ __device__ __forceinline__ double block_max(double v, double* sh) {
     return r;
 }
 
+// Combine per-warp results (valid in lane 0 of each warp) over the block in a
+// fixed order; results valid in thread 0.  op[k]: 0 sum, 1 max.
+// `sh` holds at least 32 * N doubles.
+template <int N>
+__device__ __forceinline__ void block_combine(double (&w)[N], const int (&op)[N], double* sh) {
+    const int wi = threadIdx.x >> 5, l = threadIdx.x & 31, nw = blockDim.x >> 5;
+    __syncthreads();
+    if (l == 0) {
+#pragma unroll
+        for (int k = 0; k < N; ++k) sh[k * 32 + wi] = w[k];
+    }
+    __syncthreads();
+    if (wi == 0) {
+#pragma unroll
+        for (int k = 0; k < N; ++k) {
+            double r = l < nw ? sh[k * 32 + l] : (op[k] ? -1.0 / 0.0 : 0.0);
+            r = op[k] ? warp_max(r) : warp_sum(r);
+            w[k] = r;
+        }
+    }
+}
+
 // Deterministic sum of part[i * stride + off] for i in [b, e), whole block; result in thread 0.
 __device__ __forceinline__ double sum_slots(const double* part, int stride, int off, int b, int e, double* sh) {
     double acc = 0.0;
@@ -155,34 +177,180 @@ __device__ __forceinline__ void line_search_step(CGState& S, double E) {
 }
 
 // ---------------------------------------------------------------------------
-// Bead loads.
+// Bead positions.  FP64 engine: three doubles per bead.  Mixed engine: each
+// component is an unevaluated sum hi + lo of two floats (about 48 significant
+// bits), so positions, trial moves and difference vectors need no FP64
+// arithmetic, which runs at 1/57 of the FP32 rate on this GPU.  Both formats
+// take 24 bytes per bead.
 // ---------------------------------------------------------------------------
-template <typename Real>
-__device__ __forceinline__ void bead_pos(const double* X, const Real* D, int b, bool trial, double lam, double p[3]) {
-    const double* xb = X + 3 * (size_t)b;
-    if (trial) {
-        const Real* db = D + 3 * (size_t)b;
-        p[0] = fma(lam, (double)db[0], xb[0]);
-        p[1] = fma(lam, (double)db[1], xb[1]);
-        p[2] = fma(lam, (double)db[2], xb[2]);
-    } else {
-        p[0] = xb[0];
-        p[1] = xb[1];
-        p[2] = xb[2];
+template <typename Real> struct Pos;
+template <> struct Pos<double> { double x[3]; };
+template <> struct Pos<float> { float h[3], l[3]; };
+
+__device__ __forceinline__ void two_sum(float a, float b, float& s, float& e) {
+    s = a + b;
+    const float bb = s - a;
+    e = (a - (s - bb)) + (b - bb);
+}
+__device__ __forceinline__ void fast_two_sum(float a, float b, float& s, float& e) {
+    s = a + b;
+    e = b - (s - a);
+}
+
+__device__ __forceinline__ Pos<double> load_pos(const double* X, int b) {
+    Pos<double> p;
+    const double* q = X + 3 * (size_t)b;
+    p.x[0] = q[0]; p.x[1] = q[1]; p.x[2] = q[2];
+    return p;
+}
+__device__ __forceinline__ Pos<float> load_pos(const float* X, int b) {
+    Pos<float> p;
+    const float2* q = reinterpret_cast<const float2*>(X + 6 * (size_t)b);
+    const float2 a = q[0], c = q[1], e = q[2];
+    p.h[0] = a.x; p.h[1] = a.y; p.h[2] = c.x; p.l[0] = c.y; p.l[1] = e.x; p.l[2] = e.y;
+    return p;
+}
+__device__ __forceinline__ void store_pos(double* X, int b, const Pos<double>& p) {
+    double* q = X + 3 * (size_t)b;
+    q[0] = p.x[0]; q[1] = p.x[1]; q[2] = p.x[2];
+}
+__device__ __forceinline__ void store_pos(float* X, int b, const Pos<float>& p) {
+    float2* q = reinterpret_cast<float2*>(X + 6 * (size_t)b);
+    q[0] = make_float2(p.h[0], p.h[1]);
+    q[1] = make_float2(p.h[2], p.l[0]);
+    q[2] = make_float2(p.l[1], p.l[2]);
+}
+
+// x + lambda d (CGMethod.cpp:43-46).  Every kernel that needs the trial
+// position uses these, so the materialized trial coordinates and the ones
+// formed on the fly are identical.
+__device__ __forceinline__ Pos<double> moved(const Pos<double>& p, const double* D, int b, double lam) {
+    Pos<double> o;
+    const double* d = D + 3 * (size_t)b;
+#pragma unroll
+    for (int k = 0; k < 3; ++k) o.x[k] = fma(lam, d[k], p.x[k]);
+    return o;
+}
+__device__ __forceinline__ Pos<float> moved(const Pos<float>& p, const float* D, int b, double lam) {
+    Pos<float> o;
+    const float* d = D + 3 * (size_t)b;
+    const float lf = (float)lam;
+#pragma unroll
+    for (int k = 0; k < 3; ++k) {
+        float s, e, lo;
+        two_sum(p.h[k], __fmul_rn(lf, d[k]), s, e);
+        lo = __fadd_rn(p.l[k], e);
+        fast_two_sum(s, lo, o.h[k], o.l[k]);
     }
+    return o;
+}
+
+template <typename Real>
+__device__ __forceinline__ Pos<Real> bead_at(const Real* X, const Real* D, int b, bool trial, double lam) {
+    const Pos<Real> p = load_pos(X, b);
+    return trial ? moved(p, D, b, lam) : p;
+}
+
+// a - b as Real
+__device__ __forceinline__ void pdiff(const Pos<double>& a, const Pos<double>& b, double r[3]) {
+    r[0] = a.x[0] - b.x[0]; r[1] = a.x[1] - b.x[1]; r[2] = a.x[2] - b.x[2];
+}
+__device__ __forceinline__ void pdiff(const Pos<float>& a, const Pos<float>& b, float r[3]) {
+#pragma unroll
+    for (int k = 0; k < 3; ++k) r[k] = __fadd_rn(__fsub_rn(a.h[k], b.h[k]), __fsub_rn(a.l[k], b.l[k]));
+}
+__device__ __forceinline__ void to_double(const Pos<double>& p, double o[3]) { o[0] = p.x[0]; o[1] = p.x[1]; o[2] = p.x[2]; }
+__device__ __forceinline__ void to_double(const Pos<float>& p, double o[3]) {
+#pragma unroll
+    for (int k = 0; k < 3; ++k) o[k] = (double)p.h[k] + (double)p.l[k];   // exact
+}
+__device__ __forceinline__ Pos<float> split(const double x[3]) {
+    Pos<float> p;
+#pragma unroll
+    for (int k = 0; k < 3; ++k) {
+        p.h[k] = (float)x[k];
+        p.l[k] = (float)(x[k] - (double)p.h[k]);
+    }
+    return p;
+}
+
+// ---------------------------------------------------------------------------
+// Reductions of per-thread values of the engine's precision.  FP64: plain
+// double tree.  Mixed: float pairs (hi, lo) summed with error-free
+// transformations within each warp, then double across warps and tiles.
+// ---------------------------------------------------------------------------
+__device__ __forceinline__ double warp_sum_ff(float v) {
+    float s = v, e = 0.f;
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) {
+        const float s2 = __shfl_down_sync(0xffffffffu, s, o), e2 = __shfl_down_sync(0xffffffffu, e, o);
+        float t, te;
+        two_sum(s, s2, t, te);
+        te = __fadd_rn(te, __fadd_rn(e, e2));
+        fast_two_sum(t, te, s, e);
+    }
+    return (double)s + (double)e;
+}
+__device__ __forceinline__ double warp_sum_r(double v) { return warp_sum(v); }
+__device__ __forceinline__ double warp_sum_r(float v) { return warp_sum_ff(v); }
+__device__ __forceinline__ double warp_max_r(double v) { return warp_max(v); }
+__device__ __forceinline__ double warp_max_r(float v) {
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) v = fmaxf(v, __shfl_down_sync(0xffffffffu, v, o));
+    return (double)v;
+}
+__device__ __forceinline__ double block_sum_r(double v, double* sh) { return block_sum(v, sh); }
+__device__ __forceinline__ double block_sum_r(float v, double* sh) {
+    const double w = warp_sum_ff(v);
+    const int wi = threadIdx.x >> 5, l = threadIdx.x & 31;
+    __syncthreads();
+    if (l == 0) sh[wi] = w;
+    __syncthreads();
+    double r = 0.0;
+    if (wi == 0) {
+        r = (l < (blockDim.x >> 5)) ? sh[l] : 0.0;
+        r = warp_sum(r);
+    }
+    return r;
+}
+__device__ __forceinline__ double block_max_r(double v, double* sh) { return block_max(v, sh); }
+__device__ __forceinline__ double block_max_r(float v, double* sh) {
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) v = fmaxf(v, __shfl_down_sync(0xffffffffu, v, o));
+    const int wi = threadIdx.x >> 5, l = threadIdx.x & 31;
+    __syncthreads();
+    if (l == 0) sh[wi] = (double)v;
+    __syncthreads();
+    double r = 0.0;
+    if (wi == 0) {
+        r = (l < (blockDim.x >> 5)) ? sh[l] : 0.0;
+        r = warp_max(r);
+    }
+    return r;
 }
 
 __device__ __forceinline__ bool near_zero_theta(double t) { return fabs(t - 0.0) < 1e-6; }  // areEqual (utility.h:75-78)
+
+// the four filament constants of a bead slot in one vector load
+__device__ __forceinline__ void load_par(const float* P, int j, float& ks, float& l0, float& kb, float& t0) {
+    const float4 v = reinterpret_cast<const float4*>(P)[j];
+    ks = v.x; l0 = v.y; kb = v.z; t0 = v.w;
+}
+__device__ __forceinline__ void load_par(const double* P, int j, double& ks, double& l0, double& kb, double& t0) {
+    const double2 a = reinterpret_cast<const double2*>(P)[2 * (size_t)j];
+    const double2 b = reinterpret_cast<const double2*>(P)[2 * (size_t)j + 1];
+    ks = a.x; l0 = a.y; kb = b.x; t0 = b.y;
+}
 
 // ---------------------------------------------------------------------------
 // Filament stretching (FilamentStretchingHarmonic.cpp:185-275) and cosine
 // bending (FilamentBendingCosine.cpp:199-345) on difference vectors.
 // ---------------------------------------------------------------------------
 template <typename Real>
-__device__ __forceinline__ double stretch_energy(Real rx, Real ry, Real rz, Real k, Real l0) {
+__device__ __forceinline__ Real stretch_energy(Real rx, Real ry, Real rz, Real k, Real l0) {
     const Real L = sqrt(rx * rx + ry * ry + rz * rz);
     const Real dl = L - l0;
-    return (double)((Real)0.5 * k * dl * dl);
+    return (Real)0.5 * k * dl * dl;
 }
 
 // Force on the second bead (the first gets the negation).
@@ -197,7 +365,7 @@ __device__ __forceinline__ void stretch_force(Real rx, Real ry, Real rz, Real k,
 }
 
 template <typename Real>
-__device__ __forceinline__ double bend_energy(const Real r1[3], const Real r2[3], Real k, Real t0) {
+__device__ __forceinline__ Real bend_energy(const Real r1[3], const Real r2[3], Real k, Real t0) {
     const Real L1sq = r1[0] * r1[0] + r1[1] * r1[1] + r1[2] * r1[2];
     const Real L2sq = r2[0] * r2[0] + r2[1] * r2[1] + r2[2] * r2[2];
     const Real l1l2 = r1[0] * r2[0] + r1[1] * r2[1] + r1[2] * r2[2];
@@ -212,14 +380,14 @@ __device__ __forceinline__ double bend_energy(const Real r1[3], const Real r2[3]
             const Real cy = r1[2] * r2[0] - r1[0] * r2[2];
             const Real cz = r1[0] * r2[1] - r1[1] * r2[0];
             const Real om = (cx * cx + cy * cy + cz * cz) / (L1L2 * (L1L2 + l1l2));
-            return (double)(k * om);
+            return k * om;
         }
-        return (double)(k * ((Real)1 - x));
+        return k * ((Real)1 - x);
     }
     const Real cosA = x;
     const Real sinA = fmax(sqrt((Real)1 - cosA * cosA), (Real)0);
     const Real cAmB = cosA * cos(t0) + sinA * sin(t0);
-    return (double)(k * ((Real)1 - cAmB));
+    return k * ((Real)1 - cAmB);
 }
 
 // Fr1, Fr2 of the reference: forces are b1: -Fr1, b2: Fr1 - Fr2, b3: Fr2.

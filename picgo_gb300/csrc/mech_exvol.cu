@@ -7,11 +7,14 @@
 // float).  The FP64 object is built without FMA contraction: the formula is
 // ill-conditioned for nearly coplanar pairs, and rounding each operation as
 // written keeps the GPU within a few ulps of the CPU restatement there.  In
-// mixed precision the pair geometry is single precision; pairs whose
-// coplanarity measure |n . v3| falls under kMixedFp64Coplanar are evaluated in
-// FP64, because the 1/JJ * (sum) form loses about 1/|n.v3|^2 of its relative
-// accuracy, and the reference's own coplanar move (|n . v3| < 0.1) is then
-// always decided in FP64.
+// mixed precision the pair geometry is single precision, with cancellation-free
+// cross-product forms of the invariants; the 1/JJ * (sum) form still loses
+// accuracy as the normalized triple product q = |(v12 x v34) . v31| /
+// (|v12| |v34| |v31|) goes to zero (nearly coplanar or nearly touching
+// segments), so pairs with q under a threshold are evaluated in FP64 by a
+// second pass over a compacted list.  Nearly coplanar pairs, the only ones the
+// reference moves off their plane (|n . v3| < 0.1 implies a small q), are then
+// always decided and moved in FP64.
 #include <cuda_runtime.h>
 
 #include "mech_device.cuh"
@@ -22,7 +25,6 @@
 
 namespace mech {
 
-constexpr float kMixedFp64Coplanar = 0.3f;
 constexpr int kFbNodesEnergy = 400;       // Simpson intervals, energy (:929-930)
 constexpr int kFbNodesForce = 10000;      // Simpson intervals, forces (:1041-1042)
 
@@ -69,20 +71,15 @@ __device__ __forceinline__ T dot3(const T* u, const T* v) {
     return u[0] * v[0] + u[1] * v[1] + u[2] * v[2];
 }
 
-// Scalar products and the AA..JJ terms (:355-420).  Differences of positions
-// are taken in double, then rounded to T.
+// Scalar products and the AA..JJ terms (:355-420) from the difference
+// vectors v12 = c2 - c1, v34 = c4 - c3, v31 = c1 - c3, v14 = c4 - c1,
+// v32 = c2 - c3.  `cross` selects the forms used in single precision: by
+// Lagrange's identity AA = |v12 x v31|, BB = |v34 x v31|, EE = |v12 x v14|,
+// FF = |v34 x v32|, and CC, DD, GG are dot products of cross products, which
+// avoids the cancellation of the reference's sqrt((ac + e)(ac - e)) forms.
 template <typename T>
-__device__ __forceinline__ void pair_inv(const double* c1, const double* c2, const double* c3, const double* c4,
-                                         PairInv<T>& p) {
-    T v12[3], v34[3], v31[3], v14[3], v32[3];
-#pragma unroll
-    for (int k = 0; k < 3; ++k) {
-        v12[k] = (T)(c2[k] - c1[k]);
-        v34[k] = (T)(c4[k] - c3[k]);
-        v31[k] = (T)(c1[k] - c3[k]);
-        v14[k] = (T)(c4[k] - c1[k]);
-        v32[k] = (T)(c2[k] - c3[k]);
-    }
+__device__ __forceinline__ void pair_inv(const T* v12, const T* v34, const T* v31, const T* v14, const T* v32,
+                                         PairInv<T>& p, bool cross) {
     p.a = dot3(v12, v12);
     p.b = dot3(v34, v34);
     p.c = dot3(v31, v31);
@@ -94,21 +91,38 @@ __device__ __forceinline__ void pair_inv(const double* c1, const double* c2, con
     p.I = dot3(v34, v14);
     p.D2 = dot3(v14, v14);
     p.E2 = dot3(v32, v32);
-    const T ac = sqrt(p.a * p.c), bc = sqrt(p.b * p.c), aD = sqrt(p.a * p.D2), bE = sqrt(p.b * p.E2);
-    p.AA = sqrt(fmax((T)0, (ac + p.e) * (ac - p.e)));
-    p.BB = sqrt(fmax((T)0, (bc + p.F) * (bc - p.F)));
-    p.CC = p.d * p.e - p.a * p.F;
-    p.DD = p.b * p.e - p.d * p.F;
-    p.EE = sqrt(fmax((T)0, (aD + p.g) * (aD - p.g)));
-    p.FF = sqrt(fmax((T)0, (bE + p.h) * (bE - p.h)));
-    p.GG = p.d * p.g - p.a * p.I;
-    p.HH = p.CC + p.GG - p.DD;
     // (c1 - c2) x (c3 - c4) . (c3 - c1) = (v12 x v34) . v31 up to sign; squared
-    const T cx = v12[1] * v34[2] - v12[2] * v34[1];
-    const T cy = v12[2] * v34[0] - v12[0] * v34[2];
-    const T cz = v12[0] * v34[1] - v12[1] * v34[0];
-    const T trip = cx * v31[0] + cy * v31[1] + cz * v31[2];
+    const T x21[3] = {v34[1] * v12[2] - v34[2] * v12[1], v34[2] * v12[0] - v34[0] * v12[2],
+                      v34[0] * v12[1] - v34[1] * v12[0]};
+    const T trip = -(x21[0] * v31[0] + x21[1] * v31[1] + x21[2] * v31[2]);
     p.JJ = -trip * trip;
+    if (cross) {
+        const T x13[3] = {v12[1] * v31[2] - v12[2] * v31[1], v12[2] * v31[0] - v12[0] * v31[2],
+                          v12[0] * v31[1] - v12[1] * v31[0]};
+        const T x23[3] = {v34[1] * v31[2] - v34[2] * v31[1], v34[2] * v31[0] - v34[0] * v31[2],
+                          v34[0] * v31[1] - v34[1] * v31[0]};
+        const T x14[3] = {v12[1] * v14[2] - v12[2] * v14[1], v12[2] * v14[0] - v12[0] * v14[2],
+                          v12[0] * v14[1] - v12[1] * v14[0]};
+        const T x32[3] = {v34[1] * v32[2] - v34[2] * v32[1], v34[2] * v32[0] - v34[0] * v32[2],
+                          v34[0] * v32[1] - v34[1] * v32[0]};
+        p.AA = sqrt(dot3(x13, x13));
+        p.BB = sqrt(dot3(x23, x23));
+        p.EE = sqrt(dot3(x14, x14));
+        p.FF = sqrt(dot3(x32, x32));
+        p.CC = dot3(x13, x21);
+        p.DD = dot3(x21, x23);
+        p.GG = dot3(x14, x21);
+    } else {
+        const T ac = sqrt(p.a * p.c), bc = sqrt(p.b * p.c), aD = sqrt(p.a * p.D2), bE = sqrt(p.b * p.E2);
+        p.AA = sqrt(fmax((T)0, (ac + p.e) * (ac - p.e)));
+        p.BB = sqrt(fmax((T)0, (bc + p.F) * (bc - p.F)));
+        p.CC = p.d * p.e - p.a * p.F;
+        p.DD = p.b * p.e - p.d * p.F;
+        p.EE = sqrt(fmax((T)0, (aD + p.g) * (aD - p.g)));
+        p.FF = sqrt(fmax((T)0, (bE + p.h) * (bE - p.h)));
+        p.GG = p.d * p.g - p.a * p.I;
+    }
+    p.HH = p.CC + p.GG - p.DD;
     p.ATG1 = atan_of((p.a + p.e) / p.AA) - atan_of(p.e / p.AA);
     p.ATG2 = atan_of((p.a + p.e - p.d) / p.EE) - atan_of((p.e - p.d) / p.EE);
     p.ATG3 = atan_of((p.F) / p.BB) - atan_of((p.F - p.b) / p.BB);
@@ -116,17 +130,35 @@ __device__ __forceinline__ void pair_inv(const double* c1, const double* c2, con
 }
 
 template <typename T>
+__device__ __forceinline__ void diffs_of(const double* c1, const double* c2, const double* c3, const double* c4, T* v12,
+                                         T* v34, T* v31, T* v14, T* v32) {
+#pragma unroll
+    for (int k = 0; k < 3; ++k) {
+        v12[k] = (T)(c2[k] - c1[k]);
+        v34[k] = (T)(c4[k] - c3[k]);
+        v31[k] = (T)(c1[k] - c3[k]);
+        v14[k] = (T)(c4[k] - c1[k]);
+        v32[k] = (T)(c2[k] - c3[k]);
+    }
+}
+
+template <typename T>
 __device__ __forceinline__ bool bad_value(T x) { return !(fabs(x) < (T)(1.0 / 0.0)); }
 
-// Analytic pair energy (:427-436); returns NaN when unusable (inf, NaN or < -1).
+// Analytic pair energy (:427-436); NaN when unusable (inf, NaN or < -1).
 template <typename T>
-__device__ double pair_energy(const double* c1, const double* c2, const double* c3, const double* c4, T kRepScaled) {
-    PairInv<T> p;
-    pair_inv<T>(c1, c2, c3, c4, p);
+__device__ __forceinline__ double energy_from(const PairInv<T>& p, T kRepScaled) {
     const T U = (T)0.5 * kRepScaled / p.JJ *
                 (p.CC / p.AA * p.ATG1 + p.GG / p.EE * p.ATG2 + p.DD / p.BB * p.ATG3 + p.HH / p.FF * p.ATG4);
     if (bad_value(U) || U < (T)-1) return __longlong_as_double(0x7ff8000000000000ULL);
     return (double)U;
+}
+static __device__ double pair_energy_d(const double* c1, const double* c2, const double* c3, const double* c4, double kRep) {
+    double v12[3], v34[3], v31[3], v14[3], v32[3];
+    diffs_of(c1, c2, c3, c4, v12, v34, v31, v14, v32);
+    PairInv<double> p;
+    pair_inv(v12, v34, v31, v14, v32, p, false);
+    return energy_from(p, kRep);
 }
 
 // |n_hat . v3_hat| of areInPlane (MathFunctions.h:1101-1134), n = (c2-c1) x (c3-c1), v3 = c4 - c1.
@@ -163,13 +195,10 @@ __device__ __forceinline__ void push_c1(const double* c1, const double* c2, cons
     for (int k = 0; k < 3; ++k) out[k] = (c1[k] + (n[k] / nn) * 0.01);
 }
 
-// Analytic forces (:597-860) on the given (possibly moved) beads; returns
-// false when a component is not finite.
+// Analytic forces (:597-860) from the invariants and v1 = c2 - c1,
+// v2 = c4 - c3, v3 = c1 - c3; returns false when a component is not finite.
 template <typename T>
-__device__ bool pair_forces(const double* c1, const double* c2, const double* c3, const double* c4, T kRepScaled,
-                            T out[4][3]) {
-    PairInv<T> p;
-    pair_inv<T>(c1, c2, c3, c4, p);
+__device__ bool forces_from(const PairInv<T>& p, const T* v1, const T* v2, const T* v3, T kRepScaled, T out[4][3]) {
     const T a = p.a, b = p.b, c = p.c, d = p.d, e = p.e, F = p.F;
     const T AA = p.AA, BB = p.BB, CC = p.CC, DD = p.DD, EE = p.EE, FF = p.FF, GG = p.GG, HH = p.HH;
     const T invJJ = (T)1 / p.JJ;
@@ -225,13 +254,6 @@ __device__ bool pair_forces(const double* c1, const double* c2, const double* c3
     J[2][0] = J[0][2];
     J[2][1] = J[1][2];
     J[2][2] = 2 * (d * d - a * b);
-    T v1[3], v2[3], v3[3];
-#pragma unroll
-    for (int k = 0; k < 3; ++k) {
-        v1[k] = (T)(c2[k] - c1[k]);
-        v2[k] = (T)(c4[k] - c3[k]);
-        v3[k] = (T)(c1[k] - c3[k]);
-    }
     bool ok = true;
     T dv[4][3];
 #pragma unroll
@@ -249,6 +271,23 @@ __device__ bool pair_forces(const double* c1, const double* c2, const double* c3
             if (bad_value(out[q][k])) ok = false;
         }
     return ok;
+}
+
+// FP64 forces of a pair at double positions, with the reference's coplanar
+// move of c2 (:610-626, force path only).
+static __device__ bool pair_forces_d(const double* c1, const double* c2in, const double* c3, const double* c4, double kRep,
+                              double out[4][3]) {
+    double moved2[3];
+    const double* c2 = c2in;
+    if (coplanarity<double>(c1, c2in, c3, c4) < 0.1) {
+        push_c2(c1, c2in, c3, moved2);
+        c2 = moved2;
+    }
+    double v12[3], v34[3], v31[3], v14[3], v32[3];
+    diffs_of(c1, c2, c3, c4, v12, v34, v31, v14, v32);
+    PairInv<double> p;
+    pair_inv(v12, v34, v31, v14, v32, p, false);
+    return forces_from(p, v12, v34, v31, kRep, out);
 }
 
 // ---------------------------------------------------------------------------
@@ -281,15 +320,14 @@ __global__ void __launch_bounds__(kBlock) k_exvol_fb_energy(DevNet<Real> n) {
         const int pr = n.ev_fb_list[2 * k + 1];
         const int4 bs = n.ev_bead[pr];
         const CGState& S = n.st[n.ev_fb_list[2 * k]];
-        // positions of this evaluation (trial flag stored in the list entry's sign bit of the count is not
-        // needed: the list is filled by the same launch sequence, with lambda stored alongside)
+        // positions of this evaluation: the entry records the trial lambda (0: plain evaluation)
         const double lam = __longlong_as_double(((const long long*)n.ev_fb_energy)[kExvolFallbackCap + k]);
         const bool tr = lam != 0.0;
         double c1[3], c2[3], c3[3], c4[3];
-        bead_pos(n.x[S.xbuf], n.d, bs.x, tr, lam, c1);
-        bead_pos(n.x[S.xbuf], n.d, bs.y, tr, lam, c2);
-        bead_pos(n.x[S.xbuf], n.d, bs.z, tr, lam, c3);
-        bead_pos(n.x[S.xbuf], n.d, bs.w, tr, lam, c4);
+        to_double(bead_at(n.x[S.xbuf], n.d, bs.x, tr, lam), c1);
+        to_double(bead_at(n.x[S.xbuf], n.d, bs.y, tr, lam), c2);
+        to_double(bead_at(n.x[S.xbuf], n.d, bs.z, tr, lam), c3);
+        to_double(bead_at(n.x[S.xbuf], n.d, bs.w, tr, lam), c4);
         const Quad q = quad_of(c1, c2, c3, c4);
         const int N = kFbNodesEnergy;
         double acc = 0.0;
@@ -321,12 +359,12 @@ __global__ void __launch_bounds__(kBlock) k_exvol_fb_force(DevNet<Real> n, doubl
         const int pr = n.ev_fb_list[2 * k + 1];
         const int4 bs = n.ev_bead[pr];
         const CGState& S = n.st[n.ev_fb_list[2 * k]];
-        const double* X = n.x[S.xbuf];
+        const Real* X = n.x[S.xbuf];
         double c1[3], c2[3], c3[3], c4[3];
-        bead_pos<Real>(X, nullptr, bs.x, false, 0.0, c1);
-        bead_pos<Real>(X, nullptr, bs.y, false, 0.0, c2);
-        bead_pos<Real>(X, nullptr, bs.z, false, 0.0, c3);
-        bead_pos<Real>(X, nullptr, bs.w, false, 0.0, c4);
+        to_double(load_pos(X, bs.x), c1);
+        to_double(load_pos(X, bs.y), c2);
+        to_double(load_pos(X, bs.z), c3);
+        to_double(load_pos(X, bs.w), c4);
         const Quad q = quad_of(c1, c2, c3, c4);
         const int i0 = (int)((long long)(N + 1) * ch / kFbChunks), i1 = (int)((long long)(N + 1) * (ch + 1) / kFbChunks);
         double m[6] = {0, 0, 0, 0, 0, 0};
@@ -400,6 +438,29 @@ __device__ __forceinline__ void flag_fallback(const DevNet<Real>& n, int r, int 
     }
 }
 
+constexpr float kMixedTauEnergy = 0.01f;   // FP64 below this normalized triple product (energy)
+constexpr float kMixedTauForce = 0.05f;    // (forces, whose formula loses more to cancellation)
+
+// Warp-aggregated append of (replica, pair) to the FP64 pair list.
+template <typename Real>
+__device__ __forceinline__ void append_fp64(const DevNet<Real>& n, bool need, int r, int pr) {
+    const unsigned m = __ballot_sync(0xffffffffu, need);
+    if (!m) return;
+    const int lane = threadIdx.x & 31, leader = __ffs(m) - 1;
+    int base = 0;
+    if (lane == leader) base = atomicAdd(n.ev_list_count, __popc(m));
+    base = __shfl_sync(0xffffffffu, base, leader);
+    if (need) {
+        const int k = base + __popc(m & ((1u << lane) - 1u));
+        if (k < n.n_ev) {
+            n.ev_list[2 * k] = r;
+            n.ev_list[2 * k + 1] = pr;
+        } else {
+            atomicOr(n.err, 4u);
+        }
+    }
+}
+
 template <typename Real>
 __global__ void __launch_bounds__(kBlock) k_exvol(DevNet<Real> n, int want, int trial, int force, int tile_off) {
     __shared__ double sh[32];
@@ -416,50 +477,136 @@ __global__ void __launch_bounds__(kBlock) k_exvol(DevNet<Real> n, int want, int 
     }
     __syncthreads();
     if (!s_go) return;
-    const double* X = n.x[s_xb];
+    const Real* X = n.x[s_xb];
     const bool tr = trial != 0;
     const int i = t.begin + threadIdx.x;
+    const bool valid = i < t.end;
     double e = 0.0;
-    if (i < t.end) {
+    bool need64 = false;
+    if (valid) {
         const int4 bs = n.ev_bead[i];
-        double c1[3], c2[3], c3[3], c4[3];
-        bead_pos(X, n.d, bs.x, tr, s_lam, c1);
-        bead_pos(X, n.d, bs.y, tr, s_lam, c2);
-        bead_pos(X, n.d, bs.z, tr, s_lam, c3);
-        bead_pos(X, n.d, bs.w, tr, s_lam, c4);
-        const double kRep = (double)n.ev_k[i] * (double)n.ev_la[i] * (double)n.ev_lb[i];
-        const bool fp32 = sizeof(Real) == 4 && coplanarity<float>(c1, c2, c3, c4) >= kMixedFp64Coplanar;
-        if (!force) {
-            const double u = fp32 ? pair_energy<float>(c1, c2, c3, c4, (float)kRep) : pair_energy<double>(c1, c2, c3, c4, kRep);
-            if (u != u) flag_fallback(n, r, i, tr ? s_lam : 0.0);
-            else e = u;
-        } else {
-            Real* cdst = n.contrib + 3 * (size_t)(n.slot_base[K_EXVOL] + 4 * i);
-            bool ok;
-            if (fp32) {
-                float out[4][3];
-                ok = pair_forces<float>(c1, c2, c3, c4, (float)kRep, out);
-                for (int a = 0; a < 4; ++a)
-                    for (int k = 0; k < 3; ++k) cdst[3 * a + k] = (Real)out[a][k];
+        const Pos<Real> p1 = bead_at(X, n.d, bs.x, tr, s_lam), p2 = bead_at(X, n.d, bs.y, tr, s_lam);
+        const Pos<Real> p3 = bead_at(X, n.d, bs.z, tr, s_lam), p4 = bead_at(X, n.d, bs.w, tr, s_lam);
+        const double kRepD = (double)n.ev_k[i] * (double)n.ev_la[i] * (double)n.ev_lb[i];
+        if constexpr (sizeof(Real) == 8) {
+            // FP64 engine: the reference's formulas, every pair
+            double c1[3], c2[3], c3[3], c4[3];
+            to_double(p1, c1);
+            to_double(p2, c2);
+            to_double(p3, c3);
+            to_double(p4, c4);
+            if (!force) {
+                const double u = pair_energy_d(c1, c2, c3, c4, kRepD);
+                if (u != u) flag_fallback(n, r, i, tr ? s_lam : 0.0);
+                else e = u;
             } else {
-                double moved[3];
-                const double* cc2 = c2;
-                if (coplanarity<double>(c1, c2, c3, c4) < 0.1) {   // force path only (:610-626)
-                    push_c2(c1, c2, c3, moved);
-                    cc2 = moved;
-                }
                 double out[4][3];
-                ok = pair_forces<double>(c1, cc2, c3, c4, kRep, out);
+                const bool ok = pair_forces_d(c1, c2, c3, c4, kRepD, out);
+                Real* cdst = n.contrib + 3 * (size_t)(n.slot_base[K_EXVOL] + 4 * i);
                 for (int a = 0; a < 4; ++a)
                     for (int k = 0; k < 3; ++k) cdst[3 * a + k] = (Real)out[a][k];
+                if (!ok) flag_fallback(n, r, i, 0.0);
             }
-            if (!ok) flag_fallback(n, r, i, 0.0);
+        } else {
+            // mixed engine: single precision unless the pair is ill-conditioned
+            float v12[3], v34[3], v31[3], v14[3], v32[3];
+            pdiff(p2, p1, v12);
+            pdiff(p4, p3, v34);
+            pdiff(p1, p3, v31);
+            pdiff(p4, p1, v14);
+            pdiff(p2, p3, v32);
+            const float cx = v12[1] * v34[2] - v12[2] * v34[1], cy = v12[2] * v34[0] - v12[0] * v34[2],
+                        cz = v12[0] * v34[1] - v12[1] * v34[0];
+            const float trip = fabsf(cx * v31[0] + cy * v31[1] + cz * v31[2]);
+            const float q = trip / (sqrtf(dot3(v12, v12)) * sqrtf(dot3(v34, v34)) * sqrtf(dot3(v31, v31)));
+            need64 = !(q >= (force ? kMixedTauForce : kMixedTauEnergy));
+            if (force && !need64) {
+                // the reference moves c2 off the plane of a pair it judges coplanar
+                // (|n . v3| < 0.1 with n = (c2-c1) x (c3-c1), v3 = c4 - c1); such
+                // pairs, with a margin for single-precision rounding, go to FP64
+                const float nx = v12[1] * v31[2] - v12[2] * v31[1], ny = v12[2] * v31[0] - v12[0] * v31[2],
+                            nz = v12[0] * v31[1] - v12[1] * v31[0];
+                const float cop = fabsf(nx * v14[0] + ny * v14[1] + nz * v14[2]) /
+                                  (sqrtf(nx * nx + ny * ny + nz * nz) * sqrtf(dot3(v14, v14)));
+                need64 = !(cop >= 0.1f + 2e-3f);
+            }
+            if (!need64) {
+                PairInv<float> pi;
+                pair_inv(v12, v34, v31, v14, v32, pi, true);
+                if (!force) {
+                    const double u = energy_from(pi, (float)kRepD);
+                    if (u != u) need64 = true;
+                    else e = u;
+                } else {
+                    float out[4][3];
+                    if (forces_from(pi, v12, v34, v31, (float)kRepD, out)) {
+                        Real* cdst = n.contrib + 3 * (size_t)(n.slot_base[K_EXVOL] + 4 * i);
+                        for (int a = 0; a < 4; ++a)
+                            for (int k = 0; k < 3; ++k) cdst[3 * a + k] = (Real)out[a][k];
+                    } else {
+                        need64 = true;
+                    }
+                }
+            }
+            if (!force) n.ev_energy[i] = need64 ? 0.0 : e;
         }
     }
-    if (!force) {
+    if constexpr (sizeof(Real) == 4) append_fp64(n, need64, r, i);
+    if (!force && sizeof(Real) == 8) {
         e = block_sum(e, sh);
         if (threadIdx.x == 0) n.part_sp[ti] = e;
     }
+}
+
+// Mixed engine: the listed pairs in FP64 with the reference's formulas.
+template <typename Real>
+__global__ void __launch_bounds__(128) k_exvol_fp64(DevNet<Real> n, int trial, int force) {
+    const int cnt = min(*n.ev_list_count, n.n_ev);
+    for (int k = blockIdx.x * blockDim.x + threadIdx.x; k < cnt; k += gridDim.x * blockDim.x) {
+        const int r = n.ev_list[2 * k], i = n.ev_list[2 * k + 1];
+        const CGState& S = n.st[r];
+        const Real* X = n.x[S.xbuf];
+        const bool tr = trial != 0;
+        const double lam = S.lambda;
+        const int4 bs = n.ev_bead[i];
+        double c1[3], c2[3], c3[3], c4[3];
+        to_double(bead_at(X, n.d, bs.x, tr, lam), c1);
+        to_double(bead_at(X, n.d, bs.y, tr, lam), c2);
+        to_double(bead_at(X, n.d, bs.z, tr, lam), c3);
+        to_double(bead_at(X, n.d, bs.w, tr, lam), c4);
+        const double kRepD = (double)n.ev_k[i] * (double)n.ev_la[i] * (double)n.ev_lb[i];
+        if (!force) {
+            const double u = pair_energy_d(c1, c2, c3, c4, kRepD);
+            if (u != u) {
+                flag_fallback(n, r, i, tr ? lam : 0.0);
+                n.ev_energy[i] = 0.0;
+            } else {
+                n.ev_energy[i] = u;
+            }
+        } else {
+            double out[4][3];
+            const bool ok = pair_forces_d(c1, c2, c3, c4, kRepD, out);
+            Real* cdst = n.contrib + 3 * (size_t)(n.slot_base[K_EXVOL] + 4 * i);
+            for (int a = 0; a < 4; ++a)
+                for (int q = 0; q < 3; ++q) cdst[3 * a + q] = (Real)out[a][q];
+            if (!ok) flag_fallback(n, r, i, 0.0);
+        }
+    }
+}
+
+// Mixed engine: deterministic per-tile sums of the per-pair energies.
+template <typename Real>
+__global__ void __launch_bounds__(kBlock) k_exvol_tilesum(DevNet<Real> n, int want, int tile_off) {
+    __shared__ double sh[32];
+    const int ti = tile_off + blockIdx.x;
+    const Tile t = n.stile[ti];
+    const CGState& S = n.st[t.replica];
+    const bool go = want < 0 ? (S.active != 0) : (S.phase == want);
+    if (!go) return;
+    const int i = t.begin + threadIdx.x;
+    double e = i < t.end ? n.ev_energy[i] : 0.0;
+    e = block_sum(e, sh);
+    if (threadIdx.x == 0) n.part_sp[ti] = e;
 }
 
 template <typename Real>
@@ -473,9 +620,21 @@ int launch_exvol_energy(const DevNet<Real>& n, int want, int trial, cudaStream_t
     int off = 0;
     const int nt = ev_tiles_of(n, &off);
     if (nt == 0) return 0;
+    cudaMemsetAsync(n.ev_list_count, 0, sizeof(int), s);
+    cudaMemsetAsync(n.ev_fb_count, 0, sizeof(int), s);
     k_exvol<Real><<<nt, kBlock, 0, s>>>(n, want, trial, 0, off);
+    int k = 1;
+    if (sizeof(Real) == 4) {
+        k_exvol_fp64<Real><<<2 * 152, 128, 0, s>>>(n, trial, 0);
+        ++k;
+    }
     k_exvol_fb_energy<Real><<<64, kBlock, 0, s>>>(n);
-    return 2;
+    ++k;
+    if (sizeof(Real) == 4) {
+        k_exvol_tilesum<Real><<<nt, kBlock, 0, s>>>(n, want, off);
+        ++k;
+    }
+    return k;
 }
 
 template <typename Real>
@@ -483,9 +642,16 @@ int launch_exvol_forces(const DevNet<Real>& n, int want, cudaStream_t s) {
     int off = 0;
     const int nt = ev_tiles_of(n, &off);
     if (nt == 0) return 0;
+    cudaMemsetAsync(n.ev_list_count, 0, sizeof(int), s);
+    cudaMemsetAsync(n.ev_fb_count, 0, sizeof(int), s);
     k_exvol<Real><<<nt, kBlock, 0, s>>>(n, want, 0, 1, off);
+    int k = 1;
+    if (sizeof(Real) == 4) {
+        k_exvol_fp64<Real><<<2 * 152, 128, 0, s>>>(n, 0, 1);
+        ++k;
+    }
     k_exvol_fb_force<Real><<<4 * 152, kBlock, 0, s>>>(n, n.fb_moments, n.fb_tickets);
-    return 2;
+    return k + 1;
 }
 
 template int launch_exvol_energy<MECH_EXVOL_REAL>(const DevNet<MECH_EXVOL_REAL>&, int, int, cudaStream_t);

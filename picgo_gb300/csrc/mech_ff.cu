@@ -23,32 +23,49 @@ namespace mech {
 // ---------------------------------------------------------------------------
 // helpers
 // ---------------------------------------------------------------------------
-template <typename Real>
-__device__ __forceinline__ double bead_dot(Real a0, Real a1, Real a2, Real b0, Real b1, Real b2) {
-    if (sizeof(Real) == 8) return (double)(a0 * b0 + a1 * b1 + a2 * b2);
-    // single precision: the three products of one bead are summed with fused
-    // multiply-adds, the sum over beads is carried in double
-    return (double)fmaf((float)a2, (float)b2, fmaf((float)a1, (float)b1, (float)a0 * (float)b0));
+// the three products of one bead, in the engine's precision; the sum over
+// beads is carried by block_sum_r (compensated within a warp, then double)
+__device__ __forceinline__ double bead_dot(double a0, double a1, double a2, double b0, double b1, double b2) {
+    return a0 * b0 + a1 * b1 + a2 * b2;
+}
+__device__ __forceinline__ float bead_dot(float a0, float a1, float a2, float b0, float b1, float b2) {
+    return fmaf(a2, b2, fmaf(a1, b1, a0 * b0));
+}
+
+// plane distance of a position (BoundaryElementImpl.h:49-53)
+__device__ __forceinline__ double plane_dist_p(const double* pl, const Pos<double>& p) { return plane_dist(pl, p.x); }
+__device__ __forceinline__ float plane_dist_p(const double* pl, const Pos<float>& p) {
+    const float a = (float)pl[0], b = (float)pl[1], c = (float)pl[2], d = (float)pl[3];
+    const float hi = a * p.h[0] + b * p.h[1] + c * p.h[2] + d;
+    const float lo = a * p.l[0] + b * p.l[1] + c * p.l[2];
+    return (hi + lo) / sqrtf(a * a + b * b + c * c);
+}
+
+// vector from the point at s1 on (c1, c2) to the point at s2 on (c3, c4)
+// (LinkerStretchingHarmonic.cpp:200-216).  FP64: the interpolated points
+// themselves, as the reference; mixed: the same vector from differences only,
+// (c3 - c1) + s2 (c4 - c3) - s1 (c2 - c1).
+__device__ __forceinline__ void bond_vector(const Pos<double>& c1, const Pos<double>& c2, const Pos<double>& c3,
+                                            const Pos<double>& c4, double s1, double s2, double v[3]) {
+    double p1[3], p2[3];
+    lerp3(c1.x, c2.x, s1, p1);
+    lerp3(c3.x, c4.x, s2, p2);
+    v[0] = p2[0] - p1[0];
+    v[1] = p2[1] - p1[1];
+    v[2] = p2[2] - p1[2];
+}
+__device__ __forceinline__ void bond_vector(const Pos<float>& c1, const Pos<float>& c2, const Pos<float>& c3,
+                                            const Pos<float>& c4, float s1, float s2, float v[3]) {
+    float d31[3], d43[3], d21[3];
+    pdiff(c3, c1, d31);
+    pdiff(c4, c3, d43);
+    pdiff(c2, c1, d21);
+#pragma unroll
+    for (int k = 0; k < 3; ++k) v[k] = fmaf(s2, d43[k], fmaf(-s1, d21[k], d31[k]));
 }
 
 __device__ __forceinline__ bool replica_selected(const CGState& S, int want) {
     return want < 0 ? (S.active != 0) : (S.phase == want);
-}
-
-// Whole-grid ticket: the last block to arrive clears the exvol fallback list
-// (used by the excluded-volume kernels of this evaluation).
-template <typename Real>
-__device__ __forceinline__ void grid_done(const DevNet<Real>& n) {
-    __syncthreads();
-    if (threadIdx.x == 0) {
-        __threadfence();
-        const int t = atomicAdd(n.gticket, 1);
-        if (t == (int)gridDim.x - 1) {
-            *n.ev_fb_count = 0;
-            *n.gticket = 0;
-            __threadfence();
-        }
-    }
 }
 
 // ---------------------------------------------------------------------------
@@ -57,13 +74,25 @@ __device__ __forceinline__ void grid_done(const DevNet<Real>& n) {
 template <typename Real>
 __device__ void finalize_energy(const DevNet<Real>& n, int r, int trial, double* sh) {
     const RepTiles rt = n.rt[r];
+    // every thread issues its loads back to back, then sums in a fixed order
+    double acc[MECH_NUM_FF] = {0, 0, 0, 0, 0, 0};
+#pragma unroll 8
+    for (int i = rt.fil_begin + threadIdx.x; i < rt.fil_end; i += blockDim.x) {
+        const double2 v = __ldcg(reinterpret_cast<const double2*>(n.part_fil + 4 * (size_t)i));
+        acc[MECH_FF_STRETCHING] += v.x;
+        acc[MECH_FF_BENDING] += v.y;
+    }
+    const int ffk[K_NUM_SPARSE] = {MECH_FF_LINKER, MECH_FF_MOTOR, MECH_FF_EXVOL, MECH_FF_BOUNDARY};
+#pragma unroll
+    for (int k = 0; k < K_NUM_SPARSE; ++k) {
+#pragma unroll 8
+        for (int i = rt.sp_begin[k] + threadIdx.x; i < rt.sp_end[k]; i += blockDim.x) acc[ffk[k]] += __ldcg(n.part_sp + i);
+    }
     double e[MECH_NUM_FF];
-    e[MECH_FF_STRETCHING] = sum_slots(n.part_fil, 4, 0, rt.fil_begin, rt.fil_end, sh);
-    e[MECH_FF_BENDING] = sum_slots(n.part_fil, 4, 1, rt.fil_begin, rt.fil_end, sh);
-    e[MECH_FF_LINKER] = sum_slots(n.part_sp, 1, 0, rt.sp_begin[K_LINKER], rt.sp_end[K_LINKER], sh);
-    e[MECH_FF_MOTOR] = sum_slots(n.part_sp, 1, 0, rt.sp_begin[K_MOTOR], rt.sp_end[K_MOTOR], sh);
-    e[MECH_FF_EXVOL] = sum_slots(n.part_sp, 1, 0, rt.sp_begin[K_EXVOL], rt.sp_end[K_EXVOL], sh);
-    e[MECH_FF_BOUNDARY] = sum_slots(n.part_sp, 1, 0, rt.sp_begin[K_BOUNDARY], rt.sp_end[K_BOUNDARY], sh);
+#pragma unroll
+    for (int k = 0; k < MECH_NUM_FF; ++k) e[k] = warp_sum(acc[k]);
+    const int ops[MECH_NUM_FF] = {0, 0, 0, 0, 0, 0};
+    block_combine<MECH_NUM_FF>(e, ops, sh);
     if (threadIdx.x != 0) return;
     // Pairs whose analytic energy was not usable were evaluated numerically;
     // add them in pair order.  A failed pair makes the force field report -1
@@ -110,9 +139,19 @@ __device__ void finalize_energy(const DevNet<Real>& n, int r, int trial, double*
 template <typename Real>
 __device__ void finalize_force(const DevNet<Real>& n, int r, double* sh) {
     const RepTiles rt = n.rt[r];
-    const double mx = max_slots(n.part_fil, 4, 0, rt.fil_begin, rt.fil_end, sh);
-    const double ff = sum_slots(n.part_fil, 4, 1, rt.fil_begin, rt.fil_end, sh);
-    const double ffp = sum_slots(n.part_fil, 4, 2, rt.fil_begin, rt.fil_end, sh);
+    double a_mx = 0.0, a_ff = 0.0, a_ffp = 0.0;
+#pragma unroll 8
+    for (int i = rt.fil_begin + threadIdx.x; i < rt.fil_end; i += blockDim.x) {
+        const double2 v = __ldcg(reinterpret_cast<const double2*>(n.part_fil + 4 * (size_t)i));
+        const double w = __ldcg(n.part_fil + 4 * (size_t)i + 2);
+        a_mx = fmax(a_mx, v.x);
+        a_ff += v.y;
+        a_ffp += w;
+    }
+    double red[3] = {warp_max(a_mx), warp_sum(a_ff), warp_sum(a_ffp)};
+    const int ops[3] = {1, 0, 0};
+    block_combine<3>(red, ops, sh);
+    const double mx = red[0], ff = red[1], ffp = red[2];
     if (threadIdx.x != 0) return;
     CGState& S = n.st[r];
     const int ph = S.phase;
@@ -154,8 +193,8 @@ __device__ void finalize_force(const DevNet<Real>& n, int r, double* sh) {
 // ---------------------------------------------------------------------------
 template <typename Real>
 __global__ void __launch_bounds__(kBlock) k_fil_energy(DevNet<Real> n, int want, int trial) {
-    __shared__ double xs[(kFilTile + 4) * 3];
-    __shared__ double sh[32];
+    __shared__ Pos<Real> xs[kFilTile + 4];
+    __shared__ double sh[32 * MECH_NUM_FF];
     __shared__ int s_go, s_xb, s_flag;
     __shared__ double s_lam;
     const Tile t = n.ftile[blockIdx.x];
@@ -169,50 +208,42 @@ __global__ void __launch_bounds__(kBlock) k_fil_energy(DevNet<Real> n, int want,
     __syncthreads();
     if (s_go) {
         const int T = t.end - t.begin;
-        const double* X = n.x[s_xb];
+        const Real* X = n.x[s_xb];
         const bool tr = trial != 0;
         for (int i = threadIdx.x; i < T + 4; i += blockDim.x) {
             const int b = t.begin - 2 + i;
-            double p[3] = {0.0, 0.0, 0.0};
-            if (b >= 0 && b < n.nb) bead_pos(X, n.d, b, tr, s_lam, p);
-            xs[3 * i] = p[0];
-            xs[3 * i + 1] = p[1];
-            xs[3 * i + 2] = p[2];
+            if (b >= 0 && b < n.nb) xs[i] = bead_at(X, n.d, b, tr, s_lam);
         }
         __syncthreads();
-        double es = 0.0, eb = 0.0;
+        Real es = 0, eb = 0;
         const int i = threadIdx.x;
         if (i < T) {
             const int j = t.begin + i;
             const int fl = n.bflag[j];
-            const double* pm = xs + 3 * (i + 1);
-            const double* p0 = xs + 3 * (i + 2);
-            const double* pp = xs + 3 * (i + 3);
-            if (tr) {   // materialize the trial coordinates of the owned bead
-                double* XT = n.x[s_xb ^ 1] + 3 * (size_t)j;
-                XT[0] = p0[0];
-                XT[1] = p0[1];
-                XT[2] = p0[2];
-            }
+            if (tr) store_pos(n.x[s_xb ^ 1], j, xs[i + 2]);   // materialize the owned trial position
             if (fl & 1) {
-                const Real r2[3] = {(Real)(pp[0] - p0[0]), (Real)(pp[1] - p0[1]), (Real)(pp[2] - p0[2])};
-                es = stretch_energy<Real>(r2[0], r2[1], r2[2], n.kstr[j], n.l0[j]);
+                Real ks, l0, kb, t0;
+                load_par(n.bpar, j, ks, l0, kb, t0);
+                Real r2[3];
+                pdiff(xs[i + 3], xs[i + 2], r2);
+                es = stretch_energy<Real>(r2[0], r2[1], r2[2], ks, l0);
                 if (fl & 2) {
-                    const Real r1[3] = {(Real)(p0[0] - pm[0]), (Real)(p0[1] - pm[1]), (Real)(p0[2] - pm[2])};
-                    eb = bend_energy<Real>(r1, r2, n.kbend[j], n.t0[j]);
+                    Real r1[3];
+                    pdiff(xs[i + 2], xs[i + 1], r1);
+                    eb = bend_energy<Real>(r1, r2, kb, t0);
                 }
             }
         }
-        es = block_sum(es, sh);
-        eb = block_sum(eb, sh);
+        double red[2] = {warp_sum_r(es), warp_sum_r(eb)};
+        const int ops[2] = {0, 0};
+        block_combine<2>(red, ops, sh);
         if (threadIdx.x == 0) {
-            n.part_fil[4 * (size_t)blockIdx.x + 0] = es;
-            n.part_fil[4 * (size_t)blockIdx.x + 1] = eb;
+            n.part_fil[4 * (size_t)blockIdx.x + 0] = red[0];
+            n.part_fil[4 * (size_t)blockIdx.x + 1] = red[1];
         }
         const RepTiles rt = n.rt[r];
         if (last_tile(n.ticket, r, rt.fil_end - rt.fil_begin, &s_flag)) finalize_energy(n, r, trial, sh);
     }
-    grid_done(n);
 }
 
 // ---------------------------------------------------------------------------
@@ -220,11 +251,11 @@ __global__ void __launch_bounds__(kBlock) k_fil_energy(DevNet<Real> n, int want,
 // ---------------------------------------------------------------------------
 template <typename Real>
 __global__ void __launch_bounds__(kBlock) k_fil_force(DevNet<Real> n, int want) {
-    __shared__ double xs[(kFilTile + 4) * 3];
+    __shared__ Pos<Real> xs[kFilTile + 4];
     __shared__ Real fs[(kFilTile + 2) * 3];    // stretch force on the second bead
     __shared__ Real f1[(kFilTile + 2) * 3];    // bending Fr1
     __shared__ Real f2[(kFilTile + 2) * 3];    // bending Fr2
-    __shared__ double sh[32];
+    __shared__ double sh[32 * 3];
     __shared__ int s_go, s_xb, s_fb, s_flag;
     const Tile t = n.ftile[blockIdx.x];
     const int r = t.replica;
@@ -237,14 +268,10 @@ __global__ void __launch_bounds__(kBlock) k_fil_force(DevNet<Real> n, int want) 
     __syncthreads();
     if (s_go) {
         const int T = t.end - t.begin;
-        const double* X = n.x[s_xb];
+        const Real* X = n.x[s_xb];
         for (int i = threadIdx.x; i < T + 4; i += blockDim.x) {
             const int b = t.begin - 2 + i;
-            double p[3] = {0.0, 0.0, 0.0};
-            if (b >= 0 && b < n.nb) bead_pos<Real>(X, nullptr, b, false, 0.0, p);
-            xs[3 * i] = p[0];
-            xs[3 * i + 1] = p[1];
-            xs[3 * i + 2] = p[2];
+            if (b >= 0 && b < n.nb) xs[i] = load_pos(X, b);
         }
         __syncthreads();
         // interaction slots s in [0, T + 2): bead j = begin - 1 + s, shared index s + 1
@@ -253,15 +280,16 @@ __global__ void __launch_bounds__(kBlock) k_fil_force(DevNet<Real> n, int want) 
             Real a[3] = {0, 0, 0}, b1[3] = {0, 0, 0}, b2[3] = {0, 0, 0};
             if (j >= 0 && j < n.nb) {
                 const int fl = n.bflag[j];
-                const double* pm = xs + 3 * s;
-                const double* p0 = xs + 3 * (s + 1);
-                const double* pp = xs + 3 * (s + 2);
                 if (fl & 1) {
-                    const Real r2[3] = {(Real)(pp[0] - p0[0]), (Real)(pp[1] - p0[1]), (Real)(pp[2] - p0[2])};
-                    stretch_force<Real>(r2[0], r2[1], r2[2], n.kstr[j], n.l0[j], a);
+                    Real ks, l0, kb, t0;
+                    load_par(n.bpar, j, ks, l0, kb, t0);
+                    Real r2[3];
+                    pdiff(xs[s + 2], xs[s + 1], r2);
+                    stretch_force<Real>(r2[0], r2[1], r2[2], ks, l0, a);
                     if (fl & 2) {
-                        const Real r1[3] = {(Real)(p0[0] - pm[0]), (Real)(p0[1] - pm[1]), (Real)(p0[2] - pm[2])};
-                        bend_force<Real>(r1, r2, n.kbend[j], n.t0[j], b1, b2);
+                        Real r1[3];
+                        pdiff(xs[s + 1], xs[s], r1);
+                        bend_force<Real>(r1, r2, kb, t0, b1, b2);
                     }
                 }
             }
@@ -273,7 +301,7 @@ __global__ void __launch_bounds__(kBlock) k_fil_force(DevNet<Real> n, int want) 
             }
         }
         __syncthreads();
-        double mx = 0.0, ff = 0.0, ffp = 0.0;
+        Real mx = 0, ff = 0, ffp = 0;
         const int i = threadIdx.x;
         if (i < T) {
             const int b = t.begin + i;
@@ -301,22 +329,21 @@ __global__ void __launch_bounds__(kBlock) k_fil_force(DevNet<Real> n, int want) 
             Fo[0] = F[0];
             Fo[1] = F[1];
             Fo[2] = F[2];
-            mx = fmax(fmax(fabs((double)F[0]), fabs((double)F[1])), fabs((double)F[2]));
-            ff = bead_dot<Real>(F[0], F[1], F[2], F[0], F[1], F[2]);
-            ffp = bead_dot<Real>(F[0], F[1], F[2], Fp[0], Fp[1], Fp[2]);
+            mx = fmax(fmax(fabs(F[0]), fabs(F[1])), fabs(F[2]));
+            ff = bead_dot(F[0], F[1], F[2], F[0], F[1], F[2]);
+            ffp = bead_dot(F[0], F[1], F[2], Fp[0], Fp[1], Fp[2]);
         }
-        mx = block_max(mx, sh);
-        ff = block_sum(ff, sh);
-        ffp = block_sum(ffp, sh);
+        double red[3] = {warp_max_r(mx), warp_sum_r(ff), warp_sum_r(ffp)};
+        const int ops[3] = {1, 0, 0};
+        block_combine<3>(red, ops, sh);
         if (threadIdx.x == 0) {
-            n.part_fil[4 * (size_t)blockIdx.x + 0] = mx;
-            n.part_fil[4 * (size_t)blockIdx.x + 1] = ff;
-            n.part_fil[4 * (size_t)blockIdx.x + 2] = ffp;
+            n.part_fil[4 * (size_t)blockIdx.x + 0] = red[0];
+            n.part_fil[4 * (size_t)blockIdx.x + 1] = red[1];
+            n.part_fil[4 * (size_t)blockIdx.x + 2] = red[2];
         }
         const RepTiles rt = n.rt[r];
         if (last_tile(n.ticket, r, rt.fil_end - rt.fil_begin, &s_flag)) finalize_force(n, r, sh);
     }
-    grid_done(n);
 }
 
 // ---------------------------------------------------------------------------
@@ -340,22 +367,21 @@ __global__ void __launch_bounds__(kBlock) k_bond_bnd(DevNet<Real> n, int want, i
     }
     __syncthreads();
     if (!s_go) return;
-    const double* X = n.x[s_xb];
+    const Real* X = n.x[s_xb];
     const bool tr = trial != 0;
     const int i = t.begin + threadIdx.x;
-    double e = 0.0;
+    Real e = 0;
     if (i < t.end) {
         if (kind == K_BOUNDARY) {
             const int b = n.bb_bead[i];
             const double* pl = n.planes + 4 * n.bb_plane[i];
-            double p[3];
-            bead_pos(X, n.d, b, tr, s_lam, p);
-            const double rr = plane_dist(pl, p);
+            const Pos<Real> p = bead_at(X, n.d, b, tr, s_lam);
+            const Real rr = plane_dist_p(pl, p);
             const Real K = n.bb_k[i], sl = n.bb_slen[i];
-            const Real R = (Real)(-rr / (double)sl);
+            const Real R = -rr / sl;
             const Real ex = exp(R);
             if (!force) {
-                e = (double)(K * ex);
+                e = K * ex;
             } else {
                 const Real f0 = K * ex / sl;
                 Real* c = n.contrib + 3 * (size_t)(n.slot_base[K_BOUNDARY] + i);
@@ -370,18 +396,15 @@ __global__ void __launch_bounds__(kBlock) k_bond_bnd(DevNet<Real> n, int want, i
             const Real l0 = lk ? n.lk_l0[i] : n.mt_l0[i];
             const Real s1 = lk ? n.lk_s1[i] : n.mt_s1[i];
             const Real s2 = lk ? n.lk_s2[i] : n.mt_s2[i];
-            double c1[3], c2[3], c3[3], c4[3], v1[3], v2[3];
-            bead_pos(X, n.d, bs.x, tr, s_lam, c1);
-            bead_pos(X, n.d, bs.y, tr, s_lam, c2);
-            bead_pos(X, n.d, bs.z, tr, s_lam, c3);
-            bead_pos(X, n.d, bs.w, tr, s_lam, c4);
-            lerp3(c1, c2, (double)s1, v1);
-            lerp3(c3, c4, (double)s2, v2);
-            const Real lx = (Real)(v2[0] - v1[0]), ly = (Real)(v2[1] - v1[1]), lz = (Real)(v2[2] - v1[2]);
+            const Pos<Real> c1 = bead_at(X, n.d, bs.x, tr, s_lam), c2 = bead_at(X, n.d, bs.y, tr, s_lam);
+            const Pos<Real> c3 = bead_at(X, n.d, bs.z, tr, s_lam), c4 = bead_at(X, n.d, bs.w, tr, s_lam);
+            Real v[3];
+            bond_vector(c1, c2, c3, c4, s1, s2, v);
+            const Real lx = v[0], ly = v[1], lz = v[2];
             const Real dist = sqrt(lx * lx + ly * ly + lz * lz);
             if (!force) {
                 const Real dd = dist - l0;
-                e = (double)((Real)0.5 * k * dd * dd);
+                e = (Real)0.5 * k * dd * dd;
             } else {
                 const Real invL = (Real)1 / dist;
                 const Real f0 = k * (dist - l0) * invL;
@@ -399,8 +422,8 @@ __global__ void __launch_bounds__(kBlock) k_bond_bnd(DevNet<Real> n, int want, i
         }
     }
     if (!force) {
-        e = block_sum(e, sh);
-        if (threadIdx.x == 0) n.part_sp[ti] = e;
+        const double se = block_sum_r(e, sh);
+        if (threadIdx.x == 0) n.part_sp[ti] = se;
     }
 }
 
@@ -425,7 +448,7 @@ __global__ void __launch_bounds__(kBlock) k_direction(DevNet<Real> n) {
     __syncthreads();
     if (!s_go) return;
     const int b = t.begin + threadIdx.x;
-    double dF = 0.0;
+    Real dF = 0;
     if (b < t.end) {
         const Real* F = n.f[s_fb] + 3 * (size_t)b;
         Real* D = n.d + 3 * (size_t)b;
@@ -434,17 +457,11 @@ __global__ void __launch_bounds__(kBlock) k_direction(DevNet<Real> n) {
         D[0] = d0;
         D[1] = d1;
         D[2] = d2;
-        dF = bead_dot<Real>(d0, d1, d2, F[0], F[1], F[2]);
-        if (s_bk) {
-            const double* X = n.x[s_xb] + 3 * (size_t)b;
-            double* B = n.xbest + 3 * (size_t)b;
-            B[0] = X[0];
-            B[1] = X[1];
-            B[2] = X[2];
-        }
+        dF = bead_dot(d0, d1, d2, F[0], F[1], F[2]);
+        if (s_bk) store_pos(n.xbest, b, load_pos(n.x[s_xb], b));
     }
-    dF = block_sum(dF, sh);
-    if (threadIdx.x == 0) n.part_fil[4 * (size_t)blockIdx.x + 3] = dF;
+    const double sdF = block_sum_r(dF, sh);
+    if (threadIdx.x == 0) n.part_fil[4 * (size_t)blockIdx.x + 3] = sdF;
     const RepTiles rt = n.rt[r];
     if (last_tile(n.ticket, r, rt.fil_end - rt.fil_begin, &s_flag)) {
         const double slope = sum_slots(n.part_fil, 4, 3, rt.fil_begin, rt.fil_end, sh);
@@ -529,13 +546,13 @@ __global__ void __launch_bounds__(kBlock) k_recover_maxabs(DevNet<Real> n) {
     __syncthreads();
     if (!s_go) return;
     const int b = t.begin + threadIdx.x;
-    double m = 0.0;
+    Real m = 0;
     if (b < t.end) {
         const Real* D = n.d + 3 * (size_t)b;
-        m = fmax(fmax(fabs((double)D[0]), fabs((double)D[1])), fabs((double)D[2]));
+        m = fmax(fmax(fabs(D[0]), fabs(D[1])), fabs(D[2]));
     }
-    m = block_max(m, sh);
-    if (threadIdx.x == 0) n.part_fil[4 * (size_t)blockIdx.x + 3] = m;
+    const double sm = block_max_r(m, sh);
+    if (threadIdx.x == 0) n.part_fil[4 * (size_t)blockIdx.x + 3] = sm;
     const RepTiles rt = n.rt[r];
     if (last_tile(n.ticket, r, rt.fil_end - rt.fil_begin, &s_flag)) {
         const double mx = max_slots(n.part_fil, 4, 3, rt.fil_begin, rt.fil_end, sh);
@@ -568,12 +585,9 @@ __global__ void __launch_bounds__(kBlock) k_recover_move(DevNet<Real> n) {
     __syncthreads();
     if (!s_go) return;
     const int b = t.begin + threadIdx.x;
-    if (b < t.end) {
-        double* X = n.x[s_xb] + 3 * (size_t)b;
-        const Real* D = n.d + 3 * (size_t)b;
-        X[0] += s_step * (double)D[0];
-        X[1] += s_step * (double)D[1];
-        X[2] += s_step * (double)D[2];
+    if (b < t.end) {   // coord += step * d (MController.h:321-323)
+        Real* X = n.x[s_xb];
+        store_pos(X, b, moved(load_pos(X, b), n.d, b, s_step));
     }
     const RepTiles rt = n.rt[r];
     if (last_tile(n.ticket, r, rt.fil_end - rt.fil_begin, &s_flag)) {
@@ -587,13 +601,7 @@ __global__ void __launch_bounds__(kBlock) k_backup_restore(DevNet<Real> n) {
     const CGState& S = n.st[t.replica];
     if (!S.restore) return;
     const int b = t.begin + threadIdx.x;
-    if (b < t.end) {
-        double* X = n.x[S.xbuf] + 3 * (size_t)b;
-        const double* B = n.xbest + 3 * (size_t)b;
-        X[0] = B[0];
-        X[1] = B[1];
-        X[2] = B[2];
-    }
+    if (b < t.end) store_pos(n.x[S.xbuf], b, load_pos(n.xbest, b));
 }
 
 // ---------------------------------------------------------------------------

@@ -13,6 +13,7 @@
 #include <string>
 #include <vector>
 
+#include "mech_device.cuh"
 #include "mech_internal.cuh"
 #include "mech_nl.cuh"
 
@@ -63,7 +64,7 @@ struct MechContext {
     std::vector<ReplicaHost> reps;
     bool have_net = false, have_lists = false;
     // beads
-    DeviceBuffer x[2], f[2], d, xbest, xinit, bflag, kstr, l0, kbend, t0;
+    DeviceBuffer x[2], f[2], d, xbest, xinit, bflag, bpar;
     // cylinders
     DeviceBuffer cyl_b1, cyl_id, cyl_fil, cyl_pos, cyl_rep, cyl_minus, cyl_kex, cyl_type, cyl_l0;
     // linkers / motors
@@ -71,7 +72,7 @@ struct MechContext {
     // boundary
     DeviceBuffer planes, plane_k, plane_slen, bb_k, bb_slen;
     // excluded volume
-    DeviceBuffer ev_bead, ev_k, ev_la, ev_lb;
+    DeviceBuffer ev_bead, ev_k, ev_la, ev_lb, ev_list, ev_list_count, ev_energy;
     // tiles, partials, state
     DeviceBuffer ftile, stile, stile_kind, rt, part_fil, part_sp, st, ticket, gticket, err;
     DeviceBuffer contrib, ev_fb_count, ev_fb_list, ev_fb_energy, fb_moments, fb_tickets;
@@ -112,17 +113,17 @@ DevNet<Real> make_devnet(MechContext* c) {
     DevNet<Real> n{};
     n.nb = c->nb;
     n.R = c->R;
-    n.x[0] = c->x[0].as<double>();
-    n.x[1] = c->x[1].as<double>();
+    n.x[0] = c->x[0].as<Real>();
+    n.x[1] = c->x[1].as<Real>();
     n.f[0] = c->f[0].as<Real>();
     n.f[1] = c->f[1].as<Real>();
     n.d = c->d.as<Real>();
-    n.xbest = c->xbest.as<double>();
+    n.xbest = c->xbest.as<Real>();
+    n.ev_list = c->ev_list.as<int>();
+    n.ev_list_count = c->ev_list_count.as<int>();
+    n.ev_energy = c->ev_energy.as<double>();
     n.bflag = c->bflag.as<uint8_t>();
-    n.kstr = c->kstr.as<Real>();
-    n.l0 = c->l0.as<Real>();
-    n.kbend = c->kbend.as<Real>();
-    n.t0 = c->t0.as<Real>();
+    n.bpar = c->bpar.as<Real>();
     n.n_ftiles = c->n_ftiles;
     n.ftile = c->ftile.as<Tile>();
     n.n_lk = c->nlk;
@@ -213,13 +214,30 @@ __global__ void k_gather_i32(const int* src, const long long* idx, int n, long l
 }
 
 // caller order <-> internal order of one replica's coordinates / forces
-__global__ void k_scatter_coords(const double* in, const int* perm, int nb, int base, double* out) {
+__device__ __forceinline__ void put_pos(double* X, int j, const double v[3]) {
+    Pos<double> p;
+    p.x[0] = v[0]; p.x[1] = v[1]; p.x[2] = v[2];
+    store_pos(X, j, p);
+}
+__device__ __forceinline__ void put_pos(float* X, int j, const double v[3]) { store_pos(X, j, split(v)); }
+
+template <typename Real>
+__global__ void k_scatter_coords(const double* in, const int* perm, int nb, int base, Real* out) {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= nb) return;
-    const int j = base + perm[i];
-    out[3 * (size_t)j] = in[3 * (size_t)i];
-    out[3 * (size_t)j + 1] = in[3 * (size_t)i + 1];
-    out[3 * (size_t)j + 2] = in[3 * (size_t)i + 2];
+    const double v[3] = {in[3 * (size_t)i], in[3 * (size_t)i + 1], in[3 * (size_t)i + 2]};
+    put_pos(out, base + perm[i], v);
+}
+
+template <typename Real>
+__global__ void k_gather_pos(const Real* X, const int* perm, int nb, int base, double* out) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= nb) return;
+    double v[3];
+    to_double(load_pos(X, base + perm[i]), v);
+    out[3 * (size_t)i] = v[0];
+    out[3 * (size_t)i + 1] = v[1];
+    out[3 * (size_t)i + 2] = v[2];
 }
 
 template <typename Real>
@@ -400,7 +418,21 @@ static int set_networks(MechContext* c, int R, const MechNetwork* nets) {
     cudaStream_t s = c->stream;
     const size_t rs = real_size(c);
     int rc;
-    if ((rc = upload(c->x[0], x, s))) return rc;
+    // positions in the engine's format (24 bytes per bead either way)
+    {
+        DeviceBuffer xd, ident;
+        if ((rc = upload(xd, x, s))) return rc;
+        std::vector<int> id(nb);
+        for (int i = 0; i < nb; ++i) id[i] = i;
+        if ((rc = upload(ident, id, s))) return rc;
+        CU(c->x[0].ensure(sizeof(double) * x.size()));
+        if (c->precision == MECH_PREC_FP64)
+            k_scatter_coords<double><<<(nb + 255) / 256, 256, 0, s>>>(xd.as<double>(), ident.as<int>(), nb, 0, c->x[0].as<double>());
+        else
+            k_scatter_coords<float><<<(nb + 255) / 256, 256, 0, s>>>(xd.as<double>(), ident.as<int>(), nb, 0, c->x[0].as<float>());
+        CU(cudaGetLastError());
+        CU(cudaStreamSynchronize(s));
+    }
     CU(c->x[1].ensure(sizeof(double) * x.size()));
     CU(cudaMemcpyAsync(c->x[1].p, c->x[0].p, sizeof(double) * x.size(), cudaMemcpyDeviceToDevice, s));
     CU(c->xbest.ensure(sizeof(double) * x.size()));
@@ -413,9 +445,16 @@ static int set_networks(MechContext* c, int R, const MechNetwork* nets) {
     CU(cudaMemsetAsync(c->f[1].p, 0, rs * x.size(), s));
     CU(cudaMemsetAsync(c->d.p, 0, rs * x.size(), s));
     if ((rc = upload(c->bflag, flags, s))) return rc;
-    if ((rc = upload_real(c, c->kstr, kstr)) || (rc = upload_real(c, c->l0, l0b)) || (rc = upload_real(c, c->kbend, kbend)) ||
-        (rc = upload_real(c, c->t0, t0)))
-        return rc;
+    {
+        std::vector<double> par(4 * (size_t)nb);
+        for (int i = 0; i < nb; ++i) {
+            par[4 * (size_t)i] = kstr[i];
+            par[4 * (size_t)i + 1] = l0b[i];
+            par[4 * (size_t)i + 2] = kbend[i];
+            par[4 * (size_t)i + 3] = t0[i];
+        }
+        if ((rc = upload_real(c, c->bpar, par))) return rc;
+    }
     if ((rc = upload(c->cyl_b1, cyl_b1, s)) || (rc = upload(c->cyl_id, cyl_id, s)) || (rc = upload(c->cyl_fil, cyl_fil, s)) ||
         (rc = upload(c->cyl_pos, cyl_pos, s)) || (rc = upload(c->cyl_rep, cyl_rep, s)) || (rc = upload(c->cyl_type, cyl_type, s)) ||
         (rc = upload(c->cyl_kex, cyl_kex, s)) || (rc = upload(c->cyl_l0, cyl_l0, s)) || (rc = upload(c->cyl_minus, minus, s)))
@@ -541,14 +580,15 @@ static int rebuild(MechContext* c, double cell_req, MechListInfo* info) {
     for (int r = 0; r < R; ++r) {
         if (c->h_st[r].xbuf) {
             const ReplicaHost& h = c->reps[r];
-            CU(cudaMemcpyAsync(c->x[0].as<double>() + 3 * (size_t)h.bead_begin, c->x[1].as<double>() + 3 * (size_t)h.bead_begin,
-                               sizeof(double) * 3 * h.nb, cudaMemcpyDeviceToDevice, s));
+            CU(cudaMemcpyAsync(c->x[0].as<char>() + 24 * (size_t)h.bead_begin, c->x[1].as<char>() + 24 * (size_t)h.bead_begin,
+                               24 * (size_t)h.nb, cudaMemcpyDeviceToDevice, s));
             c->h_st[r].xbuf = 0;
             moved = true;
         }
     }
     if (moved) CU(cudaMemcpyAsync(c->st.p, c->h_st, sizeof(CGState) * R, cudaMemcpyHostToDevice, s));
-    in.x = c->x[0].as<double>();
+    in.x = c->x[0].p;
+    in.mixed = c->precision == MECH_PREC_MIXED;
     long long P = 0;
     CU(build_pairs(in, c->pb, c->rep_margin.as<float>(), &P, s));
     c->nev = P;
@@ -574,6 +614,10 @@ static int rebuild(MechContext* c, double cell_req, MechListInfo* info) {
     CU(c->ev_k.ensure(rs * std::max<long long>(P, 1)));
     CU(c->ev_la.ensure(rs * std::max<long long>(P, 1)));
     CU(c->ev_lb.ensure(rs * std::max<long long>(P, 1)));
+    CU(c->ev_list.ensure(sizeof(int) * 2 * std::max<long long>(P, 1)));
+    CU(c->ev_energy.ensure(sizeof(double) * std::max<long long>(P, 1)));
+    CU(c->ev_list_count.ensure(sizeof(int) * 4));
+    CU(cudaMemsetAsync(c->ev_list_count.p, 0, sizeof(int) * 4, s));
     if (P > 0) {
         const unsigned nbk = (unsigned)((P + 255) / 256);
         if (c->precision == MECH_PREC_FP64)
@@ -821,7 +865,8 @@ static int minimize_impl(MechContext* c, const MechCGParams* p, MechResult* res)
         launches += per_graph;
         if ((rc = pull_states(c))) { cudaGraphExecDestroy(exec); return rc; }
         if (*c->h_err) {
-            status = set_err(MECH_ERR_NONFINITE, "excluded-volume numeric fallback failed");
+            status = (*c->h_err & 1u) ? set_err(MECH_ERR_NONFINITE, "excluded-volume numeric fallback failed")
+                                      : set_err(MECH_ERR_CAPACITY, "excluded-volume work list overflow");
             break;
         }
         bool all_done = true, recover = false;
@@ -954,9 +999,13 @@ int32_t mech_set_coords(MechContext* ctx, int32_t r, const double* coord) {
     if ((rc = pull_states(ctx))) return rc;
     const ReplicaHost& h = ctx->reps[r];
     CU(cudaMemcpyAsync(ctx->stage.p, coord, sizeof(double) * 3 * h.nb, cudaMemcpyHostToDevice, ctx->stream));
-    double* X = ctx->x[ctx->h_st[r].xbuf].as<double>();
-    k_scatter_coords<<<(h.nb + 255) / 256, 256, 0, ctx->stream>>>(ctx->stage.as<double>(), perm_of(ctx, r), h.nb,
-                                                                  h.bead_begin, X);
+    void* X = ctx->x[ctx->h_st[r].xbuf].p;
+    if (ctx->precision == MECH_PREC_FP64)
+        k_scatter_coords<double><<<(h.nb + 255) / 256, 256, 0, ctx->stream>>>(ctx->stage.as<double>(), perm_of(ctx, r),
+                                                                              h.nb, h.bead_begin, (double*)X);
+    else
+        k_scatter_coords<float><<<(h.nb + 255) / 256, 256, 0, ctx->stream>>>(ctx->stage.as<double>(), perm_of(ctx, r),
+                                                                             h.nb, h.bead_begin, (float*)X);
     CU(cudaGetLastError());
     CU(cudaStreamSynchronize(ctx->stream));
     return MECH_OK;
@@ -969,9 +1018,13 @@ int32_t mech_get_coords(MechContext* ctx, int32_t r, double* coord) {
     CU(cudaSetDevice(ctx->device));
     if ((rc = pull_states(ctx))) return rc;
     const ReplicaHost& h = ctx->reps[r];
-    const double* X = ctx->x[ctx->h_st[r].xbuf].as<double>();
-    k_gather_coords<double><<<(h.nb + 255) / 256, 256, 0, ctx->stream>>>(X, perm_of(ctx, r), h.nb, h.bead_begin,
-                                                                        ctx->stage.as<double>());
+    const void* X = ctx->x[ctx->h_st[r].xbuf].p;
+    if (ctx->precision == MECH_PREC_FP64)
+        k_gather_pos<double><<<(h.nb + 255) / 256, 256, 0, ctx->stream>>>((const double*)X, perm_of(ctx, r), h.nb,
+                                                                          h.bead_begin, ctx->stage.as<double>());
+    else
+        k_gather_pos<float><<<(h.nb + 255) / 256, 256, 0, ctx->stream>>>((const float*)X, perm_of(ctx, r), h.nb,
+                                                                         h.bead_begin, ctx->stage.as<double>());
     CU(cudaMemcpyAsync(coord, ctx->stage.p, sizeof(double) * 3 * h.nb, cudaMemcpyDeviceToHost, ctx->stream));
     CU(cudaStreamSynchronize(ctx->stream));
     return MECH_OK;
@@ -1070,8 +1123,7 @@ int32_t mech_reset_coords(MechContext* ctx) {
     if ((rc = pull_states(ctx))) return rc;
     for (int r = 0; r < ctx->R; ++r) ctx->h_st[r].xbuf = 0;
     if ((rc = push_states(ctx))) return rc;
-    CU(cudaMemcpyAsync(ctx->x[0].p, ctx->xinit.p, sizeof(double) * 3 * (size_t)ctx->nb, cudaMemcpyDeviceToDevice,
-                       ctx->stream));
+    CU(cudaMemcpyAsync(ctx->x[0].p, ctx->xinit.p, 24 * (size_t)ctx->nb, cudaMemcpyDeviceToDevice, ctx->stream));
     CU(cudaStreamSynchronize(ctx->stream));
     return MECH_OK;
 }

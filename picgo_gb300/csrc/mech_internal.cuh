@@ -104,15 +104,12 @@ template <typename Real>
 struct DevNet {
     int nb;                 // beads, all replicas
     int R;
-    double* x[2];
+    Real* x[2];             // positions: double[3] per bead (FP64) or float hi[3], lo[3] per bead (mixed)
     Real* f[2];
     Real* d;
-    double* xbest;
+    Real* xbest;
     const uint8_t* bflag;
-    const Real* kstr;       // per bead slot
-    const Real* l0;
-    const Real* kbend;
-    const Real* t0;
+    const Real* bpar;       // per bead slot: k_str, l0 of cylinder (i, i+1); k_bend, theta0 of the triple on i
     // filament tiles
     int n_ftiles;
     const Tile* ftile;
@@ -141,6 +138,8 @@ struct DevNet {
     int* ev_fb_count; int* ev_fb_list; double* ev_fb_energy;
     double* fb_moments;     // [cap * kFbChunks * 6]
     int* fb_tickets;        // [cap]
+    // mixed precision: pairs evaluated in FP64 (compacted list) and per-pair energies
+    int* ev_list; int* ev_list_count; double* ev_energy;
     // partial sums
     double* part_fil;       // [n_ftiles * 4]
     double* part_sp;        // [n_stiles]

@@ -130,8 +130,14 @@ __global__ void k_nl_mid(NLInput in, double* mid, float4* midf, int* cell_of, in
     const int c = blockIdx.x * blockDim.x + threadIdx.x;
     if (c >= in.ncyl) return;
     const int b = in.cyl_b1[c];
-    const double* x1 = in.x + 3 * (size_t)b;
-    const double* x2 = x1 + 3;
+    double x1[3], x2[3];
+    if (in.mixed) {
+        to_double(load_pos(static_cast<const float*>(in.x), b), x1);
+        to_double(load_pos(static_cast<const float*>(in.x), b + 1), x2);
+    } else {
+        to_double(load_pos(static_cast<const double*>(in.x), b), x1);
+        to_double(load_pos(static_cast<const double*>(in.x), b + 1), x2);
+    }
     // 0.5 * (b1 + b2) (Structure/Cylinder.cpp:45-46); equal to the boundary
     // list's b1 * 0.5 + 0.5 * b2 bit for bit
     const double m0 = 0.5 * (x1[0] + x2[0]), m1 = 0.5 * (x1[1] + x2[1]), m2 = 0.5 * (x1[2] + x2[2]);

@@ -12,7 +12,8 @@ struct NLInput {
     const int* cyl_fil;
     const int* cyl_pos;
     const int* cyl_rep;
-    const double* x;           // current coordinates
+    const void* x;             // current coordinates (engine format)
+    int mixed;                 // 1: float hi/lo pairs, 0: doubles
     const double* rep_cell;    // [R] cell edge
     const int4* rep_dims;      // [R] gx, gy, gz, first cell index
     const double* rep_rmax2;   // [R] rMax^2 rounded to float, held as double

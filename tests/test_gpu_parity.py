@@ -9,8 +9,13 @@ The excluded-volume formula is compared with the oracle's series arctangent,
 the arctangent the FP64 kernel uses (the C library's differs by an ulp, which
 nearly coplanar pairs amplify; see test_oracle_atan_sensitivity).
 Mixed precision: total energy within 1e-6 relative of the FP64 oracle, forces
-within 2e-4 * S + 1e-3 pN.
+within 2e-4 * (S + X) + 5e-3 pN, where X adds, for each excluded-volume pair
+touching the bead, the largest force component of that pair (the pair's four
+bead forces come from shared terms, so their error scales with the pair's
+largest force), and 5 mpN is the single-precision resolution of a 108 nm bond
+length times the 100 pN/nm stretching constant, with margin.
 """
+import ctypes as C
 import numpy as np
 import pytest
 
@@ -20,6 +25,27 @@ from picgo_gb300 import Engine, cg_params, jitter, make_network
 pytestmark = pytest.mark.gpu
 
 FF_FIELDS = ("n_stretch", "n_bend", "n_linker", "n_motor", "n_exvol", "n_planes")
+
+
+def exvol_pair_scale(vec, coord):
+    """Per component: sum over excluded-volume pairs touching the bead of the pair's largest force component."""
+    L = oracle.lib()
+    L.orc_exvol_pair_forces.restype = C.c_int
+    L.orc_exvol_pair_forces.argtypes = [C.POINTER(C.c_double)] * 4 + [C.c_double] * 3 + [C.POINTER(C.c_double)]
+    x = np.ascontiguousarray(coord, dtype=np.float64).reshape(-1)
+    bs = vec.arrays["ev_bs"].reshape(-1, 4)
+    k = vec.arrays["ev_k"]
+    ln = vec.arrays["ev_len"].reshape(-1, 2)
+    out = np.zeros(12)
+    T = np.zeros_like(x)
+    dp = C.POINTER(C.c_double)
+    for i in range(bs.shape[0]):
+        ptrs = [x[b:b + 3].ctypes.data_as(dp) for b in bs[i]]
+        L.orc_exvol_pair_forces(*ptrs, float(k[i]), float(ln[i, 0]), float(ln[i, 1]), out.ctypes.data_as(dp))
+        m = np.abs(out).max()
+        for b in bs[i]:
+            T[b:b + 3] += m
+    return T.reshape(-1, 3)
 
 
 def check_energies(per_gpu, per_orc):
@@ -128,9 +154,26 @@ def test_mixed_energy_error_against_fp64():
     fo = oracle.forces(vec, net.coord)
     with Engine("mixed") as eng:
         eng.set_network(net)
+        assert np.array_equal(eng.pairs(), vec.pairs)
+        assert np.abs(eng.coords() - net.coord).max() <= 1e-11 * np.abs(net.coord).max()
         per, tot, _ = eng.energies()
         f = eng.forces()
     assert abs(tot - o_tot) <= 1e-6 * abs(o_tot), (tot, o_tot)
-    scale = oracle.force_scale(vec, net.coord)
+    S = oracle.force_scale(vec, net.coord)
+    X = exvol_pair_scale(vec, net.coord)
     err = np.abs(f - fo)
-    assert np.all(err <= 2e-4 * scale + 1e-3), np.max(err / (2e-4 * scale + 1e-3))
+    ratio = err / (2e-4 * (S + X) + 5e-3)
+    i = np.unravel_index(np.argmax(ratio), ratio.shape)
+    assert ratio.max() <= 1.0, dict(worst=i, ratio=ratio[i], err=err[i], S=S[i], X=X[i], f=f[i], fo=fo[i])
+
+
+def test_mixed_minimizer_reaches_tolerance():
+    net = _net("small_motors")
+    with Engine("mixed") as eng:
+        eng.set_network(net)
+        r = eng.minimize(cg_params(energy_rel_tol=0.0, force_call_limit=200000))[0]
+        f = eng.last_forces()
+    assert r["status"] == 0
+    assert r["grad_inf_norm"] < 1.0
+    assert np.abs(f).max() < 1.0
+    assert r["energies_after"][6] < r["energies_before"][6]
