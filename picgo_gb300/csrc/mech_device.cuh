@@ -250,6 +250,52 @@ __device__ __forceinline__ Pos<Real> bead_at(const Real* X, const Real* D, int b
     const Pos<Real> p = load_pos(X, b);
     return trial ? moved(p, D, b, lam) : p;
 }
+// single-precision step already rounded by the caller (same result as the double-lambda form)
+__device__ __forceinline__ Pos<float> moved_f(const Pos<float>& p, const float* D, int b, float lf) {
+    Pos<float> o;
+    const float* d = D + 3 * (size_t)b;
+#pragma unroll
+    for (int k = 0; k < 3; ++k) {
+        float s, e, lo;
+        two_sum(p.h[k], __fmul_rn(lf, d[k]), s, e);
+        lo = __fadd_rn(p.l[k], e);
+        fast_two_sum(s, lo, o.h[k], o.l[k]);
+    }
+    return o;
+}
+
+// compensated single-precision accumulator
+struct FF {
+    float h = 0.f, l = 0.f;
+    __device__ __forceinline__ void add(float v) {
+        float s, e;
+        two_sum(h, v, s, e);
+        const float lo = __fadd_rn(l, e);
+        fast_two_sum(s, lo, h, l);
+    }
+};
+// warp sum of (h, l) pairs; the double value is formed in lane 0 only
+__device__ __forceinline__ double warp_sum_pair(FF a) {
+    float s = a.h, e = a.l;
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) {
+        const float s2 = __shfl_down_sync(0xffffffffu, s, o), e2 = __shfl_down_sync(0xffffffffu, e, o);
+        float t, te;
+        two_sum(s, s2, t, te);
+        te = __fadd_rn(te, __fadd_rn(e, e2));
+        fast_two_sum(t, te, s, e);
+    }
+    double r = 0.0;
+    if ((threadIdx.x & 31) == 0) r = (double)s + (double)e;
+    return r;
+}
+__device__ __forceinline__ double warp_max_lane0(float v) {
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) v = fmaxf(v, __shfl_down_sync(0xffffffffu, v, o));
+    double r = 0.0;
+    if ((threadIdx.x & 31) == 0) r = (double)v;
+    return r;
+}
 
 // a - b as Real
 __device__ __forceinline__ void pdiff(const Pos<double>& a, const Pos<double>& b, double r[3]) {
@@ -289,7 +335,9 @@ __device__ __forceinline__ double warp_sum_ff(float v) {
         te = __fadd_rn(te, __fadd_rn(e, e2));
         fast_two_sum(t, te, s, e);
     }
-    return (double)s + (double)e;
+    double r = 0.0;
+    if ((threadIdx.x & 31) == 0) r = (double)s + (double)e;
+    return r;
 }
 __device__ __forceinline__ double warp_sum_r(double v) { return warp_sum(v); }
 __device__ __forceinline__ double warp_sum_r(float v) { return warp_sum_ff(v); }
@@ -297,7 +345,9 @@ __device__ __forceinline__ double warp_max_r(double v) { return warp_max(v); }
 __device__ __forceinline__ double warp_max_r(float v) {
 #pragma unroll
     for (int o = 16; o > 0; o >>= 1) v = fmaxf(v, __shfl_down_sync(0xffffffffu, v, o));
-    return (double)v;
+    double r = 0.0;
+    if ((threadIdx.x & 31) == 0) r = (double)v;
+    return r;
 }
 __device__ __forceinline__ double block_sum_r(double v, double* sh) { return block_sum(v, sh); }
 __device__ __forceinline__ double block_sum_r(float v, double* sh) {
@@ -329,7 +379,9 @@ __device__ __forceinline__ double block_max_r(float v, double* sh) {
     return r;
 }
 
-__device__ __forceinline__ bool near_zero_theta(double t) { return fabs(t - 0.0) < 1e-6; }  // areEqual (utility.h:75-78)
+// areEqual(theta0, 0) (utility.h:75-78), in the engine's precision
+__device__ __forceinline__ bool near_zero_theta(double t) { return fabs(t - 0.0) < 1e-6; }
+__device__ __forceinline__ bool near_zero_theta(float t) { return fabsf(t) < 1e-6f; }
 
 // the four filament constants of a bead slot in one vector load
 __device__ __forceinline__ void load_par(const float* P, int j, float& ks, float& l0, float& kb, float& t0) {
@@ -373,7 +425,7 @@ __device__ __forceinline__ Real bend_energy(const Real r1[3], const Real r2[3], 
     Real x = l1l2 / L1L2;
     if (x < (Real)-1) x = (Real)-1;
     else if (x > (Real)1) x = (Real)1;
-    if (near_zero_theta((double)t0)) {
+    if (near_zero_theta(t0)) {
         if (sizeof(Real) == 4 && l1l2 > (Real)0) {
             // 1 - cos = |r1 x r2|^2 / (L1 L2 (L1 L2 + r1.r2)): no cancellation in single precision
             const Real cx = r1[1] * r2[2] - r1[2] * r2[1];
@@ -401,7 +453,7 @@ __device__ __forceinline__ void bend_force(const Real r1[3], const Real r2[3], R
     const Real B = x / L1sq;
     const Real C = x / L2sq;
     Real kk;
-    if (near_zero_theta((double)t0)) {
+    if (near_zero_theta(t0)) {
         kk = k;
     } else {
         if (fabs(fabs(x) - (Real)1) < (Real)0.001) x = (Real)0.999 * x;

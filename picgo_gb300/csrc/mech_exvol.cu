@@ -79,7 +79,7 @@ __device__ __forceinline__ T dot3(const T* u, const T* v) {
 // avoids the cancellation of the reference's sqrt((ac + e)(ac - e)) forms.
 template <typename T>
 __device__ __forceinline__ void pair_inv(const T* v12, const T* v34, const T* v31, const T* v14, const T* v32,
-                                         PairInv<T>& p, bool cross) {
+                                         const T* v24, PairInv<T>& p, bool cross) {
     p.a = dot3(v12, v12);
     p.b = dot3(v34, v34);
     p.c = dot3(v31, v31);
@@ -123,15 +123,25 @@ __device__ __forceinline__ void pair_inv(const T* v12, const T* v34, const T* v3
         p.GG = p.d * p.g - p.a * p.I;
     }
     p.HH = p.CC + p.GG - p.DD;
-    p.ATG1 = atan_of((p.a + p.e) / p.AA) - atan_of(p.e / p.AA);
-    p.ATG2 = atan_of((p.a + p.e - p.d) / p.EE) - atan_of((p.e - p.d) / p.EE);
-    p.ATG3 = atan_of((p.F) / p.BB) - atan_of((p.F - p.b) / p.BB);
-    p.ATG4 = atan_of((p.d + p.F) / p.FF) - atan_of((p.d + p.F - p.b) / p.FF);
+    if (cross) {
+        // each arctangent difference as one atan2 (exact identities, e.g.
+        // atan((a+e)/AA) - atan(e/AA) = atan2(AA, c + e) with c + e = v31 . v32),
+        // free of the cancellation between two angles near +-pi/2
+        p.ATG1 = atan2(p.AA, dot3(v31, v32));
+        p.ATG2 = atan2(p.EE, dot3(v14, v24));
+        p.ATG3 = atan2(p.BB, -dot3(v31, v14));
+        p.ATG4 = atan2(p.FF, -dot3(v32, v24));
+    } else {
+        p.ATG1 = atan_of((p.a + p.e) / p.AA) - atan_of(p.e / p.AA);
+        p.ATG2 = atan_of((p.a + p.e - p.d) / p.EE) - atan_of((p.e - p.d) / p.EE);
+        p.ATG3 = atan_of((p.F) / p.BB) - atan_of((p.F - p.b) / p.BB);
+        p.ATG4 = atan_of((p.d + p.F) / p.FF) - atan_of((p.d + p.F - p.b) / p.FF);
+    }
 }
 
 template <typename T>
 __device__ __forceinline__ void diffs_of(const double* c1, const double* c2, const double* c3, const double* c4, T* v12,
-                                         T* v34, T* v31, T* v14, T* v32) {
+                                         T* v34, T* v31, T* v14, T* v32, T* v24) {
 #pragma unroll
     for (int k = 0; k < 3; ++k) {
         v12[k] = (T)(c2[k] - c1[k]);
@@ -139,6 +149,7 @@ __device__ __forceinline__ void diffs_of(const double* c1, const double* c2, con
         v31[k] = (T)(c1[k] - c3[k]);
         v14[k] = (T)(c4[k] - c1[k]);
         v32[k] = (T)(c2[k] - c3[k]);
+        v24[k] = (T)(c4[k] - c2[k]);
     }
 }
 
@@ -153,11 +164,14 @@ __device__ __forceinline__ double energy_from(const PairInv<T>& p, T kRepScaled)
     if (bad_value(U) || U < (T)-1) return __longlong_as_double(0x7ff8000000000000ULL);
     return (double)U;
 }
-static __device__ double pair_energy_d(const double* c1, const double* c2, const double* c3, const double* c4, double kRep) {
-    double v12[3], v34[3], v31[3], v14[3], v32[3];
-    diffs_of(c1, c2, c3, c4, v12, v34, v31, v14, v32);
+// `ref` selects the reference's forms (the FP64 engine, for parity);
+// otherwise the cancellation-free forms (the mixed engine's FP64 pass).
+static __device__ double pair_energy_d(const double* c1, const double* c2, const double* c3, const double* c4, double kRep,
+                                       bool ref = true) {
+    double v12[3], v34[3], v31[3], v14[3], v32[3], v24[3];
+    diffs_of(c1, c2, c3, c4, v12, v34, v31, v14, v32, v24);
     PairInv<double> p;
-    pair_inv(v12, v34, v31, v14, v32, p, false);
+    pair_inv(v12, v34, v31, v14, v32, v24, p, !ref);
     return energy_from(p, kRep);
 }
 
@@ -276,17 +290,17 @@ __device__ bool forces_from(const PairInv<T>& p, const T* v1, const T* v2, const
 // FP64 forces of a pair at double positions, with the reference's coplanar
 // move of c2 (:610-626, force path only).
 static __device__ bool pair_forces_d(const double* c1, const double* c2in, const double* c3, const double* c4, double kRep,
-                              double out[4][3]) {
+                                     double out[4][3], bool ref = true) {
     double moved2[3];
     const double* c2 = c2in;
     if (coplanarity<double>(c1, c2in, c3, c4) < 0.1) {
         push_c2(c1, c2in, c3, moved2);
         c2 = moved2;
     }
-    double v12[3], v34[3], v31[3], v14[3], v32[3];
-    diffs_of(c1, c2, c3, c4, v12, v34, v31, v14, v32);
+    double v12[3], v34[3], v31[3], v14[3], v32[3], v24[3];
+    diffs_of(c1, c2, c3, c4, v12, v34, v31, v14, v32, v24);
     PairInv<double> p;
-    pair_inv(v12, v34, v31, v14, v32, p, false);
+    pair_inv(v12, v34, v31, v14, v32, v24, p, !ref);
     return forces_from(p, v12, v34, v31, kRep, out);
 }
 
@@ -438,8 +452,8 @@ __device__ __forceinline__ void flag_fallback(const DevNet<Real>& n, int r, int 
     }
 }
 
-constexpr float kMixedTauEnergy = 0.01f;   // FP64 below this normalized triple product (energy)
-constexpr float kMixedTauForce = 0.05f;    // (forces, whose formula loses more to cancellation)
+constexpr float kMixedTauEnergy = 0.005f;  // FP64 below this normalized triple product (energy)
+constexpr float kMixedTauForce = 0.02f;    // (forces, whose formula loses more to cancellation)
 
 // Warp-aggregated append of (replica, pair) to the FP64 pair list.
 template <typename Real>
@@ -509,12 +523,13 @@ __global__ void __launch_bounds__(kBlock) k_exvol(DevNet<Real> n, int want, int 
             }
         } else {
             // mixed engine: single precision unless the pair is ill-conditioned
-            float v12[3], v34[3], v31[3], v14[3], v32[3];
+            float v12[3], v34[3], v31[3], v14[3], v32[3], v24[3];
             pdiff(p2, p1, v12);
             pdiff(p4, p3, v34);
             pdiff(p1, p3, v31);
             pdiff(p4, p1, v14);
             pdiff(p2, p3, v32);
+            pdiff(p4, p2, v24);
             const float cx = v12[1] * v34[2] - v12[2] * v34[1], cy = v12[2] * v34[0] - v12[0] * v34[2],
                         cz = v12[0] * v34[1] - v12[1] * v34[0];
             const float trip = fabsf(cx * v31[0] + cy * v31[1] + cz * v31[2]);
@@ -532,7 +547,7 @@ __global__ void __launch_bounds__(kBlock) k_exvol(DevNet<Real> n, int want, int 
             }
             if (!need64) {
                 PairInv<float> pi;
-                pair_inv(v12, v34, v31, v14, v32, pi, true);
+                pair_inv(v12, v34, v31, v14, v32, v24, pi, true);
                 if (!force) {
                     const double u = energy_from(pi, (float)kRepD);
                     if (u != u) need64 = true;
@@ -576,7 +591,7 @@ __global__ void __launch_bounds__(128) k_exvol_fp64(DevNet<Real> n, int trial, i
         to_double(bead_at(X, n.d, bs.w, tr, lam), c4);
         const double kRepD = (double)n.ev_k[i] * (double)n.ev_la[i] * (double)n.ev_lb[i];
         if (!force) {
-            const double u = pair_energy_d(c1, c2, c3, c4, kRepD);
+            const double u = pair_energy_d(c1, c2, c3, c4, kRepD, false);
             if (u != u) {
                 flag_fallback(n, r, i, tr ? lam : 0.0);
                 n.ev_energy[i] = 0.0;
@@ -585,7 +600,7 @@ __global__ void __launch_bounds__(128) k_exvol_fp64(DevNet<Real> n, int trial, i
             }
         } else {
             double out[4][3];
-            const bool ok = pair_forces_d(c1, c2, c3, c4, kRepD, out);
+            const bool ok = pair_forces_d(c1, c2, c3, c4, kRepD, out, false);
             Real* cdst = n.contrib + 3 * (size_t)(n.slot_base[K_EXVOL] + 4 * i);
             for (int a = 0; a < 4; ++a)
                 for (int q = 0; q < 3; ++q) cdst[3 * a + q] = (Real)out[a][q];

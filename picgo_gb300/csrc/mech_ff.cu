@@ -16,6 +16,8 @@
 // forces follow the reference's per-bead summation order.
 #include <cuda_runtime.h>
 
+#include <algorithm>
+
 #include "mech_device.cuh"
 
 namespace mech {
@@ -71,13 +73,27 @@ __device__ __forceinline__ bool replica_selected(const CGState& S, int want) {
 // ---------------------------------------------------------------------------
 // finalizers (run by the whole last block of a replica)
 // ---------------------------------------------------------------------------
+// Partial-sum slots of a replica's tile range [b, e): the FP64 kernels write
+// one per tile (stride 1); the persistent mixed kernels write one per run of
+// tiles, at b and at every multiple of their tiles-per-block inside (b, e).
+__device__ __forceinline__ int run_slots(int b, int e, int stride) {
+    const int m0 = (b / stride + 1) * stride;
+    return 1 + (m0 < e ? (e - 1 - m0) / stride + 1 : 0);
+}
+__device__ __forceinline__ int run_slot(int b, int stride, int k) {
+    return k == 0 ? b : (b / stride + 1) * stride + (k - 1) * stride;
+}
+
 template <typename Real>
 __device__ void finalize_energy(const DevNet<Real>& n, int r, int trial, double* sh) {
     const RepTiles rt = n.rt[r];
+    const int stride = sizeof(Real) == 4 ? n.ptiles[0] : 1;
+    const int nslot = run_slots(rt.fil_begin, rt.fil_end, stride);
     // every thread issues its loads back to back, then sums in a fixed order
     double acc[MECH_NUM_FF] = {0, 0, 0, 0, 0, 0};
 #pragma unroll 8
-    for (int i = rt.fil_begin + threadIdx.x; i < rt.fil_end; i += blockDim.x) {
+    for (int k = threadIdx.x; k < nslot; k += blockDim.x) {
+        const int i = run_slot(rt.fil_begin, stride, k);
         const double2 v = __ldcg(reinterpret_cast<const double2*>(n.part_fil + 4 * (size_t)i));
         acc[MECH_FF_STRETCHING] += v.x;
         acc[MECH_FF_BENDING] += v.y;
@@ -139,9 +155,12 @@ __device__ void finalize_energy(const DevNet<Real>& n, int r, int trial, double*
 template <typename Real>
 __device__ void finalize_force(const DevNet<Real>& n, int r, double* sh) {
     const RepTiles rt = n.rt[r];
+    const int stride = sizeof(Real) == 4 ? n.ptiles[1] : 1;
+    const int nslot = run_slots(rt.fil_begin, rt.fil_end, stride);
     double a_mx = 0.0, a_ff = 0.0, a_ffp = 0.0;
 #pragma unroll 8
-    for (int i = rt.fil_begin + threadIdx.x; i < rt.fil_end; i += blockDim.x) {
+    for (int k = threadIdx.x; k < nslot; k += blockDim.x) {
+        const int i = run_slot(rt.fil_begin, stride, k);
         const double2 v = __ldcg(reinterpret_cast<const double2*>(n.part_fil + 4 * (size_t)i));
         const double w = __ldcg(n.part_fil + 4 * (size_t)i + 2);
         a_mx = fmax(a_mx, v.x);
@@ -344,6 +363,280 @@ __global__ void __launch_bounds__(kBlock) k_fil_force(DevNet<Real> n, int want) 
         const RepTiles rt = n.rt[r];
         if (last_tile(n.ticket, r, rt.fil_end - rt.fil_begin, &s_flag)) finalize_force(n, r, sh);
     }
+}
+
+// ---------------------------------------------------------------------------
+// Mixed engine: persistent, barrier-free filament kernels.  Each block walks
+// `ptiles` consecutive tiles; every thread owns one bead per tile and
+// recomputes in single precision the few neighbouring stretching and bending
+// terms it needs (cheaper than staging through shared memory at the FP32
+// rate), keeps compensated sums in registers across tiles, and the block
+// reduces once per run of tiles of the same replica.
+// ---------------------------------------------------------------------------
+
+// Close a run of `cnt` tiles of replica r that starts at tile `first`: reduce
+// the block's lane-0 warp results, store the partials in the run's first tile
+// slot (zeros in the others), count the tiles; true in every thread of the
+// block that completed the replica.
+template <int N>
+__device__ bool flush_run(const DevNet<float>& n, int r, int first, int cnt, double (&w)[N], const int (&ops)[N],
+                          double* sh, int* s_flag) {
+    block_combine<N>(w, ops, sh);
+    if (threadIdx.x == 0) {
+#pragma unroll
+        for (int k = 0; k < N; ++k) n.part_fil[4 * (size_t)first + k] = w[k];
+        __threadfence();
+        const RepTiles rt = n.rt[r];
+        const int old = atomicAdd(n.ticket + r, cnt);
+        *s_flag = (old + cnt == rt.fil_end - rt.fil_begin);
+        if (*s_flag) n.ticket[r] = 0;
+    }
+    __syncthreads();
+    const bool last = *s_flag != 0;
+    if (last) __threadfence();
+    return last;
+}
+
+__device__ __forceinline__ Pos<float> pos_at(const DevNet<float>& n, const float* X, int b, bool tr, float lf) {
+    const Pos<float> p = load_pos(X, b);
+    return tr ? moved_f(p, n.d, b, lf) : p;
+}
+
+__global__ void __launch_bounds__(kBlock) k_fil_energy_mx(DevNet<float> n, int want, int trial) {
+    __shared__ double sh[32 * MECH_NUM_FF];
+    __shared__ int s_flag;
+    const int t0 = blockIdx.x * n.ptiles[0], t1 = min(t0 + n.ptiles[0], n.n_ftiles);
+    const bool tr = trial != 0;
+    int cur = -1, first = 0, cnt = 0, xb = 0;
+    bool go = false;
+    float lf = 0.f;
+    FF es, eb;
+    const int ops[2] = {0, 0};
+    for (int ti = t0; ti < t1; ++ti) {
+        const Tile t = n.ftile[ti];
+        if (t.replica != cur) {
+            if (cnt) {
+                double w[2] = {warp_sum_pair(es), warp_sum_pair(eb)};
+                if (flush_run<2>(n, cur, first, cnt, w, ops, sh, &s_flag)) finalize_energy(n, cur, trial, sh);
+            }
+            cur = t.replica;
+            first = ti;
+            cnt = 0;
+            es = FF();
+            eb = FF();
+            const CGState& S = n.st[cur];
+            go = replica_selected(S, want);
+            xb = S.xbuf;
+            lf = (float)S.lambda;
+        }
+        if (!go) continue;
+        ++cnt;
+        const int b = t.begin + threadIdx.x;
+        if (b < t.end) {
+            const float* X = n.x[xb];
+            const int fl = n.bflag[b];
+            const Pos<float> p0 = pos_at(n, X, b, tr, lf);
+            if (tr) store_pos(n.x[xb ^ 1], b, p0);   // materialize the owned trial position
+            if (fl & 1) {
+                float ks, l0, kb, th;
+                load_par(n.bpar, b, ks, l0, kb, th);
+                const Pos<float> pp = pos_at(n, X, b + 1, tr, lf);
+                float r2[3];
+                pdiff(pp, p0, r2);
+                es.add(stretch_energy<float>(r2[0], r2[1], r2[2], ks, l0));
+                if (fl & 2) {
+                    const Pos<float> pm = pos_at(n, X, b - 1, tr, lf);
+                    float r1[3];
+                    pdiff(p0, pm, r1);
+                    eb.add(bend_energy<float>(r1, r2, kb, th));
+                }
+            }
+        }
+    }
+    if (cnt) {
+        double w[2] = {warp_sum_pair(es), warp_sum_pair(eb)};
+        if (flush_run<2>(n, cur, first, cnt, w, ops, sh, &s_flag)) finalize_energy(n, cur, trial, sh);
+    }
+}
+
+__global__ void __launch_bounds__(kBlock) k_fil_force_mx(DevNet<float> n, int want) {
+    __shared__ double sh[32 * 3];
+    __shared__ int s_flag;
+    const int t0 = blockIdx.x * n.ptiles[1], t1 = min(t0 + n.ptiles[1], n.n_ftiles);
+    int cur = -1, first = 0, cnt = 0, xb = 0, fb = 0;
+    bool go = false;
+    float mx = 0.f;
+    FF ff, ffp;
+    const int ops[3] = {1, 0, 0};
+    for (int ti = t0; ti < t1; ++ti) {
+        const Tile t = n.ftile[ti];
+        if (t.replica != cur) {
+            if (cnt) {
+                double w[3] = {warp_max_lane0(mx), warp_sum_pair(ff), warp_sum_pair(ffp)};
+                if (flush_run<3>(n, cur, first, cnt, w, ops, sh, &s_flag)) finalize_force(n, cur, sh);
+            }
+            cur = t.replica;
+            first = ti;
+            cnt = 0;
+            mx = 0.f;
+            ff = FF();
+            ffp = FF();
+            const CGState& S = n.st[cur];
+            go = replica_selected(S, want);
+            xb = S.xbuf;
+            fb = S.fbuf;
+        }
+        if (!go) continue;
+        ++cnt;
+        const int b = t.begin + threadIdx.x;
+        if (b < t.end) {
+            const float* X = n.x[xb];
+            const int f0 = n.bflag[b];
+            const int fm = (f0 & 2) ? n.bflag[b - 1] : 0;
+            const int fp = (f0 & 1) ? n.bflag[b + 1] : 0;
+            const Pos<float> p0 = load_pos(X, b);
+            Pos<float> pm1 = p0, pp1 = p0, pm2 = p0, pp2 = p0;
+            if (f0 & 2) pm1 = load_pos(X, b - 1);
+            if (f0 & 1) pp1 = load_pos(X, b + 1);
+            if (fm & 2) pm2 = load_pos(X, b - 2);
+            if (fp & 1) pp2 = load_pos(X, b + 2);
+            float F[3] = {0.f, 0.f, 0.f};
+            float ksm = 0, l0m = 0, kbm = 0, thm = 0, ks = 0, l0 = 0, kb = 0, th = 0;
+            if (f0 & 2) load_par(n.bpar, b - 1, ksm, l0m, kbm, thm);
+            if (f0 & 1) load_par(n.bpar, b, ks, l0, kb, th);
+            float rm[3] = {0, 0, 0}, rp[3] = {0, 0, 0};
+            if (f0 & 2) pdiff(p0, pm1, rm);
+            if (f0 & 1) pdiff(pp1, p0, rp);
+            // stretching: cylinder (b-1, b) then (b, b+1)
+            if (f0 & 2) {
+                float S1[3];
+                stretch_force<float>(rm[0], rm[1], rm[2], ksm, l0m, S1);
+                F[0] += S1[0]; F[1] += S1[1]; F[2] += S1[2];
+            }
+            if (f0 & 1) {
+                float S2[3];
+                stretch_force<float>(rp[0], rp[1], rp[2], ks, l0, S2);
+                F[0] += -S2[0]; F[1] += -S2[1]; F[2] += -S2[2];
+            }
+            // bending: triples centred on b-1, b, b+1
+            if ((f0 & 2) && (fm & 2)) {
+                float r1[3], a1[3], a2[3];
+                pdiff(pm1, pm2, r1);
+                bend_force<float>(r1, rm, kbm, thm, a1, a2);
+                F[0] += a2[0]; F[1] += a2[1]; F[2] += a2[2];
+            }
+            if ((f0 & 3) == 3) {
+                float a1[3], a2[3];
+                bend_force<float>(rm, rp, kb, th, a1, a2);
+                F[0] += a1[0] - a2[0]; F[1] += a1[1] - a2[1]; F[2] += a1[2] - a2[2];
+            }
+            if ((f0 & 1) && (fp & 1)) {
+                float ksp, l0p, kbp, thp, r2[3], a1[3], a2[3];
+                load_par(n.bpar, b + 1, ksp, l0p, kbp, thp);
+                pdiff(pp2, pp1, r2);
+                bend_force<float>(rp, r2, kbp, thp, a1, a2);
+                F[0] += -a1[0]; F[1] += -a1[1]; F[2] += -a1[2];
+            }
+            const int c0 = n.csr_off[b], c1 = n.csr_off[b + 1];
+            for (int c = c0; c < c1; ++c) {
+                const int sl = n.csr_slot[c];
+                F[0] += n.contrib[3 * (size_t)sl];
+                F[1] += n.contrib[3 * (size_t)sl + 1];
+                F[2] += n.contrib[3 * (size_t)sl + 2];
+            }
+            float* Fo = n.f[fb ^ 1] + 3 * (size_t)b;
+            const float* Fp = n.f[fb] + 3 * (size_t)b;
+            Fo[0] = F[0];
+            Fo[1] = F[1];
+            Fo[2] = F[2];
+            mx = fmaxf(mx, fmaxf(fmaxf(fabsf(F[0]), fabsf(F[1])), fabsf(F[2])));
+            ff.add(bead_dot(F[0], F[1], F[2], F[0], F[1], F[2]));
+            ffp.add(bead_dot(F[0], F[1], F[2], Fp[0], Fp[1], Fp[2]));
+        }
+    }
+    if (cnt) {
+        double w[3] = {warp_max_lane0(mx), warp_sum_pair(ff), warp_sum_pair(ffp)};
+        if (flush_run<3>(n, cur, first, cnt, w, ops, sh, &s_flag)) finalize_force(n, cur, sh);
+    }
+}
+
+// Mixed engine: persistent direction update d = F + beta d with the d.F partials.
+__global__ void __launch_bounds__(kBlock) k_direction_mx(DevNet<float> n) {
+    __shared__ double sh[32];
+    __shared__ int s_flag;
+    const int t0 = blockIdx.x * n.ptiles[2], t1 = min(t0 + n.ptiles[2], n.n_ftiles);
+    int cur = -1, first = 0, cnt = 0, fb = 0, xb = 0, bk = 0;
+    bool go = false;
+    float beta = 0.f;
+    FF dF;
+    const int ops[1] = {0};
+    auto finish = [&](int r) {
+        double w[1] = {warp_sum_pair(dF)};
+        // the run's partial goes to slot 3 of its first tile (zeros elsewhere)
+        block_combine<1>(w, ops, sh);
+        if (threadIdx.x == 0) {
+            n.part_fil[4 * (size_t)first + 3] = w[0];
+            __threadfence();
+            const RepTiles rt = n.rt[r];
+            const int old = atomicAdd(n.ticket + r, cnt);
+            s_flag = (old + cnt == rt.fil_end - rt.fil_begin);
+            if (s_flag) n.ticket[r] = 0;
+        }
+        __syncthreads();
+        if (s_flag) {
+            __threadfence();
+            const RepTiles rt = n.rt[r];
+            double a = 0.0;
+            const int nslot = run_slots(rt.fil_begin, rt.fil_end, n.ptiles[2]);
+            for (int k = threadIdx.x; k < nslot; k += blockDim.x)
+                a += __ldcg(n.part_fil + 4 * (size_t)run_slot(rt.fil_begin, n.ptiles[2], k) + 3);
+            const double slope = block_sum(a, sh);
+            if (threadIdx.x == 0) {
+                CGState& S = n.st[r];
+                if (S.backupPending) {
+                    S.backupValid = 1;
+                    S.backupPending = 0;
+                }
+                if (slope <= 0) {
+                    S.phase = PH_RESET;
+                } else {
+                    S.slope = slope;
+                    if (S.method >= 1) S.lastFdotF = S.newGrad;
+                    begin_iteration(S);
+                }
+            }
+        }
+    };
+    for (int ti = t0; ti < t1; ++ti) {
+        const Tile t = n.ftile[ti];
+        if (t.replica != cur) {
+            if (cnt) finish(cur);
+            cur = t.replica;
+            first = ti;
+            cnt = 0;
+            dF = FF();
+            const CGState& S = n.st[cur];
+            go = S.phase == PH_DIR;
+            fb = S.fbuf;
+            xb = S.xbuf;
+            bk = S.backupPending;
+            beta = (float)S.beta;
+        }
+        if (!go) continue;
+        ++cnt;
+        const int b = t.begin + threadIdx.x;
+        if (b < t.end) {
+            const float* F = n.f[fb] + 3 * (size_t)b;
+            float* D = n.d + 3 * (size_t)b;
+            const float d0 = F[0] + beta * D[0], d1 = F[1] + beta * D[1], d2 = F[2] + beta * D[2];
+            D[0] = d0;
+            D[1] = d1;
+            D[2] = d2;
+            dF.add(bead_dot(d0, d1, d2, F[0], F[1], F[2]));
+            if (bk) store_pos(n.xbest, b, load_pos(n.x[xb], b));
+        }
+    }
+    if (cnt) finish(cur);
 }
 
 // ---------------------------------------------------------------------------
@@ -624,7 +917,8 @@ int launch_energy(const DevNet<Real>& n, int want, int trial, cudaStream_t s) {
         ++launched;
     }
     launched += launch_exvol_energy<Real>(n, want, trial, s);
-    k_fil_energy<Real><<<n.n_ftiles, kBlock, 0, s>>>(n, want, trial);
+    if constexpr (sizeof(Real) == 4) k_fil_energy_mx<<<n.pgrid[0], kBlock, 0, s>>>(n, want, trial);
+    else k_fil_energy<Real><<<n.n_ftiles, kBlock, 0, s>>>(n, want, trial);
     return launched + 1;
 }
 
@@ -638,13 +932,15 @@ int launch_forces(const DevNet<Real>& n, int want, cudaStream_t s) {
         ++launched;
     }
     launched += launch_exvol_forces<Real>(n, want, s);
-    k_fil_force<Real><<<n.n_ftiles, kBlock, 0, s>>>(n, want);
+    if constexpr (sizeof(Real) == 4) k_fil_force_mx<<<n.pgrid[1], kBlock, 0, s>>>(n, want);
+    else k_fil_force<Real><<<n.n_ftiles, kBlock, 0, s>>>(n, want);
     return launched + 1;
 }
 
 template <typename Real>
 int launch_direction(const DevNet<Real>& n, cudaStream_t s) {
-    k_direction<Real><<<n.n_ftiles, kBlock, 0, s>>>(n);
+    if constexpr (sizeof(Real) == 4) k_direction_mx<<<n.pgrid[2], kBlock, 0, s>>>(n);
+    else k_direction<Real><<<n.n_ftiles, kBlock, 0, s>>>(n);
     return 1;
 }
 
@@ -683,12 +979,33 @@ int launch_part(const DevNet<Real>& n, int which, cudaStream_t s) {
     int ev_t = 0, bb_t = 0;
     const int lm = n_lm_tiles(n, &ev_t, &bb_t);
     switch (which) {
-        case 0: k_fil_energy<Real><<<n.n_ftiles, kBlock, 0, s>>>(n, -1, 0); return 1;
-        case 1: k_fil_force<Real><<<n.n_ftiles, kBlock, 0, s>>>(n, -1); return 1;
+        case 0:
+            if constexpr (sizeof(Real) == 4) k_fil_energy_mx<<<n.pgrid[0], kBlock, 0, s>>>(n, -1, 0);
+            else k_fil_energy<Real><<<n.n_ftiles, kBlock, 0, s>>>(n, -1, 0);
+            return 1;
+        case 1:
+            if constexpr (sizeof(Real) == 4) k_fil_force_mx<<<n.pgrid[1], kBlock, 0, s>>>(n, -1);
+            else k_fil_force<Real><<<n.n_ftiles, kBlock, 0, s>>>(n, -1);
+            return 1;
         case 2: if (lm + bb_t > 0) { k_bond_bnd<Real><<<lm + bb_t, kBlock, 0, s>>>(n, -1, 0, 0, lm, ev_t); return 1; } return 0;
         case 3: if (lm + bb_t > 0) { k_bond_bnd<Real><<<lm + bb_t, kBlock, 0, s>>>(n, -1, 0, 1, lm, ev_t); return 1; } return 0;
     }
     return 0;
+}
+
+// Grid of the mixed engine's persistent filament kernels: every SM full.
+int persistent_blocks(int device, int which) {
+    static int cached_dev = -1, cached[3] = {0, 0, 0};
+    if (cached_dev != device) {
+        int sms = 0, b[3] = {0, 0, 0};
+        cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, device);
+        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b[0], k_fil_energy_mx, kBlock, 0);
+        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b[1], k_fil_force_mx, kBlock, 0);
+        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b[2], k_direction_mx, kBlock, 0);
+        for (int k = 0; k < 3; ++k) cached[k] = std::max(1, sms) * std::max(1, b[k]);
+        cached_dev = device;
+    }
+    return cached[which];
 }
 
 #define MECH_INSTANTIATE(R)                                                             \

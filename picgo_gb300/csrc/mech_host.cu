@@ -126,6 +126,11 @@ DevNet<Real> make_devnet(MechContext* c) {
     n.bpar = c->bpar.as<Real>();
     n.n_ftiles = c->n_ftiles;
     n.ftile = c->ftile.as<Tile>();
+    for (int k = 0; k < 3; ++k) {
+        n.pgrid[k] = std::max(1, std::min(c->n_ftiles, persistent_blocks(c->device, k)));
+        n.ptiles[k] = (c->n_ftiles + n.pgrid[k] - 1) / n.pgrid[k];
+        n.pgrid[k] = (c->n_ftiles + n.ptiles[k] - 1) / n.ptiles[k];
+    }
     n.n_lk = c->nlk;
     n.n_mt = c->nmt;
     n.n_ev = (int)c->nev;
@@ -1158,8 +1163,13 @@ static int profile_impl(MechContext* c, int iters, MechProfile* o) {
     o->ms_fil_force = timeit([&] { launch_part<Real>(n, 1, s); });
     o->ms_bond_energy = timeit([&] { launch_part<Real>(n, 2, s); });
     o->ms_bond_force = timeit([&] { launch_part<Real>(n, 3, s); });
+    int cnt = 0;
     o->ms_exvol_energy = timeit([&] { launch_exvol_energy<Real>(n, -1, 0, s); });
+    cudaMemcpy(&cnt, c->ev_list_count.p, sizeof(int), cudaMemcpyDeviceToHost);
+    o->n_exvol_fp64_energy = c->precision == MECH_PREC_MIXED ? cnt : c->nev;
     o->ms_exvol_force = timeit([&] { launch_exvol_forces<Real>(n, -1, s); });
+    cudaMemcpy(&cnt, c->ev_list_count.p, sizeof(int), cudaMemcpyDeviceToHost);
+    o->n_exvol_fp64_force = c->precision == MECH_PREC_MIXED ? cnt : c->nev;
     cudaEventDestroy(e0);
     cudaEventDestroy(e1);
     CU(cudaGetLastError());

@@ -110,9 +110,11 @@ struct DevNet {
     Real* xbest;
     const uint8_t* bflag;
     const Real* bpar;       // per bead slot: k_str, l0 of cylinder (i, i+1); k_bend, theta0 of the triple on i
-    // filament tiles
+    // filament tiles; the mixed engine's persistent filament kernels give each
+    // block `ptiles` consecutive tiles on a grid of `pgrid` blocks
     int n_ftiles;
     const Tile* ftile;
+    int pgrid[3], ptiles[3];   // [0] energy, [1] force, [2] direction kernels
     // sparse interactions (internal bead indices)
     int n_lk, n_mt, n_ev, n_bb;
     const int4* lk_bead; const Real* lk_k; const Real* lk_l0; const Real* lk_s1; const Real* lk_s2;
@@ -167,6 +169,9 @@ template <typename Real> int launch_backup_restore(const DevNet<Real>& n, cudaSt
 // single kernel families in plain-evaluation mode, for profiling:
 // 0 filament energy, 1 filament force, 2 bond/boundary energy, 3 bond/boundary force
 template <typename Real> int launch_part(const DevNet<Real>& n, int which, cudaStream_t s);
+// blocks of the mixed engine's persistent filament kernels on `device`
+// (which: 0 energy, 1 force, 2 direction)
+int persistent_blocks(int device, int which);
 // excluded-volume kernels (mech_exvol.cu, one object per precision)
 template <typename Real> int launch_exvol_energy(const DevNet<Real>& n, int want, int trial, cudaStream_t s);
 template <typename Real> int launch_exvol_forces(const DevNet<Real>& n, int want, cudaStream_t s);
