@@ -253,6 +253,37 @@ typedef struct MechProfile {
 } MechProfile;
 int32_t mech_profile(MechContext* ctx, int32_t iters, MechProfile* out);
 
+/*
+ * Filament stretching and bending energies (FP64) of one network held in
+ * caller-owned DEVICE memory, without allocating: no reference counterpart
+ * (MEDYAN evaluates these inside ForceFieldManager::computeIndividualEnergies;
+ * this is a stand-alone variant for callers that cannot allocate).
+ *
+ * For callers that must not allocate device memory at this point: cudaMalloc
+ * and cudaFree can synchronize the whole device, and some hosts hand every
+ * byte of HBM to their own pool up front.  The call needs no context; its
+ * scratch is a fixed 131,328-byte device array inside the library.
+ *
+ * Inputs (device pointers, current device): fil_cyl_start[n_filaments+1]
+ * ascending cylinder ranges from 0 to n_cylinders (not checked: the arrays
+ * are on the device); coord[3 * (n_cylinders + n_filaments)] with the
+ * beads filament by filament, minus end first (cylinder c of filament f joins
+ * beads c + f and c + f + 1); per-cylinder k_stretch, eq_length, k_bend,
+ * eq_theta (the bending triple ending in cylinder c uses c's constants).
+ * Output: energies[2] = {stretching, bending}, written on `stream` (a
+ * cudaStream_t; NULL = legacy default stream); synchronize before reading.
+ *
+ * Limits: n_cylinders <= 2,097,152, else MECH_ERR_CAPACITY and nothing runs.
+ * The first call on each device looks up the scratch address: make it before
+ * any stream capture on that device.  The scratch's completion ticket must be
+ * zero at launch: the call clears it on `stream` and the kernel leaves it
+ * zero.  Calls that overlap in time on one device share the scratch and
+ * race: issue them on one stream or order them.
+ */
+int32_t mech_filament_energy_device(int32_t n_filaments, int32_t n_cylinders, const int32_t* fil_cyl_start,
+                                    const double* coord, const double* k_stretch, const double* eq_length,
+                                    const double* k_bend, const double* eq_theta, double* energies, void* stream);
+
 #ifdef __cplusplus
 }
 #endif

@@ -32,7 +32,7 @@ EXPORTS = [
     "mech_abi_version", "mech_last_error", "mech_ctx_create", "mech_ctx_destroy", "mech_set_networks",
     "mech_set_coords", "mech_get_coords", "mech_rebuild_neighbors", "mech_get_pairs", "mech_energy",
     "mech_forces", "mech_minimize", "mech_get_forces", "mech_get_stretch_forces", "mech_get_timing",
-    "mech_reset_coords", "mech_profile",
+    "mech_reset_coords", "mech_profile", "mech_filament_energy_device",
 ]
 
 
@@ -134,6 +134,7 @@ def load(build_if_missing: bool = False):
         L.mech_get_timing.argtypes = [vp, C.POINTER(MechTiming)]
         L.mech_reset_coords.argtypes = [vp]
         L.mech_profile.argtypes = [vp, C.c_int32, C.POINTER(MechProfile)]
+        L.mech_filament_energy_device.argtypes = [C.c_int32, C.c_int32, vp, vp, vp, vp, vp, vp, vp, vp]
         for name in EXPORTS:
             f = getattr(L, name)
             if f.restype is None or f.restype is C.c_int:

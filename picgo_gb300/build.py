@@ -25,6 +25,7 @@ UNITS = [
     ("mech_exvol.cu", "mech_exvol_f32.o", ["-DMECH_EXVOL_REAL=float"]),
     ("mech_nl.cu", "mech_nl.o", []),
     ("mech_host.cu", "mech_host.o", []),
+    ("mech_static.cu", "mech_static.o", []),
 ]
 
 

@@ -26,6 +26,8 @@ static int set_err(int code, const std::string& msg) {
     return code;
 }
 
+int set_error_text(int code, const std::string& msg) { return set_err(code, msg); }
+
 #define CU(call)                                                                                   \
     do {                                                                                           \
         cudaError_t _e = (call);                                                                   \

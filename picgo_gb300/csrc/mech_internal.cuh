@@ -172,6 +172,9 @@ template <typename Real> int launch_part(const DevNet<Real>& n, int which, cudaS
 // blocks of the mixed engine's persistent filament kernels on `device`
 // (which: 0 energy, 1 force, 2 direction)
 int persistent_blocks(int device, int which);
+
+// Records the text mech_last_error returns on this thread; returns `code`.
+int set_error_text(int code, const std::string& msg);
 // excluded-volume kernels (mech_exvol.cu, one object per precision)
 template <typename Real> int launch_exvol_energy(const DevNet<Real>& n, int want, int trial, cudaStream_t s);
 template <typename Real> int launch_exvol_forces(const DevNet<Real>& n, int want, cudaStream_t s);
