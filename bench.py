@@ -14,13 +14,15 @@ the FP64 path's figures and the CPU oracle's are beside it.
 
 --impl reference: the oracle (a loop-for-loop CPU restatement of MEDYAN's
 minimizer; MEDYAN itself cannot be built here) on a bounded sample of the
-same workload, same metric.
+same workload, same metric, on all host threads (OpenMP); the single-thread
+figure, MEDYAN's own execution model, is reported beside the GPU line.
 """
 from __future__ import annotations
 
 import argparse
 import json
 import os
+import platform
 import statistics
 import subprocess
 import sys
@@ -254,26 +256,38 @@ def fp64_compare(args, net):
             "energy_after": r["energies_after"][6], "warmup_iters": r0["num_iter"]}
 
 
-def cpu_sample(net, seconds: float):
-    """The oracle's CG on the same network, bounded: force evaluations per second on one core."""
+def cpu_sample(net, seconds: float, threads: int = 1):
+    """The oracle's CG on the same network, bounded: force evaluations per second
+    on `threads` host threads (1 = serial, like MEDYAN's minimizer)."""
     import oracle
     t0 = time.perf_counter()
     vec = oracle.vectorize(net)
     t_vec = time.perf_counter() - t0
     limit = 8
-    while True:
-        t0 = time.perf_counter()
-        x, f, res = oracle.minimize(vec, net.coord, oracle.cg_params(energyRelTol=0.0, energyCallLimit=limit,
-                                                                       forceCallLimit=1_000_000))
-        dt = time.perf_counter() - t0
-        if dt >= seconds or limit >= 4096:
-            break
-        limit = int(limit * max(2.0, min(8.0, seconds / max(dt, 1e-3))))
-    return {"value": round(res.numForceCall / dt, 4), "unit": UNIT, "cores": 1, "kind": "port",
+    with oracle.threads(threads):
+        while True:
+            t0 = time.perf_counter()
+            x, f, res = oracle.minimize(vec, net.coord, oracle.cg_params(energyRelTol=0.0, energyCallLimit=limit,
+                                                                           forceCallLimit=1_000_000))
+            dt = time.perf_counter() - t0
+            if dt >= seconds or limit >= 4096:
+                break
+            limit = int(limit * max(2.0, min(8.0, seconds / max(dt, 1e-3))))
+    how = "single-threaded like MEDYAN's minimizer" if threads == 1 else \
+        f"OpenMP over {threads} host threads (force fields and CG vector loops)"
+    return {"value": round(res.numForceCall / dt, 4), "unit": UNIT, "cores": threads, "kind": "port",
             "sample": f"oracle CG on the same 1M-cylinder network from the same start, first {res.numIter} "
                       f"iterations ({res.numForceCall} force + {res.numEnergyCall} energy evaluations) in {dt:.1f} s "
-                      f"(vectorize {t_vec:.1f} s excluded); single-threaded like MEDYAN's minimizer",
+                      f"(vectorize {t_vec:.1f} s excluded); {how}; host {platform.machine()}, "
+                      f"{os.cpu_count()} logical CPUs",
             "seconds": round(dt, 2), "energy_evals_per_force_eval": round(res.numEnergyCall / max(1, res.numForceCall), 3)}
+
+
+def host_threads() -> int:
+    try:
+        return max(1, len(os.sched_getaffinity(0)))
+    except (AttributeError, OSError):
+        return max(1, os.cpu_count() or 1)
 
 
 def run_reference(args, rank, world):
@@ -284,7 +298,7 @@ def run_reference(args, rank, world):
     for _ in range(args.warmup):
         pass   # the oracle has no warm-up state; each step is a fresh bounded sample
     for _ in range(args.steps):
-        s = cpu_sample(net, args.cpu_seconds / max(1, args.steps))
+        s = cpu_sample(net, args.cpu_seconds / max(1, args.steps), host_threads())
         vals.append(s)
     v = sum(s["value"] for s in vals) / len(vals)
     cpu = dict(vals[-1])
@@ -293,7 +307,7 @@ def run_reference(args, rank, world):
             "steps": args.steps, "warmup": args.warmup, "higher_is_better": True, "scaling": "weak",
             "vs_baseline": None, "dtype": "f64", "data": "synthetic (seeded network generator; no dataset)",
             "config": {"workload": "20,000 filaments x 50 cylinders (1M cylinders), 50k linkers, 5k motors, 10 um box",
-                       "seed": SEED, "precision": "fp64 (CPU restatement of MEDYAN's minimizer)"},
+                       "seed": SEED, "precision": "fp64 (CPU restatement of MEDYAN's minimizer, all host threads)"},
             "cpu_baseline": cpu,
             "e2e": {"value": round(v, 4), "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
 
@@ -331,7 +345,9 @@ def main():
             out["mixed_vs_fp64_time_to_1pN"] = round(f["time_to_1pN_s"] / out["time_to_1pN_s"], 3)
             out["mixed_vs_fp64_evals_per_s"] = round(out["value"] / max(f["force_evals_per_s"], 1e-9), 3)
         if not args.no_cpu and world == 1:
-            out["cpu_baseline"] = cpu_sample(net, args.cpu_seconds)
+            out["cpu_baseline"] = cpu_sample(net, args.cpu_seconds * 0.6, host_threads())
+            one = cpu_sample(net, args.cpu_seconds * 0.4, 1)
+            out["cpu_baseline_1thread"] = {k: one[k] for k in ("value", "unit", "cores", "seconds")}
         print(json.dumps(out))
     if dist is not None:
         dist.destroy_process_group()

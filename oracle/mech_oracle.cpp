@@ -736,13 +736,99 @@ struct OrcSystem {
 
 enum { FF_STRETCH, FF_BEND, FF_LINKER, FF_MOTOR, FF_EXVOL, FF_BOUNDARY, FF_COUNT };
 
+// Host threads for the CPU baseline (orc_set_threads).  1, the default, keeps
+// every loop serial in the order the reference runs it, which is what the
+// parity tests compare against; more threads split each force field's
+// interactions into contiguous chunks (per-thread force buffers, chunk sums
+// added in chunk order) and the CG vector loops, so sums round differently.
+static int g_threads = 1;
+
+}  // extern "C"
+
+template <class Fn>
+static double chunked_energy(int n, Fn fn) {
+    const int T = g_threads;
+    if (T <= 1 || n < 2048) return fn(0, n);
+    std::vector<double> part(T, 0.0);
+#pragma omp parallel for num_threads(T) schedule(static, 1)
+    for (int t = 0; t < T; ++t) {
+        const int b = (int)((long long)n * t / T), e = (int)((long long)n * (t + 1) / T);
+        part[t] = fn(b, e - b);
+    }
+    double U = 0.0;
+    for (int t = 0; t < T; ++t) {
+        if (part[t] == -1.0) return -1.0;
+        U += part[t];
+    }
+    return U;
+}
+
+// fn(begin, count, force buffer) accumulates one chunk into a per-thread
+// buffer that covers only the DOF range its interactions touch (bs: `stride`
+// DOF offsets per interaction); the buffers are then added into f in thread
+// order.  Returns the chunks' summed status (-1 if any failed).
+template <class Fn>
+static int chunked_forces(int n, int stride, const int* bs, double* f, int nvar, Fn fn) {
+    const int T = g_threads;
+    if (T <= 1 || n < 2048) return fn(0, n, f);
+    static std::vector<std::vector<double>> bufs;   // one per worker, reused across calls
+    if ((int)bufs.size() < T) bufs.resize(T);
+    std::vector<int> st(T, 0), lo(T, 0), hi(T, 0);
+#pragma omp parallel for num_threads(T) schedule(static, 1)
+    for (int t = 0; t < T; ++t) {
+        const int b = (int)((long long)n * t / T), e = (int)((long long)n * (t + 1) / T);
+        int l = nvar, h = 0;
+        for (long long k = (long long)stride * b; k < (long long)stride * e; ++k) {
+            l = std::min(l, bs[k]);
+            h = std::max(h, bs[k] + 3);
+        }
+        if (l >= h) { lo[t] = hi[t] = 0; continue; }
+        lo[t] = l;
+        hi[t] = h;
+        auto& B = bufs[t];
+        if ((int)B.size() < nvar) B.resize(nvar);
+        std::fill(B.begin() + l, B.begin() + h, 0.0);
+        st[t] = fn(b, e - b, B.data());
+    }
+#pragma omp parallel for num_threads(T) schedule(static)
+    for (int i = 0; i < nvar; ++i) {
+        double v = f[i];
+        for (int t = 0; t < T; ++t)
+            if (i >= lo[t] && i < hi[t]) v += bufs[t][i];
+        f[i] = v;
+    }
+    int r = 0;
+    for (int t = 0; t < T; ++t) {
+        if (st[t] < 0) return -1;
+        r += st[t];
+    }
+    return r;
+}
+
+extern "C" {
+
 static double ff_energy(const OrcSystem* s, int which, const double* x) {
     switch (which) {
-        case FF_STRETCH: return orc_stretch_energy(x, s->n_stretch, s->st_bs, s->st_k, s->st_l0);
-        case FF_BEND: return orc_bend_energy(x, s->n_bend, s->bd_bs, s->bd_k, s->bd_t0);
-        case FF_LINKER: return orc_bond_energy(x, s->n_linker, s->lk_bs, s->lk_k, s->lk_l0, s->lk_s1, s->lk_s2);
-        case FF_MOTOR: return orc_bond_energy(x, s->n_motor, s->mt_bs, s->mt_k, s->mt_l0, s->mt_s1, s->mt_s2);
-        case FF_EXVOL: return orc_exvol_energy(x, s->n_exvol, s->ev_bs, s->ev_k, s->ev_len);
+        case FF_STRETCH:
+            return chunked_energy(s->n_stretch, [&](int b, int c) {
+                return orc_stretch_energy(x, c, s->st_bs + 2 * b, s->st_k + b, s->st_l0 + b);
+            });
+        case FF_BEND:
+            return chunked_energy(s->n_bend, [&](int b, int c) {
+                return orc_bend_energy(x, c, s->bd_bs + 3 * b, s->bd_k + b, s->bd_t0 + b);
+            });
+        case FF_LINKER:
+            return chunked_energy(s->n_linker, [&](int b, int c) {
+                return orc_bond_energy(x, c, s->lk_bs + 4 * b, s->lk_k + b, s->lk_l0 + b, s->lk_s1 + b, s->lk_s2 + b);
+            });
+        case FF_MOTOR:
+            return chunked_energy(s->n_motor, [&](int b, int c) {
+                return orc_bond_energy(x, c, s->mt_bs + 4 * b, s->mt_k + b, s->mt_l0 + b, s->mt_s1 + b, s->mt_s2 + b);
+            });
+        case FF_EXVOL:
+            return chunked_energy(s->n_exvol, [&](int b, int c) {
+                return orc_exvol_energy(x, c, s->ev_bs + 4 * b, s->ev_k + b, s->ev_len + 2 * b);
+            });
         case FF_BOUNDARY: return orc_boundary_energy(x, s->n_planes, s->planes, s->bd_nn, s->bb_bs, s->bb_k, s->bb_slen);
     }
     return 0.0;
@@ -773,11 +859,50 @@ double orc_system_energies(const OrcSystem* s, const double* x, double* per_ff) 
 // computeForces: zero-fill then every FF accumulates, in order.
 int orc_system_forces(const OrcSystem* s, const double* x, double* f, int nvar, double* lk_sf, double* mt_sf) {
     std::fill(f, f + nvar, 0.0);
-    orc_stretch_forces(x, f, s->n_stretch, s->st_bs, s->st_k, s->st_l0);
-    orc_bend_forces(x, f, s->n_bend, s->bd_bs, s->bd_k, s->bd_t0);
+    if (g_threads <= 1) {
+        orc_stretch_forces(x, f, s->n_stretch, s->st_bs, s->st_k, s->st_l0);
+        orc_bend_forces(x, f, s->n_bend, s->bd_bs, s->bd_k, s->bd_t0);
+        orc_bond_forces(x, f, s->n_linker, s->lk_bs, s->lk_k, s->lk_l0, s->lk_s1, s->lk_s2, lk_sf);
+        orc_bond_forces(x, f, s->n_motor, s->mt_bs, s->mt_k, s->mt_l0, s->mt_s1, s->mt_s2, mt_sf);
+        const int r = orc_exvol_forces(x, f, s->n_exvol, s->ev_bs, s->ev_k, s->ev_len);
+        orc_boundary_forces(x, f, s->n_planes, s->planes, s->bd_nn, s->bb_bs, s->bb_k, s->bb_slen);
+        return r;
+    }
+    chunked_forces(s->n_stretch, 2, s->st_bs, f, nvar, [&](int b, int c, double* F) {
+        orc_stretch_forces(x, F, c, s->st_bs + 2 * b, s->st_k + b, s->st_l0 + b);
+        return 0;
+    });
+    chunked_forces(s->n_bend, 3, s->bd_bs, f, nvar, [&](int b, int c, double* F) {
+        orc_bend_forces(x, F, c, s->bd_bs + 3 * b, s->bd_k + b, s->bd_t0 + b);
+        return 0;
+    });
+    // linkers and motors touch beads all over the network: serial (a few ms)
     orc_bond_forces(x, f, s->n_linker, s->lk_bs, s->lk_k, s->lk_l0, s->lk_s1, s->lk_s2, lk_sf);
     orc_bond_forces(x, f, s->n_motor, s->mt_bs, s->mt_k, s->mt_l0, s->mt_s1, s->mt_s2, mt_sf);
-    const int r = orc_exvol_forces(x, f, s->n_exvol, s->ev_bs, s->ev_k, s->ev_len);
+    // excluded volume: pair contributions in parallel, accumulated in pair order
+    int r = 0;
+    {
+        const int n = s->n_exvol;
+        static std::vector<double> contrib;
+        static std::vector<int> status;
+        contrib.resize(12 * (size_t)n);
+        status.resize(n);
+#pragma omp parallel for num_threads(g_threads) schedule(dynamic, 256)
+        for (int i = 0; i < n; ++i) {
+            const int* q = s->ev_bs + 4 * i;
+            double out[4][3];
+            status[i] = orc_exvol_pair_forces(x + q[0], x + q[1], x + q[2], x + q[3], s->ev_k[i], s->ev_len[2 * i],
+                                              s->ev_len[2 * i + 1], out);
+            std::memcpy(&contrib[12 * (size_t)i], out, sizeof(out));
+        }
+        for (int i = 0; i < n && r >= 0; ++i) {
+            if (status[i] < 0) { r = -1; break; }
+            r += status[i];
+            const int* q = s->ev_bs + 4 * i;
+            for (int a = 0; a < 4; ++a)
+                for (int k = 0; k < 3; ++k) acc(f[q[a] + k], contrib[12 * (size_t)i + 3 * a + k]);
+        }
+    }
     orc_boundary_forces(x, f, s->n_planes, s->planes, s->bd_nn, s->bb_bs, s->bb_k, s->bb_slen);
     return r;
 }
@@ -811,8 +936,19 @@ struct OrcCGResult {
 
 static double vdot(const std::vector<double>& a, const std::vector<double>& b, int n) {
     double r = 0.0;
+    if (g_threads <= 1) {
+        for (int i = 0; i < n; ++i) r += a[i] * b[i];
+        return r;
+    }
+#pragma omp parallel for num_threads(g_threads) schedule(static) reduction(+ : r)
     for (int i = 0; i < n; ++i) r += a[i] * b[i];
     return r;
+}
+
+// y[i] = x[i] + s * d[i] (serial with one thread)
+static void vaxpy(double* y, const double* x, double s, const double* d, int n) {
+#pragma omp parallel for num_threads(g_threads) schedule(static) if (g_threads > 1)
+    for (int i = 0; i < n; ++i) y[i] = x[i] + s * d[i];
 }
 
 int orc_minimize(const OrcSystem* s, const OrcCGParams* prm, double* coord_io, int ndof, int nbeads,
@@ -832,7 +968,18 @@ int orc_minimize(const OrcSystem* s, const OrcCGParams* prm, double* coord_io, i
 
     auto maxF = [&](double& out) {
         double m = 0;
-        for (int i = 0; i < n; ++i) m = std::max(m, std::fabs(f[i]));
+        if (g_threads <= 1) {
+            for (int i = 0; i < n; ++i) m = std::max(m, std::fabs(f[i]));
+        } else {
+            bool nonfinite = false;
+#pragma omp parallel for num_threads(g_threads) schedule(static) reduction(max : m) reduction(|| : nonfinite)
+            for (int i = 0; i < n; ++i) {
+                const double a = std::fabs(f[i]);
+                if (!(a <= std::numeric_limits<double>::max())) nonfinite = true;
+                else m = std::max(m, a);
+            }
+            if (nonfinite) m = std::numeric_limits<double>::infinity();
+        }
         out = m;
         return std::isfinite(m);
     };
@@ -874,7 +1021,7 @@ int orc_minimize(const OrcSystem* s, const OrcCGParams* prm, double* coord_io, i
                 bool done = false;
                 double Elam = 0.0;
                 while (!done) {
-                    for (int i = 0; i < n; ++i) xt[i] = x[i] + lambda * d[i];
+                    vaxpy(xt.data(), x.data(), lambda, d.data(), n);
                     Elam = orc_system_energy(s, xt.data());
                     ++res->numEnergyCall;
                     ++res->numLineSearchTrials;
@@ -914,7 +1061,7 @@ int orc_minimize(const OrcSystem* s, const OrcCGParams* prm, double* coord_io, i
             }
             continue;
         }
-        for (int i = 0; i < n; ++i) x[i] += lambda * d[i];
+        vaxpy(x.data(), x.data(), lambda, d.data(), n);
         orc_system_forces(s, x.data(), f.data(), n, nullptr, nullptr);
         ++res->numForceCall;
         if (!maxF(res->gradInfNorm)) { res->status = 1; break; }
@@ -926,7 +1073,7 @@ int orc_minimize(const OrcSystem* s, const OrcCGParams* prm, double* coord_io, i
         else if (prm->method == 2) { newGrad = vdot(f, f, n); prevGrad = vdot(f, fprev, n); }
         if (prm->method == 1) beta = newGrad / lastFdotF;
         else if (prm->method == 2) beta = std::max(0.0, (newGrad - prevGrad) / lastFdotF);
-        for (int i = 0; i < n; ++i) d[i] = f[i] + beta * d[i];
+        vaxpy(d.data(), f.data(), beta, d.data(), n);
         if (vdot(d, f, n) <= 0) resetCG();
         if (prm->method == 2) fprev = f;
 
@@ -1048,6 +1195,8 @@ int orc_minimize_quadratic(int n, const double* w, const double* o, const OrcCGP
 }
 
 int orc_version(void) { return 1; }
+void orc_set_threads(int n) { g_threads = n < 1 ? 1 : n; }
+int orc_get_threads(void) { return g_threads; }
 
 // Arctangent used by the excluded-volume formula: 0 = the C library's atan
 // (the reference's), 1 = series_atan above (rounds identically on the GPU).

@@ -119,6 +119,8 @@ def lib():
             L.orc_series_atan.restype = C.c_double
             L.orc_series_atan.argtypes = [C.c_double]
             L.orc_system_force_scale.argtypes = [C.POINTER(System), _dp, _dp, C.c_int]
+            L.orc_set_threads.argtypes = [C.c_int]
+            L.orc_get_threads.restype = C.c_int
             _lib = L
     return _lib
 
@@ -341,6 +343,23 @@ class series_atan_mode:
 
     def __exit__(self, *exc):
         lib().orc_set_series_atan(0)
+
+
+class threads:
+    """Context manager: the oracle's force fields and CG vector loops on `n`
+    host threads (OpenMP).  Only for timing the CPU baseline: with more than
+    one thread the sums round differently from the reference's serial order,
+    so parity checks run with the default single thread."""
+    def __init__(self, n: int):
+        self.n = max(1, int(n))
+
+    def __enter__(self):
+        self.prev = lib().orc_get_threads()
+        lib().orc_set_threads(self.n)
+        return self
+
+    def __exit__(self, *exc):
+        lib().orc_set_threads(self.prev)
 
 
 def cg_params(method=2, maxDist=1.0, lambdaMax=0.01, gradTol=1.0, energyRelTol=1e-9, energyCallLimit=0,

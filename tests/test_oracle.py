@@ -304,3 +304,24 @@ def test_force_scale_bounds_forces():
     f = oracle.forces(v, net.coord)
     s = oracle.force_scale(v, net.coord)
     assert np.all(np.abs(f) <= s * (1 + 1e-12) + 1e-12)
+
+
+def test_threaded_oracle_agrees_with_serial():
+    """The all-cores CPU baseline computes the same energies, forces and CG run
+    as the serial oracle, up to summation order."""
+    net = jitter(make_network("c1"), 0.5, seed=3)
+    vec = oracle.vectorize(net)
+    e1, p1 = oracle.energies(vec, net.coord)
+    f1 = oracle.forces(vec, net.coord)
+    x1, _, r1 = oracle.minimize(vec, net.coord, oracle.cg_params(energyCallLimit=60))
+    with oracle.threads(4):
+        e4, p4 = oracle.energies(vec, net.coord)
+        f4 = oracle.forces(vec, net.coord)
+        x4, _, r4 = oracle.minimize(vec, net.coord, oracle.cg_params(energyCallLimit=60))
+    assert oracle.lib().orc_get_threads() == 1
+    assert np.all(np.abs(p4 - p1) <= 1e-12 * np.abs(p1) + 1e-12)
+    scale = oracle.force_scale(vec, net.coord)
+    assert np.all(np.abs(f4 - f1) <= 1e-12 * scale + 1e-12)
+    # same line-search branches for the first iterations: same call counts, nearly the same positions
+    assert r4.numEnergyCall == r1.numEnergyCall and r4.numForceCall == r1.numForceCall
+    assert np.abs(x4 - x1).max() < 1e-6
