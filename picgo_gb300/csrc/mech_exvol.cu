@@ -12,9 +12,9 @@
 // accuracy as the normalized triple product q = |(v12 x v34) . v31| /
 // (|v12| |v34| |v31|) goes to zero (nearly coplanar or nearly touching
 // segments), so pairs with q under a threshold are evaluated in FP64 by a
-// second pass over a compacted list.  Nearly coplanar pairs, the only ones the
-// reference moves off their plane (|n . v3| < 0.1 implies a small q), are then
-// always decided and moved in FP64.
+// second pass over a compacted list.  The reference's coplanarity move (forces
+// only) is decided and applied in single precision, except for pairs whose
+// test lies within rounding of its threshold, which go to the FP64 pass.
 #include <cuda_runtime.h>
 
 #include "mech_device.cuh"
@@ -211,12 +211,36 @@ __device__ __forceinline__ void push_c1(const double* c1, const double* c2, cons
 
 // Analytic forces (:597-860) from the invariants and v1 = c2 - c1,
 // v2 = c4 - c3, v3 = c1 - c3; returns false when a component is not finite.
-template <typename T>
+// Fast = false divides exactly as the reference writes it (the FP64 engine's
+// parity); Fast = true multiplies by the four reciprocals 1/AA, 1/EE, 1/BB,
+// 1/FF instead (13 divisions per pair instead of 51; within an ulp or two of
+// each quotient, for the mixed engine).
+template <bool Fast, typename T>
 __device__ bool forces_from(const PairInv<T>& p, const T* v1, const T* v2, const T* v3, T kRepScaled, T out[4][3]) {
     const T a = p.a, b = p.b, c = p.c, d = p.d, e = p.e, F = p.F;
     const T AA = p.AA, BB = p.BB, CC = p.CC, DD = p.DD, EE = p.EE, FF = p.FF, GG = p.GG, HH = p.HH;
+    T rA = 0, rE = 0, rB = 0, rF = 0;
+    if constexpr (Fast) {
+        rA = (T)1 / AA;
+        rE = (T)1 / EE;
+        rB = (T)1 / BB;
+        rF = (T)1 / FF;
+    }
+    // x / Y, x / Y^2, x / Y^3 for Y in {AA, EE, BB, FF}
+    auto q1 = [](T x, T Y, T rY) -> T {
+        if constexpr (Fast) return x * rY;
+        else return x / Y;
+    };
+    auto q2 = [](T x, T Y, T rY) -> T {
+        if constexpr (Fast) return x * (rY * rY);
+        else return x / (Y * Y);
+    };
+    auto q3 = [](T x, T Y, T rY) -> T {
+        if constexpr (Fast) return x * (rY * rY * rY);
+        else return x / (Y * Y * Y);
+    };
     const T invJJ = (T)1 / p.JJ;
-    const T S = CC / AA * p.ATG1 + GG / EE * p.ATG2 + DD / BB * p.ATG3 + HH / FF * p.ATG4;
+    const T S = q1(CC, AA, rA) * p.ATG1 + q1(GG, EE, rE) * p.ATG2 + q1(DD, BB, rB) * p.ATG3 + q1(HH, FF, rF) * p.ATG4;
     const T pref = kRepScaled * invJJ / (T)2;
     const T A1 = AA * AA / (AA * AA + (a + e) * (a + e));
     const T A2 = AA * AA / (AA * AA + e * e);
@@ -227,37 +251,37 @@ __device__ bool forces_from(const PairInv<T>& p, const T* v1, const T* v2, const
     const T F1 = FF * FF / (FF * FF + (d + F) * (d + F));
     const T F2 = FF * FF / (FF * FF + (d + F - b) * (d + F - b));
     // partials of the four terms of S in their own arguments
-    const T tA_C = p.ATG1 / AA;
-    const T tA_X = -(p.ATG1 * CC) / (AA * AA) + (-A1 * (a + e) + A2 * e) * CC / (AA * AA * AA);
-    const T tA_e = ((A1 - A2) * CC) / (AA * AA);
-    const T tA_a = (A1 * CC) / (AA * AA);
-    const T tE_G = p.ATG2 / EE;
-    const T tE_X = -(p.ATG2 * GG) / (EE * EE) + (-E1 * (a + e - d) + E2 * (e - d)) * GG / (EE * EE * EE);
-    const T tE_em = ((E1 - E2) * GG) / (EE * EE);
-    const T tE_a = (E1 * GG) / (EE * EE);
-    const T tB_D = p.ATG3 / BB;
-    const T tB_X = -(p.ATG3 * DD) / (BB * BB) + (-B1 * F + B2 * (F - b)) * DD / (BB * BB * BB);
-    const T tB_fm = ((B1 - B2) * DD) / (BB * BB);
-    const T tB_b = (B1 * DD) / (BB * BB);
-    const T tF_H = p.ATG4 / FF;
-    const T tF_X = -(p.ATG4 * HH) / (FF * FF) + (-F1 * (d + F) + F2 * (d + F - b)) * HH / (FF * FF * FF);
-    const T tF_dfm = ((F1 - F2) * HH) / (FF * FF);
-    const T tF_b = (F1 * HH) / (FF * FF);
+    const T tA_C = q1(p.ATG1, AA, rA);
+    const T tA_X = q2(-(p.ATG1 * CC), AA, rA) + q3((-A1 * (a + e) + A2 * e) * CC, AA, rA);
+    const T tA_e = q2((A1 - A2) * CC, AA, rA);
+    const T tA_a = q2(A1 * CC, AA, rA);
+    const T tE_G = q1(p.ATG2, EE, rE);
+    const T tE_X = q2(-(p.ATG2 * GG), EE, rE) + q3((-E1 * (a + e - d) + E2 * (e - d)) * GG, EE, rE);
+    const T tE_em = q2((E1 - E2) * GG, EE, rE);
+    const T tE_a = q2(E1 * GG, EE, rE);
+    const T tB_D = q1(p.ATG3, BB, rB);
+    const T tB_X = q2(-(p.ATG3 * DD), BB, rB) + q3((-B1 * F + B2 * (F - b)) * DD, BB, rB);
+    const T tB_fm = q2((B1 - B2) * DD, BB, rB);
+    const T tB_b = q2(B1 * DD, BB, rB);
+    const T tF_H = q1(p.ATG4, FF, rF);
+    const T tF_X = q2(-(p.ATG4 * HH), FF, rF) + q3((-F1 * (d + F) + F2 * (d + F - b)) * HH, FF, rF);
+    const T tF_dfm = q2((F1 - F2) * HH, FF, rF);
+    const T tF_b = q2(F1 * HH, FF, rF);
     T G[3][3];
-    G[0][0] = tA_C * (-2 * F) + tA_X * (c / AA) + tA_a * 2 + tE_G * (2 * (F - b)) + tE_X * ((b + c - 2 * F) / EE) +
-              tE_a * 2 + tF_H * (-2 * b) + tF_X * (b / FF);
-    G[0][1] = tA_C * e + tE_G * (2 * d - e) + tE_X * ((e - d) / EE) + tE_em * (-1) + tB_D * (-F) + tF_H * (2 * d + F) +
-              tF_X * (-(d + F) / FF) + tF_dfm;
-    G[0][2] = tA_C * d + tA_X * (-e / AA) + tA_e + tE_G * (-d) + tE_X * (-(e - d) / EE) + tE_em + tB_D * b +
-              tF_H * (-b) + tF_X * (b / FF);
+    G[0][0] = tA_C * (-2 * F) + tA_X * q1(c, AA, rA) + tA_a * 2 + tE_G * (2 * (F - b)) + tE_X * q1(b + c - 2 * F, EE, rE) +
+              tE_a * 2 + tF_H * (-2 * b) + tF_X * q1(b, FF, rF);
+    G[0][1] = tA_C * e + tE_G * (2 * d - e) + tE_X * q1(e - d, EE, rE) + tE_em * (-1) + tB_D * (-F) + tF_H * (2 * d + F) +
+              tF_X * q1(-(d + F), FF, rF) + tF_dfm;
+    G[0][2] = tA_C * d + tA_X * q1(-e, AA, rA) + tA_e + tE_G * (-d) + tE_X * q1(-(e - d), EE, rE) + tE_em + tB_D * b +
+              tF_H * (-b) + tF_X * q1(b, FF, rF);
     G[1][0] = G[0][1];
-    G[1][1] = tE_G * (-2 * a) + tE_X * (a / EE) + tB_D * (2 * e) + tB_X * (c / BB) + tB_fm * (-2) + tB_b * 2 +
-              tF_H * (-2 * (a + e)) + tF_X * ((a + c + 2 * e) / FF) + tF_dfm * (-2) + tF_b * 2;
-    G[1][2] = tA_C * (-a) + tE_G * a + tE_X * (-a / EE) + tB_D * (-d) + tB_X * (-F / BB) + tB_fm + tF_H * d +
-              tF_X * (-(d + F) / FF) + tF_dfm;
+    G[1][1] = tE_G * (-2 * a) + tE_X * q1(a, EE, rE) + tB_D * (2 * e) + tB_X * q1(c, BB, rB) + tB_fm * (-2) + tB_b * 2 +
+              tF_H * (-2 * (a + e)) + tF_X * q1(a + c + 2 * e, FF, rF) + tF_dfm * (-2) + tF_b * 2;
+    G[1][2] = tA_C * (-a) + tE_G * a + tE_X * q1(-a, EE, rE) + tB_D * (-d) + tB_X * q1(-F, BB, rB) + tB_fm + tF_H * d +
+              tF_X * q1(-(d + F), FF, rF) + tF_dfm;
     G[2][0] = G[0][2];
     G[2][1] = G[1][2];
-    G[2][2] = tA_X * (a / AA) + tE_X * (a / EE) + tB_X * (b / BB) + tF_X * (b / FF);
+    G[2][2] = tA_X * q1(a, AA, rA) + tE_X * q1(a, EE, rE) + tB_X * q1(b, BB, rB) + tF_X * q1(b, FF, rF);
     T J[3][3];
     J[0][0] = 2 * (-b * c + F * F);
     J[0][1] = 2 * (c * d - e * F);
@@ -301,7 +325,7 @@ static __device__ bool pair_forces_d(const double* c1, const double* c2in, const
     diffs_of(c1, c2, c3, c4, v12, v34, v31, v14, v32, v24);
     PairInv<double> p;
     pair_inv(v12, v34, v31, v14, v32, v24, p, !ref);
-    return forces_from(p, v12, v34, v31, kRep, out);
+    return ref ? forces_from<false>(p, v12, v34, v31, kRep, out) : forces_from<true>(p, v12, v34, v31, kRep, out);
 }
 
 // ---------------------------------------------------------------------------
@@ -429,9 +453,10 @@ __global__ void __launch_bounds__(kBlock) k_exvol_fb_force(DevNet<Real> n, doubl
                 for (int a = 0; a < 4; ++a)
                     for (int kk = 0; kk < 3; ++kk) out[a][kk] = __longlong_as_double(0x7ff8000000000000ULL);
             }
-            Real* cdst = n.contrib + 3 * (size_t)(n.slot_base[K_EXVOL] + 4 * pr);
-            for (int a = 0; a < 4; ++a)
-                for (int kk = 0; kk < 3; ++kk) cdst[3 * a + kk] = (Real)out[a][kk];
+            for (int a = 0; a < 4; ++a) {
+                Real* cdst = slot_ptr(n, n.slot_base[K_EXVOL] + 4 * pr + a);
+                for (int kk = 0; kk < 3; ++kk) cdst[kk] = (Real)out[a][kk];
+            }
         }
         __syncthreads();
     }
@@ -516,9 +541,10 @@ __global__ void __launch_bounds__(kBlock) k_exvol(DevNet<Real> n, int want, int 
             } else {
                 double out[4][3];
                 const bool ok = pair_forces_d(c1, c2, c3, c4, kRepD, out);
-                Real* cdst = n.contrib + 3 * (size_t)(n.slot_base[K_EXVOL] + 4 * i);
-                for (int a = 0; a < 4; ++a)
-                    for (int k = 0; k < 3; ++k) cdst[3 * a + k] = (Real)out[a][k];
+                for (int a = 0; a < 4; ++a) {
+                    Real* cdst = slot_ptr(n, n.slot_base[K_EXVOL] + 4 * i + a);
+                    for (int k = 0; k < 3; ++k) cdst[k] = (Real)out[a][k];
+                }
                 if (!ok) flag_fallback(n, r, i, 0.0);
             }
         } else {
@@ -536,14 +562,24 @@ __global__ void __launch_bounds__(kBlock) k_exvol(DevNet<Real> n, int want, int 
             const float q = trip / (sqrtf(dot3(v12, v12)) * sqrtf(dot3(v34, v34)) * sqrtf(dot3(v31, v31)));
             need64 = !(q >= (force ? kMixedTauForce : kMixedTauEnergy));
             if (force && !need64) {
-                // the reference moves c2 off the plane of a pair it judges coplanar
-                // (|n . v3| < 0.1 with n = (c2-c1) x (c3-c1), v3 = c4 - c1); such
-                // pairs, with a margin for single-precision rounding, go to FP64
+                // the reference moves c2 0.01 nm along the unit normal of (c1, c2, c3)
+                // when it judges the pair coplanar (|n . v3| < 0.1 with
+                // n = (c2-c1) x (c3-c1), v3 = c4 - c1; :610-626).  Pairs whose test
+                // single precision cannot decide go to FP64; the others are moved
+                // here (with q >= kMixedTauForce the move leaves them well conditioned).
                 const float nx = v12[1] * v31[2] - v12[2] * v31[1], ny = v12[2] * v31[0] - v12[0] * v31[2],
-                            nz = v12[0] * v31[1] - v12[1] * v31[0];
-                const float cop = fabsf(nx * v14[0] + ny * v14[1] + nz * v14[2]) /
-                                  (sqrtf(nx * nx + ny * ny + nz * nz) * sqrtf(dot3(v14, v14)));
-                need64 = !(cop >= 0.1f + 2e-3f);
+                            nz = v12[0] * v31[1] - v12[1] * v31[0];   // = -n
+                const float nn = sqrtf(nx * nx + ny * ny + nz * nz);
+                const float cop = fabsf(nx * v14[0] + ny * v14[1] + nz * v14[2]) / (nn * sqrtf(dot3(v14, v14)));
+                if (!(fabsf(cop - 0.1f) >= 2e-3f)) {
+                    need64 = true;
+                } else if (cop < 0.1f) {
+                    const float s = -0.01f / nn;
+                    const float dx = s * nx, dy = s * ny, dz = s * nz;   // c2 moves by +0.01 n / |n|
+                    v12[0] += dx; v12[1] += dy; v12[2] += dz;
+                    v32[0] += dx; v32[1] += dy; v32[2] += dz;
+                    v24[0] -= dx; v24[1] -= dy; v24[2] -= dz;
+                }
             }
             if (!need64) {
                 PairInv<float> pi;
@@ -554,10 +590,11 @@ __global__ void __launch_bounds__(kBlock) k_exvol(DevNet<Real> n, int want, int 
                     else e = u;
                 } else {
                     float out[4][3];
-                    if (forces_from(pi, v12, v34, v31, (float)kRepD, out)) {
-                        Real* cdst = n.contrib + 3 * (size_t)(n.slot_base[K_EXVOL] + 4 * i);
-                        for (int a = 0; a < 4; ++a)
-                            for (int k = 0; k < 3; ++k) cdst[3 * a + k] = (Real)out[a][k];
+                    if (forces_from<true>(pi, v12, v34, v31, (float)kRepD, out)) {
+                        for (int a = 0; a < 4; ++a) {
+                            Real* cdst = slot_ptr(n, n.slot_base[K_EXVOL] + 4 * i + a);
+                            for (int k = 0; k < 3; ++k) cdst[k] = (Real)out[a][k];
+                        }
                     } else {
                         need64 = true;
                     }
@@ -601,9 +638,10 @@ __global__ void __launch_bounds__(128) k_exvol_fp64(DevNet<Real> n, int trial, i
         } else {
             double out[4][3];
             const bool ok = pair_forces_d(c1, c2, c3, c4, kRepD, out, false);
-            Real* cdst = n.contrib + 3 * (size_t)(n.slot_base[K_EXVOL] + 4 * i);
-            for (int a = 0; a < 4; ++a)
-                for (int q = 0; q < 3; ++q) cdst[3 * a + q] = (Real)out[a][q];
+            for (int a = 0; a < 4; ++a) {
+                Real* cdst = slot_ptr(n, n.slot_base[K_EXVOL] + 4 * i + a);
+                for (int q = 0; q < 3; ++q) cdst[q] = (Real)out[a][q];
+            }
             if (!ok) flag_fallback(n, r, i, 0.0);
         }
     }

@@ -338,10 +338,9 @@ __global__ void __launch_bounds__(kBlock) k_fil_force(DevNet<Real> n, int want) 
             }
             const int c0 = n.csr_off[b], c1 = n.csr_off[b + 1];
             for (int c = c0; c < c1; ++c) {
-                const int sl = n.csr_slot[c];
-                F[0] += n.contrib[3 * (size_t)sl];
-                F[1] += n.contrib[3 * (size_t)sl + 1];
-                F[2] += n.contrib[3 * (size_t)sl + 2];
+                F[0] += n.contrib[3 * (size_t)c];
+                F[1] += n.contrib[3 * (size_t)c + 1];
+                F[2] += n.contrib[3 * (size_t)c + 2];
             }
             Real* Fo = n.f[s_fb ^ 1] + 3 * (size_t)b;
             const Real* Fp = n.f[s_fb] + 3 * (size_t)b;
@@ -434,18 +433,20 @@ __global__ void __launch_bounds__(kBlock) k_fil_energy_mx(DevNet<float> n, int w
         const int b = t.begin + threadIdx.x;
         if (b < t.end) {
             const float* X = n.x[xb];
+            // every load is issued up front (neighbours clamped to the bead
+            // range, unused at filament ends) so none waits on the flags
             const int fl = n.bflag[b];
             const Pos<float> p0 = pos_at(n, X, b, tr, lf);
+            const Pos<float> pp = pos_at(n, X, min(b + 1, n.nb - 1), tr, lf);
+            const Pos<float> pm = pos_at(n, X, max(b - 1, 0), tr, lf);
+            float ks, l0, kb, th;
+            load_par(n.bpar, b, ks, l0, kb, th);
             if (tr) store_pos(n.x[xb ^ 1], b, p0);   // materialize the owned trial position
             if (fl & 1) {
-                float ks, l0, kb, th;
-                load_par(n.bpar, b, ks, l0, kb, th);
-                const Pos<float> pp = pos_at(n, X, b + 1, tr, lf);
                 float r2[3];
                 pdiff(pp, p0, r2);
                 es.add(stretch_energy<float>(r2[0], r2[1], r2[2], ks, l0));
                 if (fl & 2) {
-                    const Pos<float> pm = pos_at(n, X, b - 1, tr, lf);
                     float r1[3];
                     pdiff(p0, pm, r1);
                     eb.add(bend_energy<float>(r1, r2, kb, th));
@@ -491,19 +492,21 @@ __global__ void __launch_bounds__(kBlock) k_fil_force_mx(DevNet<float> n, int wa
         const int b = t.begin + threadIdx.x;
         if (b < t.end) {
             const float* X = n.x[xb];
-            const int f0 = n.bflag[b];
-            const int fm = (f0 & 2) ? n.bflag[b - 1] : 0;
-            const int fp = (f0 & 1) ? n.bflag[b + 1] : 0;
+            // every load is issued up front (neighbours clamped to the bead
+            // range, unused at filament ends) so none waits on the flags
+            const int bm1 = max(b - 1, 0), bm2 = max(b - 2, 0), bp1 = min(b + 1, n.nb - 1), bp2 = min(b + 2, n.nb - 1);
+            const int f0 = n.bflag[b], fm_raw = n.bflag[bm1], fp_raw = n.bflag[bp1];
+            const int fm = (f0 & 2) ? fm_raw : 0;
+            const int fp = (f0 & 1) ? fp_raw : 0;
             const Pos<float> p0 = load_pos(X, b);
-            Pos<float> pm1 = p0, pp1 = p0, pm2 = p0, pp2 = p0;
-            if (f0 & 2) pm1 = load_pos(X, b - 1);
-            if (f0 & 1) pp1 = load_pos(X, b + 1);
-            if (fm & 2) pm2 = load_pos(X, b - 2);
-            if (fp & 1) pp2 = load_pos(X, b + 2);
+            const Pos<float> pm1 = load_pos(X, bm1), pp1 = load_pos(X, bp1);
+            const Pos<float> pm2 = load_pos(X, bm2), pp2 = load_pos(X, bp2);
+            const int c0 = n.csr_off[b], c1 = n.csr_off[b + 1];
+            float ksm, l0m, kbm, thm, ks, l0, kb, th, ksp, l0p, kbp, thp;
+            load_par(n.bpar, bm1, ksm, l0m, kbm, thm);
+            load_par(n.bpar, b, ks, l0, kb, th);
+            load_par(n.bpar, bp1, ksp, l0p, kbp, thp);
             float F[3] = {0.f, 0.f, 0.f};
-            float ksm = 0, l0m = 0, kbm = 0, thm = 0, ks = 0, l0 = 0, kb = 0, th = 0;
-            if (f0 & 2) load_par(n.bpar, b - 1, ksm, l0m, kbm, thm);
-            if (f0 & 1) load_par(n.bpar, b, ks, l0, kb, th);
             float rm[3] = {0, 0, 0}, rp[3] = {0, 0, 0};
             if (f0 & 2) pdiff(p0, pm1, rm);
             if (f0 & 1) pdiff(pp1, p0, rp);
@@ -531,18 +534,15 @@ __global__ void __launch_bounds__(kBlock) k_fil_force_mx(DevNet<float> n, int wa
                 F[0] += a1[0] - a2[0]; F[1] += a1[1] - a2[1]; F[2] += a1[2] - a2[2];
             }
             if ((f0 & 1) && (fp & 1)) {
-                float ksp, l0p, kbp, thp, r2[3], a1[3], a2[3];
-                load_par(n.bpar, b + 1, ksp, l0p, kbp, thp);
+                float r2[3], a1[3], a2[3];
                 pdiff(pp2, pp1, r2);
                 bend_force<float>(rp, r2, kbp, thp, a1, a2);
                 F[0] += -a1[0]; F[1] += -a1[1]; F[2] += -a1[2];
             }
-            const int c0 = n.csr_off[b], c1 = n.csr_off[b + 1];
             for (int c = c0; c < c1; ++c) {
-                const int sl = n.csr_slot[c];
-                F[0] += n.contrib[3 * (size_t)sl];
-                F[1] += n.contrib[3 * (size_t)sl + 1];
-                F[2] += n.contrib[3 * (size_t)sl + 2];
+                F[0] += n.contrib[3 * (size_t)c];
+                F[1] += n.contrib[3 * (size_t)c + 1];
+                F[2] += n.contrib[3 * (size_t)c + 2];
             }
             float* Fo = n.f[fb ^ 1] + 3 * (size_t)b;
             const float* Fp = n.f[fb] + 3 * (size_t)b;
@@ -677,7 +677,7 @@ __global__ void __launch_bounds__(kBlock) k_bond_bnd(DevNet<Real> n, int want, i
                 e = K * ex;
             } else {
                 const Real f0 = K * ex / sl;
-                Real* c = n.contrib + 3 * (size_t)(n.slot_base[K_BOUNDARY] + i);
+                Real* c = slot_ptr(n, n.slot_base[K_BOUNDARY] + i);
                 c[0] = f0 * (Real)pl[0];
                 c[1] = f0 * (Real)pl[1];
                 c[2] = f0 * (Real)pl[2];
@@ -702,13 +702,17 @@ __global__ void __launch_bounds__(kBlock) k_bond_bnd(DevNet<Real> n, int want, i
                 const Real invL = (Real)1 / dist;
                 const Real f0 = k * (dist - l0) * invL;
                 const Real Fl[3] = {-f0 * lx, -f0 * ly, -f0 * lz};
-                Real* c = n.contrib + 3 * (size_t)(n.slot_base[kind] + 4 * i);
+                const int sb = n.slot_base[kind] + 4 * i;
+                Real* ca = slot_ptr(n, sb);
+                Real* cb = slot_ptr(n, sb + 1);
+                Real* cc = slot_ptr(n, sb + 2);
+                Real* cd = slot_ptr(n, sb + 3);
 #pragma unroll
                 for (int q = 0; q < 3; ++q) {
-                    c[q] = -Fl[q] * ((Real)1 - s1);
-                    c[3 + q] = -Fl[q] * (s1);
-                    c[6 + q] = Fl[q] * ((Real)1 - s2);
-                    c[9 + q] = Fl[q] * (s2);
+                    ca[q] = -Fl[q] * ((Real)1 - s1);
+                    cb[q] = -Fl[q] * (s1);
+                    cc[q] = Fl[q] * ((Real)1 - s2);
+                    cd[q] = Fl[q] * (s2);
                 }
                 (lk ? n.lk_sf : n.mt_sf)[i] = (double)(f0 / invL);
             }

@@ -163,7 +163,7 @@ DevNet<Real> make_devnet(MechContext* c) {
     n.contrib = c->contrib.as<Real>();
     for (int k = 0; k <= K_NUM_SPARSE; ++k) n.slot_base[k] = c->slot_base[k];
     n.csr_off = c->cb.off.as<int>();
-    n.csr_slot = c->cb.slots.as<int>();
+    n.slot_pos = c->cb.pos.as<int>();
     n.lk_sf = c->lk_sf.as<double>();
     n.mt_sf = c->mt_sf.as<double>();
     n.ev_fb_count = c->ev_fb_count.as<int>();

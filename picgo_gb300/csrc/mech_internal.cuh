@@ -129,10 +129,10 @@ struct DevNet {
     const int* stile_kind;
     int sp_tiles[K_NUM_SPARSE];   // tiles per kind
     // contributions and gather index
-    Real* contrib;          // [3 * n_slots]
+    Real* contrib;          // [3 * n_slots] in bead order: bead b's are [csr_off[b], csr_off[b+1])
     int slot_base[K_NUM_SPARSE + 1];
     const int* csr_off;     // [nb + 1]
-    const int* csr_slot;
+    const int* slot_pos;    // slot (interaction-major) -> its position in contrib
     // stretch forces of linkers / motors (assignforcemags)
     double* lk_sf; double* mt_sf;
     // exvol numeric fallback list: count, (replica, pair) entries, energies
@@ -152,6 +152,14 @@ struct DevNet {
     int* gticket;           // whole-grid ticket
     unsigned* err;          // device error word
 };
+
+#ifdef __CUDACC__
+// Where the contribution of slot `slot` (= slot_base[kind] + interaction * beads + bead) is written.
+template <typename Real>
+__device__ __forceinline__ Real* slot_ptr(const DevNet<Real>& n, int slot) {
+    return n.contrib + 3 * (size_t)__ldg(n.slot_pos + slot);
+}
+#endif
 
 // ---- kernels (mech_ff.cu) -------------------------------------------------
 // mode: 0 = line-search trial at x + lambda d (replicas in PH_LS_TRIAL),

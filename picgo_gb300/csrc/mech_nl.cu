@@ -387,6 +387,15 @@ __global__ void k_csr_sort(int nb, const int* off, int* slots) {
     }
 }
 
+// Position of every slot in the bead-ordered CSR sequence: the sparse force
+// kernels write each contribution there, so a bead's contributions are
+// contiguous, in the CSR order, for the filament force kernels to read.
+__global__ void k_csr_inverse(int ns, const int* slots, int* pos) {
+    const int c = blockIdx.x * blockDim.x + threadIdx.x;
+    if (c >= ns) return;
+    pos[slots[c]] = c;
+}
+
 cudaError_t build_csr(const CsrInput& in, CsrBuild& cb, cudaStream_t s) {
     cudaError_t e;
     const int ns = in.base[4];
@@ -394,6 +403,7 @@ cudaError_t build_csr(const CsrInput& in, CsrBuild& cb, cudaStream_t s) {
     if ((e = cb.cursor.ensure(sizeof(int) * (size_t)(in.nb + 1))) != cudaSuccess) return e;
     if ((e = cb.off.ensure(sizeof(int) * (size_t)(in.nb + 1))) != cudaSuccess) return e;
     if ((e = cb.slots.ensure(sizeof(int) * (size_t)(ns > 0 ? ns : 1))) != cudaSuccess) return e;
+    if ((e = cb.pos.ensure(sizeof(int) * (size_t)(ns > 0 ? ns : 1))) != cudaSuccess) return e;
     cudaMemsetAsync(cb.cnt.p, 0, sizeof(int) * (size_t)(in.nb + 1), s);
     cudaMemsetAsync(cb.cursor.p, 0, sizeof(int) * (size_t)(in.nb + 1), s);
     const int tb = 256;
@@ -402,6 +412,7 @@ cudaError_t build_csr(const CsrInput& in, CsrBuild& cb, cudaStream_t s) {
     if (ns > 0) {
         k_csr_fill<<<(ns + tb - 1) / tb, tb, 0, s>>>(in, cb.off.as<int>(), cb.cursor.as<int>(), cb.slots.as<int>());
         k_csr_sort<<<(in.nb + tb - 1) / tb, tb, 0, s>>>(in.nb, cb.off.as<int>(), cb.slots.as<int>());
+        k_csr_inverse<<<(ns + tb - 1) / tb, tb, 0, s>>>(ns, cb.slots.as<int>(), cb.pos.as<int>());
     }
     return cudaGetLastError();
 }

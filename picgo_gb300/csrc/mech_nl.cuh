@@ -59,7 +59,7 @@ struct CsrInput {
 };
 
 struct CsrBuild {
-    DeviceBuffer cnt, cursor, off, slots, scan_tmp;
+    DeviceBuffer cnt, cursor, off, slots, pos, scan_tmp;   // pos: slot -> its CSR position
 };
 
 cudaError_t build_csr(const CsrInput& in, CsrBuild& cb, cudaStream_t s);

@@ -66,10 +66,12 @@ NETS = {
     "small_motors": dict(config="c1", n_filaments=60, n_cyl_per_filament=12, box=1500.0, n_linkers=80, n_motors=40,
                          seed=3),
 }
+# networks for the mixed-precision error checks only (the FP64 checks above cover the formulas)
+MIXED_NETS = [("c1", 0.5), ("small_motors", 1.5), ("c5", 0.5)]
 
 
 def _net(name, sigma=0.0):
-    kw = dict(NETS[name])
+    kw = dict(NETS[name]) if name in NETS else dict(config=name)
     cfg = kw.pop("config")
     net = make_network(cfg, **kw)
     return jitter(net, sigma, seed=7) if sigma else net
@@ -147,8 +149,9 @@ def test_fp64_minimizer_converges_like_oracle():
     assert abs(r["energies_after"][6] - r_o.energiesAfter[6]) <= 2e-2 * abs(r_o.energiesAfter[6])
 
 
-def test_mixed_energy_error_against_fp64():
-    net = _net("c1", 0.5)
+@pytest.mark.parametrize("name,sigma", MIXED_NETS)
+def test_mixed_energy_error_against_fp64(name, sigma):
+    net = _net(name, sigma)
     vec = oracle.vectorize(net)
     o_tot, o_per = oracle.energies(vec, net.coord)
     fo = oracle.forces(vec, net.coord)
