@@ -256,6 +256,97 @@ def fp64_compare(args, net):
             "energy_after": r["energies_after"][6], "warmup_iters": r0["num_iter"]}
 
 
+def c3_report(seed: int = 20261203 + 1):
+    """Mixed precision against the FP64 path on the 200 x 20 network (4,000 cylinders, 500 linkers).
+
+    Both minimize from the same seeded start to max|F| < 1 pN; reported: the
+    relative energy difference of the end states, their max|F|, the bead
+    position RMS / max difference, and the per-evaluation error of the mixed
+    engine at the mixed end state (energy relative, force max abs) against FP64
+    at the same coordinates.  The FP64 path is the one that matches the CPU
+    oracle to 1e-12.
+    """
+    import numpy as np
+    from picgo_gb300 import Engine, make_network
+    net = make_network("c1", seed=seed)
+    out = {"workload": "200 filaments x 20 cylinders (4,000 cylinders), 500 linkers, 2 um box", "seed": seed}
+    ends = {}
+    for prec in ("fp64", "mixed"):
+        with Engine(prec) as eng:
+            eng.set_network(net)
+            t0 = time.perf_counter()
+            r = eng.minimize(cg(energy_rel_tol=0.0))[0]
+            dt = time.perf_counter() - t0
+            ends[prec] = (eng.coords(), r)
+            out[prec] = {"seconds": round(dt, 4), "cg_iterations": r["num_iter"], "max_force_pN": r["grad_inf_norm"],
+                         "energy": r["energies_after"][6], "status": r["status"]}
+    (xf, rf), (xm, rm) = ends["fp64"], ends["mixed"]
+    d = np.linalg.norm(xm - xf, axis=1)
+    out["end_state"] = {"energy_rel_diff": abs(rm["energies_after"][6] - rf["energies_after"][6]) /
+                        abs(rf["energies_after"][6]),
+                        "max_force_diff_pN": abs(rm["grad_inf_norm"] - rf["grad_inf_norm"]),
+                        "position_rms_nm": float(np.sqrt((d ** 2).mean())), "position_max_nm": float(d.max())}
+    with Engine("fp64") as e64, Engine("mixed") as emx:
+        e64.set_network(net)
+        emx.set_network(net)
+        e64.set_coords(xm)
+        emx.set_coords(xm)
+        _, t64, _ = e64.energies()
+        _, tmx, _ = emx.energies()
+        f64 = e64.forces()
+        fmx = emx.forces()
+    out["same_coords"] = {"energy_rel_err": abs(tmx - t64) / abs(t64),
+                          "force_max_abs_err_pN": float(np.abs(fmx - f64).max()),
+                          "force_max_pN": float(np.abs(f64).max())}
+    return out
+
+
+def c4_report(n_replicas: int, precision: str = "mixed"):
+    """Batched ensemble: `n_replicas` independent networks of uneven size
+    (filaments log-uniform on 50-5,000, 20-50 cylinders each, C1 density)
+    minimized together in one context vs one after another; replicas/s."""
+    import torch
+    from picgo_gb300 import Engine
+    from picgo_gb300.network import make_ensemble
+    t0 = time.perf_counter()
+    nets = make_ensemble(n_replicas)
+    t_gen = time.perf_counter() - t0
+    ncyl = sum(n.n_cyl for n in nets)
+    prm = cg(energy_rel_tol=0.0)
+    out = {"workload": f"{n_replicas} replicas, filaments log-uniform 50-5,000, 20-50 cylinders, C1 density",
+           "n_replicas": n_replicas, "cylinders_total": ncyl, "precision": precision,
+           "generate_s": round(t_gen, 1)}
+    with Engine(precision) as eng:
+        eng.set_networks(nets)
+        eng.minimize(cg(energy_call_limit=20))           # warm-up: graph capture, first launches
+        eng.reset_coords()
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        eng.rebuild()
+        res = eng.minimize(prm)
+        t_b = time.perf_counter() - t0
+    out["batched"] = {"seconds": round(t_b, 3), "replicas_per_s": round(n_replicas / t_b, 2),
+                      "converged": sum(1 for r in res if r["status"] == 0 and r["grad_inf_norm"] < 1.0),
+                      "max_iterations": max(r["num_iter"] for r in res)}
+    t_loop = 0.0
+    conv = 0
+    with Engine(precision) as eng:
+        for i, net in enumerate(nets):
+            eng.set_network(net)
+            if i == 0:
+                eng.minimize(cg(energy_call_limit=20))
+                eng.reset_coords()
+            torch.cuda.synchronize()
+            t0 = time.perf_counter()
+            eng.rebuild()
+            r = eng.minimize(prm)[0]
+            t_loop += time.perf_counter() - t0
+            conv += int(r["status"] == 0 and r["grad_inf_norm"] < 1.0)
+    out["looped"] = {"seconds": round(t_loop, 3), "replicas_per_s": round(n_replicas / t_loop, 2), "converged": conv}
+    out["batched_vs_looped"] = round(t_loop / t_b, 3)
+    return out
+
+
 def cpu_sample(net, seconds: float, threads: int = 1):
     """The oracle's CG on the same network, bounded: force evaluations per second
     on `threads` host threads (1 = serial, like MEDYAN's minimizer)."""
@@ -322,6 +413,9 @@ def main():
     ap.add_argument("--cpu-seconds", type=float, default=20.0)
     ap.add_argument("--no-fp64", action="store_true")
     ap.add_argument("--no-cpu", action="store_true")
+    ap.add_argument("--no-c3", action="store_true", help="skip the mixed-vs-FP64 end-state report on the small network")
+    ap.add_argument("--c4", type=int, default=0, metavar="R",
+                    help="only run the batched-ensemble comparison on R replicas and print its JSON line")
     args = ap.parse_args()
     world = int(os.environ.get("WORLD_SIZE", "1"))
     rank = int(os.environ.get("RANK", "0"))
@@ -330,6 +424,10 @@ def main():
         import torch.distributed as tdist
         tdist.init_process_group("nccl" if args.impl == "ours" else "gloo")
         dist = tdist
+    if args.c4 > 0:
+        if rank == 0:
+            print(json.dumps({"c4": c4_report(args.c4, args.precision)}))
+        return
     if args.impl == "reference":
         out = run_reference(args, rank, world)
         if out is not None:
@@ -344,6 +442,8 @@ def main():
             out["fp64"] = f
             out["mixed_vs_fp64_time_to_1pN"] = round(f["time_to_1pN_s"] / out["time_to_1pN_s"], 3)
             out["mixed_vs_fp64_evals_per_s"] = round(out["value"] / max(f["force_evals_per_s"], 1e-9), 3)
+        if not args.no_c3:
+            out["c3_mixed_vs_fp64"] = c3_report()
         if not args.no_cpu and world == 1:
             out["cpu_baseline"] = cpu_sample(net, args.cpu_seconds * 0.6, host_threads())
             one = cpu_sample(net, args.cpu_seconds * 0.4, 1)

@@ -170,6 +170,34 @@ def _place_filaments(rng, n_fil, length, box, max_tries):
     return starts, dirs, n_fil / tries
 
 
+def _place_chains(rng, n_fil, n_cyl, box, bend_sigma=0.35):
+    """Filaments as confined persistent random walks of n_cyl 108 nm steps: the
+    direction of each step is the previous one plus N(0, bend_sigma) per
+    component, renormalised; a step that would leave the box (inset like the
+    straight rods) has the offending direction components reflected.  Used
+    where straight rods cannot fit, e.g. 50-cylinder filaments (5.4 um) in
+    boxes shrunk to keep the 2 um / 4000-cylinder density."""
+    lo = BOUNDARY_INSET + BOUNDARY_CUTOFF / 4.0
+    hi = box - BOUNDARY_INSET - BOUNDARY_CUTOFF / 4.0
+    if hi - lo < 3 * CYLINDER_SIZE:
+        raise ValueError(f"box {box} nm too small for chains of {CYLINDER_SIZE} nm cylinders")
+    pts = np.empty((n_fil, n_cyl + 1, 3))
+    pts[:, 0] = rng.uniform(lo, hi, size=(n_fil, 3))
+    phi = rng.uniform(0.0, 2.0 * math.pi, size=n_fil)
+    cz = rng.uniform(-1.0, 1.0, size=n_fil)
+    sz = np.sqrt(1.0 - cz * cz)
+    u = np.stack([sz * np.cos(phi), sz * np.sin(phi), cz], axis=1)
+    for j in range(1, n_cyl + 1):
+        if j > 1:
+            u = u + rng.normal(0.0, bend_sigma, size=u.shape)
+            u /= np.linalg.norm(u, axis=1)[:, None]
+        q = pts[:, j - 1] + CYLINDER_SIZE * u
+        out = (q < lo) | (q > hi)
+        u = np.where(out, -u, u)
+        pts[:, j] = pts[:, j - 1] + CYLINDER_SIZE * u
+    return pts.reshape(-1, 3)
+
+
 def _link_pairs(rng, mid, cyl_fil, n_need, r):
     """Cylinder pairs of different filaments with midpoint distance < r."""
     from scipy.spatial import cKDTree
@@ -220,9 +248,13 @@ def make_network(config: str | dict = "c1", seed: int | None = None, *, n_filame
     rng = np.random.default_rng(seed)
 
     length = nc * CYLINDER_SIZE
-    starts, dirs, acc = _place_filaments(rng, nf, length, L, max_tries)
-    k = np.arange(nc + 1, dtype=np.float64) * CYLINDER_SIZE
-    coord = (starts[:, None, :] + k[None, :, None] * dirs[:, None, :]).reshape(-1, 3)
+    if cfg.get("shape", "straight") == "chain":
+        coord = _place_chains(rng, nf, nc, L)
+        acc = 1.0
+    else:
+        starts, dirs, acc = _place_filaments(rng, nf, length, L, max_tries)
+        k = np.arange(nc + 1, dtype=np.float64) * CYLINDER_SIZE
+        coord = (starts[:, None, :] + k[None, :, None] * dirs[:, None, :]).reshape(-1, 3)
     nb = coord.shape[0]
     bead_of = np.arange(nb, dtype=np.int64).reshape(nf, nc + 1)
     b1 = bead_of[:, :-1].reshape(-1)
@@ -289,3 +321,22 @@ def jitter(net: Network, sigma: float, seed: int = 1) -> Network:
     rng = np.random.default_rng(seed)
     out.coord = out.coord + rng.normal(0.0, sigma, size=out.coord.shape)
     return out
+
+
+def make_ensemble(n_replicas: int = 512, seed: int = 20261203 + 4, fil_range=(50, 5000), cyl_range=(20, 50),
+                  linkers_per_cylinder: float = 500 / 4000) -> list:
+    """Independent replica networks of uneven size: filament counts log-uniform
+    on ``fil_range``, cylinders per filament uniform on ``cyl_range``, box side
+    scaled to hold the 2 um / 4000-cylinder density, linkers at the 200 x 20
+    network's ratio; filaments as confined chains (:func:`_place_chains`),
+    since straight rods do not fit the shrunk boxes."""
+    rng = np.random.default_rng(seed)
+    nfs = np.rint(np.exp(rng.uniform(math.log(fil_range[0]), math.log(fil_range[1]), size=n_replicas))).astype(int)
+    ncs = rng.integers(cyl_range[0], cyl_range[1] + 1, size=n_replicas)
+    nets = []
+    for i in range(n_replicas):
+        ncyl = int(nfs[i] * ncs[i])
+        cfg = dict(n_filaments=int(nfs[i]), n_cyl_per_filament=int(ncs[i]), box=None,
+                   n_linkers=int(round(linkers_per_cylinder * ncyl)), linker_k=8.0, n_motors=0, shape="chain")
+        nets.append(make_network(cfg, seed=seed * 1000 + i))
+    return nets
