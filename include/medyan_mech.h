@@ -254,6 +254,65 @@ typedef struct MechProfile {
 int32_t mech_profile(MechContext* ctx, int32_t iters, MechProfile* out);
 
 /*
+ * Second-order calls (FP64 contexts; a mixed context returns MECH_ERR_STATE).
+ * They replace ForceFieldManager::computeHessian's finite-difference Hessian
+ * (Mechanics/ForceField/ForceFieldManager.cpp:354-489) with exact
+ * Hessian-vector products: every force field differentiated in forward mode
+ * along v, at the context's current coordinates and neighbor lists.
+ */
+typedef struct MechSolveParams {
+    double rel_tol;                 /* CG stops at |r| <= rel_tol |b| */
+    int32_t max_iter;               /* CG iterations per solve */
+    double shift;                   /* solves (H + shift I) y = b; 0 for the plain Hessian */
+} MechSolveParams;
+
+typedef struct MechSolveInfo {
+    int32_t iterations;             /* CG iterations (summed over Newton steps) */
+    int32_t converged;              /* last solve reached rel_tol */
+    double rel_residual;            /* |r| / |b| of the last solve */
+    int64_t launches;               /* kernel launches */
+    int32_t newton_steps;           /* mech_newton_refine only */
+    double max_force;               /* mech_newton_refine: max |F| at exit */
+    int32_t negative_curvature;     /* a solve met p . H p <= 0 and stopped there */
+} MechSolveInfo;
+
+/*
+ * hv = H v for replica r (caller bead order, 3 doubles per bead).
+ * MECH_HVP_ENERGY: the exact Hessian of the total energy (symmetric).
+ * MECH_HVP_FORCE_JACOBIAN: minus the Jacobian of computeForces as the
+ * reference evaluates it, including its move of nearly coplanar
+ * excluded-volume pairs off their plane (CylinderExclVolRepulsion.cpp:610-626),
+ * which makes it slightly non-symmetric; this is what the reference's
+ * finite-difference computeHessian approximates before symmetrizing.
+ */
+#define MECH_HVP_ENERGY          0
+#define MECH_HVP_FORCE_JACOBIAN  1
+int32_t mech_hvp(MechContext* ctx, int32_t replica, int32_t mode, const double* v, double* hv);
+
+/* Replace the stiffness and/or rest length of replica r's linkers (NULL keeps
+ * one); the parameters the adjoint differentiates. */
+int32_t mech_set_linker_params(MechContext* ctx, int32_t replica, const double* k, const double* eq_length);
+
+/*
+ * Implicit adjoint at an equilibrium x* of replica r: for a loss
+ * L(x*, theta) = dL_dE * E(x*, theta) + R(x*) with dL_dx = dR/dx at x*,
+ * solves H lambda = dL_dx by CG and returns, per linker,
+ *   dL/dk  = dL_dE * dE/dk  - lambda . d(grad_x E)/dk
+ *   dL/dl0 = dL_dE * dE/dl0 - lambda . d(grad_x E)/dl0
+ * (the E term contributes no implicit part since grad_x E = 0 at x*).
+ * Returns MECH_ERR_ITER_LIMIT (gradients still written) if CG stopped early.
+ */
+int32_t mech_adjoint(MechContext* ctx, int32_t replica, const double* dL_dx, double dL_dE, const MechSolveParams* sp,
+                     double* dL_dk, double* dL_dl0, MechSolveInfo* info);
+
+/* Newton refinement of every replica's equilibrium (run after mech_minimize):
+ * dx = (H + shift I)^-1 F by CG (truncated at non-positive curvature), then
+ * x += alpha dx with alpha halved from 1 until max |F| decreases; repeated
+ * until max |F| < force_tol, max_steps steps, or no decrease. */
+int32_t mech_newton_refine(MechContext* ctx, int32_t max_steps, double force_tol, const MechSolveParams* sp,
+                           MechSolveInfo* info);
+
+/*
  * Filament stretching and bending energies (FP64) of one network held in
  * caller-owned DEVICE memory, without allocating: no reference counterpart
  * (MEDYAN evaluates these inside ForceFieldManager::computeIndividualEnergies;

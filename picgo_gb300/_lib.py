@@ -32,7 +32,8 @@ EXPORTS = [
     "mech_abi_version", "mech_last_error", "mech_ctx_create", "mech_ctx_destroy", "mech_set_networks",
     "mech_set_coords", "mech_get_coords", "mech_rebuild_neighbors", "mech_get_pairs", "mech_energy",
     "mech_forces", "mech_minimize", "mech_get_forces", "mech_get_stretch_forces", "mech_get_timing",
-    "mech_reset_coords", "mech_profile", "mech_filament_energy_device",
+    "mech_reset_coords", "mech_profile", "mech_filament_energy_device", "mech_hvp", "mech_set_linker_params",
+    "mech_adjoint", "mech_newton_refine",
 ]
 
 
@@ -94,6 +95,19 @@ class MechProfile(C.Structure):
                 ("n_exvol_fp64_force", C.c_int64)]
 
 
+class MechSolveParams(C.Structure):
+    _fields_ = [("rel_tol", C.c_double), ("max_iter", C.c_int32), ("shift", C.c_double)]
+
+
+class MechSolveInfo(C.Structure):
+    _fields_ = [("iterations", C.c_int32), ("converged", C.c_int32), ("rel_residual", C.c_double),
+                ("launches", C.c_int64), ("newton_steps", C.c_int32), ("max_force", C.c_double),
+                ("negative_curvature", C.c_int32)]
+
+    def as_dict(self) -> dict:
+        return {k: getattr(self, k) for k, _ in self._fields_}
+
+
 _lock = threading.Lock()
 _lib = None
 
@@ -135,6 +149,12 @@ def load(build_if_missing: bool = False):
         L.mech_reset_coords.argtypes = [vp]
         L.mech_profile.argtypes = [vp, C.c_int32, C.POINTER(MechProfile)]
         L.mech_filament_energy_device.argtypes = [C.c_int32, C.c_int32, vp, vp, vp, vp, vp, vp, vp, vp]
+        L.mech_hvp.argtypes = [vp, C.c_int32, C.c_int32, _dp, _dp]
+        L.mech_set_linker_params.argtypes = [vp, C.c_int32, _dp, _dp]
+        L.mech_adjoint.argtypes = [vp, C.c_int32, _dp, C.c_double, C.POINTER(MechSolveParams), _dp, _dp,
+                                   C.POINTER(MechSolveInfo)]
+        L.mech_newton_refine.argtypes = [vp, C.c_int32, C.c_double, C.POINTER(MechSolveParams),
+                                         C.POINTER(MechSolveInfo)]
         for name in EXPORTS:
             f = getattr(L, name)
             if f.restype is None or f.restype is C.c_int:

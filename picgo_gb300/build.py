@@ -26,6 +26,7 @@ UNITS = [
     ("mech_nl.cu", "mech_nl.o", []),
     ("mech_host.cu", "mech_host.o", []),
     ("mech_static.cu", "mech_static.o", []),
+    ("mech_hvp.cu", "mech_hvp.o", []),
 ]
 
 

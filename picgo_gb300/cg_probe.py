@@ -2,12 +2,14 @@
 
     python -m picgo_gb300.cg_probe --workload c2 --precision mixed --energy-calls 40
     python -m picgo_gb300.cg_probe --workload c2 --precision mixed --evals 2
+    python -m picgo_gb300.cg_probe --workload c2 --precision mixed --forces 3
 
 The first form runs neighbor-list rebuild + Polak-Ribiere CG from the seeded
 start until `--energy-calls` energy calls (a launch-list target: every kernel
 of real CG iterations); the second launches each evaluation kernel `--evals`
-times through mech_profile (a target for one-kernel captures).  Both print one
-JSON line.
+times through mech_profile; the third makes only `--forces` mech_forces calls
+(or `--energies` mech_energy calls), so that a profiler's first matching
+launches are those of one evaluation kind.  Each prints one JSON line.
 """
 from __future__ import annotations
 
@@ -25,13 +27,21 @@ def main(argv=None):
     ap.add_argument("--precision", choices=["mixed", "fp64"], default="mixed")
     ap.add_argument("--energy-calls", type=int, default=40)
     ap.add_argument("--evals", type=int, default=0, help="profile mode: launches per evaluation kernel")
+    ap.add_argument("--forces", type=int, default=0, help="only this many mech_forces calls")
+    ap.add_argument("--energies", type=int, default=0, help="only this many mech_energy calls")
     args = ap.parse_args(argv)
     net = make_network(args.workload, seed=args.seed)
     out = {"workload": args.workload, "precision": args.precision, "n_beads": net.n_beads}
     with Engine(args.precision) as eng:
         eng.set_network(net)
         out["lists"] = eng.rebuild()
-        if args.evals > 0:
+        if args.forces > 0 or args.energies > 0:
+            for _ in range(args.forces):
+                f = eng.forces()
+            for _ in range(args.energies):
+                e = eng.energies()[1]
+            out["calls"] = {"forces": args.forces, "energies": args.energies}
+        elif args.evals > 0:
             out["profile"] = eng.profile(args.evals)
         else:
             t0 = time.perf_counter()

@@ -18,6 +18,7 @@
 
 #include <algorithm>
 
+#include "mech_bulk.cuh"
 #include "mech_device.cuh"
 
 namespace mech {
@@ -401,12 +402,105 @@ __device__ __forceinline__ Pos<float> pos_at(const DevNet<float>& n, const float
     return tr ? moved_f(p, n.d, b, lf) : p;
 }
 
-__global__ void __launch_bounds__(kBlock) k_fil_energy_mx(DevNet<float> n, int want, int trial) {
+
+// ---------------------------------------------------------------------------
+// Mixed engine, bulk-staged filament energy: a persistent walk over runs of
+// tiles with run-start partial slots (see flush_run), where each selected
+// tile's positions (with a one-bead halo),
+// constants, flags and (for a trial) search direction arrive in shared memory
+// by cp.async.bulk on a three-stage mbarrier ring, so a block keeps several
+// ~14 KB transfers in flight instead of per-thread dependent loads.  Ranges
+// are rounded outward to the 16-byte copy granularity; the bead arrays are
+// allocated with the padding that rounding needs.
+// ---------------------------------------------------------------------------
+constexpr int kBulkStages = 3;
+constexpr int kBulkXBeads = kFilTile + 4;    // tile + 1-bead halo, even-aligned ends
+constexpr int kBulkDBeads = kFilTile + 8;    // tile + halo, 4-bead aligned ends
+constexpr int kBulkFlags = kFilTile + 32;    // tile + halo, 16-byte aligned ends
+constexpr int kBulkWaitLimit = 1 << 22;      // mbarrier polls before a stage counts as lost
+
+struct __align__(16) EnergyStage {
+    float x[6 * kBulkXBeads];      // float-float positions, beads [xs, xe)
+    float4 par[kFilTile];          // k_str, l0, k_bend, theta0, beads [tb, te)
+    float d[3 * kBulkDBeads];      // search direction, beads [ds, de)
+    uint8_t flag[kBulkFlags];      // bead flags, beads [fs, fe)
+};
+
+struct StageRange {
+    int xs, xe, ds, de, fs, fe;
+};
+// Staged ranges of tile [tb, te) with `halo` beads each side, clamped to the
+// network and rounded outward: positions to even beads (24 B each), the
+// direction to multiples of 4 beads (12 B), flags to 16 beads (1 B).
+__device__ __forceinline__ StageRange stage_range(int tb, int te, int nb, int halo) {
+    StageRange r;
+    const int lo = max(tb - halo, 0), hi = min(te + halo, nb);
+    r.xs = lo & ~1;
+    r.xe = (hi + 1) & ~1;
+    r.ds = lo & ~3;
+    r.de = (hi + 3) & ~3;
+    r.fs = lo & ~15;
+    r.fe = (hi + 15) & ~15;
+    return r;
+}
+
+// Issue the copies of tile ti into stage `st` (thread 0).  A range that fails
+// the alignment check is not copied: the barrier is completed without it and
+// the error word records it.
+__device__ void issue_energy_stage(const DevNet<float>& n, int ti, bool tr, EnergyStage* st, uint64_t* bar) {
+    const Tile t = n.ftile[ti];
+    const CGState& S = n.st[t.replica];
+    const float* X = n.x[S.xbuf];
+    const StageRange rg = stage_range(t.begin, t.end, n.nb, 1);
+    const void* src[4] = {X + 6 * (size_t)rg.xs, n.bpar + 4 * (size_t)t.begin, n.d + 3 * (size_t)rg.ds, n.bflag + rg.fs};
+    void* dst[4] = {st->x, st->par, st->d, st->flag};
+    const unsigned bytes[4] = {24u * (unsigned)(rg.xe - rg.xs), 16u * (unsigned)(t.end - t.begin),
+                               tr ? 12u * (unsigned)(rg.de - rg.ds) : 0u, (unsigned)(rg.fe - rg.fs)};
+    unsigned total = 0;
+    bool ok = true;
+    for (int k = 0; k < 4; ++k) {
+        if (!bytes[k]) continue;
+        if (!aligned16(src[k], bytes[k]) || !aligned16(dst[k], bytes[k])) ok = false;
+        total += bytes[k];
+    }
+    fence_proxy_async_smem();
+    if (!ok) {
+        atomicOr(n.err, 16u);
+        mbar_arrive_expect_tx(bar, 0);
+        return;
+    }
+    mbar_arrive_expect_tx(bar, total);
+    for (int k = 0; k < 4; ++k)
+        if (bytes[k]) bulk_copy_g2s(dst[k], src[k], bytes[k], bar);
+}
+
+__device__ __forceinline__ bool tile_selected(const DevNet<float>& n, int ti, int want) {
+    return replica_selected(n.st[n.ftile[ti].replica], want);
+}
+
+__global__ void __launch_bounds__(kBlock) k_fil_energy_bulk(DevNet<float> n, int want, int trial) {
+    __shared__ EnergyStage stage[kBulkStages];
+    __shared__ __align__(8) uint64_t bar[kBulkStages];
     __shared__ double sh[32 * MECH_NUM_FF];
-    __shared__ int s_flag;
+    __shared__ int s_flag, s_abort;
     const int t0 = blockIdx.x * n.ptiles[0], t1 = min(t0 + n.ptiles[0], n.n_ftiles);
     const bool tr = trial != 0;
-    int cur = -1, first = 0, cnt = 0, xb = 0;
+    if (threadIdx.x == 0) {
+        for (int k = 0; k < kBulkStages; ++k) mbar_init(&bar[k], 1);
+        mbar_init_fence();
+        s_abort = 0;
+    }
+    __syncthreads();
+    // producer state (thread 0): next tile to consider, copies issued
+    int pi = t0, issued = 0;
+    if (threadIdx.x == 0) {
+        for (; pi < t1 && issued < kBulkStages; ++pi)
+            if (tile_selected(n, pi, want)) {
+                issue_energy_stage(n, pi, tr, &stage[issued % kBulkStages], &bar[issued % kBulkStages]);
+                ++issued;
+            }
+    }
+    int cur = -1, first = 0, cnt = 0, xb = 0, j = 0;
     bool go = false;
     float lf = 0.f;
     FF es, eb;
@@ -430,29 +524,56 @@ __global__ void __launch_bounds__(kBlock) k_fil_energy_mx(DevNet<float> n, int w
         }
         if (!go) continue;
         ++cnt;
+        const int sidx = j % kBulkStages;
+        if (!mbar_wait_bounded(&bar[sidx], (unsigned)((j / kBulkStages) & 1), kBulkWaitLimit)) {
+            atomicOr(n.err, 32u);
+            s_abort = 1;
+        }
+        const EnergyStage& S = stage[sidx];
         const int b = t.begin + threadIdx.x;
         if (b < t.end) {
-            const float* X = n.x[xb];
-            // every load is issued up front (neighbours clamped to the bead
-            // range, unused at filament ends) so none waits on the flags
-            const int fl = n.bflag[b];
-            const Pos<float> p0 = pos_at(n, X, b, tr, lf);
-            const Pos<float> pp = pos_at(n, X, min(b + 1, n.nb - 1), tr, lf);
-            const Pos<float> pm = pos_at(n, X, max(b - 1, 0), tr, lf);
-            float ks, l0, kb, th;
-            load_par(n.bpar, b, ks, l0, kb, th);
-            if (tr) store_pos(n.x[xb ^ 1], b, p0);   // materialize the owned trial position
+            const StageRange rg = stage_range(t.begin, t.end, n.nb, 1);
+            const int fl = S.flag[b - rg.fs];
+            Pos<float> p0 = load_pos(S.x, b - rg.xs);
+            Pos<float> pp = fl & 1 ? load_pos(S.x, b + 1 - rg.xs) : p0;
+            Pos<float> pm = fl & 2 ? load_pos(S.x, b - 1 - rg.xs) : p0;
+            if (tr) {
+                p0 = moved_f(p0, S.d, b - rg.ds, lf);
+                if (fl & 1) pp = moved_f(pp, S.d, b + 1 - rg.ds, lf);
+                if (fl & 2) pm = moved_f(pm, S.d, b - 1 - rg.ds, lf);
+                store_pos(n.x[xb ^ 1], b, p0);   // materialize the owned trial position
+            }
+            const float4 pr = S.par[b - t.begin];
             if (fl & 1) {
                 float r2[3];
                 pdiff(pp, p0, r2);
-                es.add(stretch_energy<float>(r2[0], r2[1], r2[2], ks, l0));
+                es.add(stretch_energy<float>(r2[0], r2[1], r2[2], pr.x, pr.y));
                 if (fl & 2) {
                     float r1[3];
                     pdiff(p0, pm, r1);
-                    eb.add(bend_energy<float>(r1, r2, kb, th));
+                    eb.add(bend_energy<float>(r1, r2, pr.z, pr.w));
                 }
             }
         }
+        ++j;
+        __syncthreads();   // stage sidx fully read
+        if (s_abort) break;
+        if (threadIdx.x == 0) {
+            for (; pi < t1; ++pi)
+                if (tile_selected(n, pi, want)) {
+                    issue_energy_stage(n, pi, tr, &stage[issued % kBulkStages], &bar[issued % kBulkStages]);
+                    ++issued;
+                    ++pi;
+                    break;
+                }
+        }
+    }
+    if (s_abort) {
+        // drain: copies still in flight must land before the block's shared memory is released
+        if (threadIdx.x == 0)
+            for (int q = max(j - 1, 0); q < issued; ++q)
+                mbar_wait_bounded(&bar[q % kBulkStages], (unsigned)((q / kBulkStages) & 1), kBulkWaitLimit);
+        return;
     }
     if (cnt) {
         double w[2] = {warp_sum_pair(es), warp_sum_pair(eb)};
@@ -460,11 +581,97 @@ __global__ void __launch_bounds__(kBlock) k_fil_energy_mx(DevNet<float> n, int w
     }
 }
 
-__global__ void __launch_bounds__(kBlock) k_fil_force_mx(DevNet<float> n, int want) {
+
+// ---------------------------------------------------------------------------
+// Mixed engine, bulk-staged filament forces: the same walk, with each
+// selected tile's positions (two-bead halo), constants and flags of
+// the neighbouring beads, previous forces and CSR offsets staged by
+// cp.async.bulk like k_fil_energy_bulk; the bead's gathered contributions are
+// contiguous in memory and read directly.
+// ---------------------------------------------------------------------------
+constexpr int kBulkFXBeads = kFilTile + 8;    // tile + 2-bead halo, even-aligned ends
+constexpr int kBulkFPar = kFilTile + 4;       // constants of beads tb - 1 .. te
+constexpr int kBulkFPrev = kFilTile + 4;      // previous forces, 4-bead aligned ends
+constexpr int kBulkCsr = kFilTile + 8;        // CSR offsets tb .. te, 4-entry aligned ends
+
+struct __align__(16) ForceStage {
+    float x[6 * kBulkFXBeads];
+    float4 par[kBulkFPar];
+    float fp[3 * kBulkFPrev];
+    int csr[kBulkCsr];
+    uint8_t flag[kBulkFlags];
+};
+
+struct ForceRange {
+    int xs, xe, ps, pe, qs, qe, cs, ce, fs, fe;
+};
+__device__ __forceinline__ ForceRange force_range(int tb, int te, int nb) {
+    ForceRange r;
+    const int lo2 = max(tb - 2, 0), hi2 = min(te + 2, nb);
+    r.xs = lo2 & ~1;
+    r.xe = (hi2 + 1) & ~1;
+    r.ps = max(tb - 1, 0);
+    r.pe = min(te + 1, nb);
+    r.qs = tb & ~3;
+    r.qe = (te + 3) & ~3;
+    r.cs = tb & ~3;
+    r.ce = (te + 1 + 3) & ~3;
+    r.fs = lo2 & ~15;
+    r.fe = (hi2 + 15) & ~15;
+    return r;
+}
+
+__device__ void issue_force_stage(const DevNet<float>& n, int ti, ForceStage* st, uint64_t* bar) {
+    const Tile t = n.ftile[ti];
+    const CGState& S = n.st[t.replica];
+    const float* X = n.x[S.xbuf];
+    const float* Fp = n.f[S.fbuf];
+    const ForceRange rg = force_range(t.begin, t.end, n.nb);
+    const void* src[5] = {X + 6 * (size_t)rg.xs, n.bpar + 4 * (size_t)rg.ps, Fp + 3 * (size_t)rg.qs, n.csr_off + rg.cs,
+                          n.bflag + rg.fs};
+    void* dst[5] = {st->x, st->par, st->fp, st->csr, st->flag};
+    const unsigned bytes[5] = {24u * (unsigned)(rg.xe - rg.xs), 16u * (unsigned)(rg.pe - rg.ps),
+                               12u * (unsigned)(rg.qe - rg.qs), 4u * (unsigned)(rg.ce - rg.cs),
+                               (unsigned)(rg.fe - rg.fs)};
+    unsigned total = 0;
+    bool ok = true;
+    for (int k = 0; k < 5; ++k) {
+        if (!bytes[k]) continue;
+        if (!aligned16(src[k], bytes[k]) || !aligned16(dst[k], bytes[k])) ok = false;
+        total += bytes[k];
+    }
+    fence_proxy_async_smem();
+    if (!ok) {
+        atomicOr(n.err, 16u);
+        mbar_arrive_expect_tx(bar, 0);
+        return;
+    }
+    mbar_arrive_expect_tx(bar, total);
+    for (int k = 0; k < 5; ++k)
+        if (bytes[k]) bulk_copy_g2s(dst[k], src[k], bytes[k], bar);
+}
+
+__global__ void __launch_bounds__(kBlock) k_fil_force_bulk(DevNet<float> n, int want) {
+    __shared__ ForceStage stage[kBulkStages];
+    __shared__ __align__(8) uint64_t bar[kBulkStages];
     __shared__ double sh[32 * 3];
-    __shared__ int s_flag;
+    __shared__ int s_flag, s_abort;
     const int t0 = blockIdx.x * n.ptiles[1], t1 = min(t0 + n.ptiles[1], n.n_ftiles);
-    int cur = -1, first = 0, cnt = 0, xb = 0, fb = 0;
+    if (threadIdx.x == 0) {
+        for (int k = 0; k < kBulkStages; ++k) mbar_init(&bar[k], 1);
+        mbar_init_fence();
+        s_abort = 0;
+    }
+    __syncthreads();
+    int pi = t0, issued = 0;
+    if (threadIdx.x == 0) {
+        for (; pi < t1 && issued < kBulkStages; ++pi)
+            if (tile_selected(n, pi, want)) {
+                issue_force_stage(n, pi, &stage[issued % kBulkStages], &bar[issued % kBulkStages]);
+                ++issued;
+            }
+    }
+    int cur = -1, first = 0, cnt = 0, fb = 0, j = 0;
     bool go = false;
     float mx = 0.f;
     FF ff, ffp;
@@ -484,75 +691,94 @@ __global__ void __launch_bounds__(kBlock) k_fil_force_mx(DevNet<float> n, int wa
             ffp = FF();
             const CGState& S = n.st[cur];
             go = replica_selected(S, want);
-            xb = S.xbuf;
             fb = S.fbuf;
         }
         if (!go) continue;
         ++cnt;
+        const int sidx = j % kBulkStages;
+        if (!mbar_wait_bounded(&bar[sidx], (unsigned)((j / kBulkStages) & 1), kBulkWaitLimit)) {
+            atomicOr(n.err, 32u);
+            s_abort = 1;
+        }
+        const ForceStage& S = stage[sidx];
         const int b = t.begin + threadIdx.x;
         if (b < t.end) {
-            const float* X = n.x[xb];
-            // every load is issued up front (neighbours clamped to the bead
-            // range, unused at filament ends) so none waits on the flags
-            const int bm1 = max(b - 1, 0), bm2 = max(b - 2, 0), bp1 = min(b + 1, n.nb - 1), bp2 = min(b + 2, n.nb - 1);
-            const int f0 = n.bflag[b], fm_raw = n.bflag[bm1], fp_raw = n.bflag[bp1];
-            const int fm = (f0 & 2) ? fm_raw : 0;
-            const int fp = (f0 & 1) ? fp_raw : 0;
-            const Pos<float> p0 = load_pos(X, b);
-            const Pos<float> pm1 = load_pos(X, bm1), pp1 = load_pos(X, bp1);
-            const Pos<float> pm2 = load_pos(X, bm2), pp2 = load_pos(X, bp2);
-            const int c0 = n.csr_off[b], c1 = n.csr_off[b + 1];
-            float ksm, l0m, kbm, thm, ks, l0, kb, th, ksp, l0p, kbp, thp;
-            load_par(n.bpar, bm1, ksm, l0m, kbm, thm);
-            load_par(n.bpar, b, ks, l0, kb, th);
-            load_par(n.bpar, bp1, ksp, l0p, kbp, thp);
+            const ForceRange rg = force_range(t.begin, t.end, n.nb);
+            const int f0 = S.flag[b - rg.fs];
+            const int fm = (f0 & 2) ? S.flag[b - 1 - rg.fs] : 0;
+            const int fp = (f0 & 1) ? S.flag[b + 1 - rg.fs] : 0;
+            const Pos<float> p0 = load_pos(S.x, b - rg.xs);
+            const Pos<float> pm1 = (f0 & 2) ? load_pos(S.x, b - 1 - rg.xs) : p0;
+            const Pos<float> pp1 = (f0 & 1) ? load_pos(S.x, b + 1 - rg.xs) : p0;
+            const Pos<float> pm2 = (fm & 2) ? load_pos(S.x, b - 2 - rg.xs) : p0;
+            const Pos<float> pp2 = (fp & 1) ? load_pos(S.x, b + 2 - rg.xs) : p0;
+            const float4 prm = (f0 & 2) ? S.par[b - 1 - rg.ps] : make_float4(0.f, 0.f, 0.f, 0.f);
+            const float4 pr0 = S.par[b - rg.ps];
+            const float4 prp = (f0 & 1) ? S.par[b + 1 - rg.ps] : make_float4(0.f, 0.f, 0.f, 0.f);
             float F[3] = {0.f, 0.f, 0.f};
             float rm[3] = {0, 0, 0}, rp[3] = {0, 0, 0};
             if (f0 & 2) pdiff(p0, pm1, rm);
             if (f0 & 1) pdiff(pp1, p0, rp);
-            // stretching: cylinder (b-1, b) then (b, b+1)
             if (f0 & 2) {
                 float S1[3];
-                stretch_force<float>(rm[0], rm[1], rm[2], ksm, l0m, S1);
+                stretch_force<float>(rm[0], rm[1], rm[2], prm.x, prm.y, S1);
                 F[0] += S1[0]; F[1] += S1[1]; F[2] += S1[2];
             }
             if (f0 & 1) {
                 float S2[3];
-                stretch_force<float>(rp[0], rp[1], rp[2], ks, l0, S2);
+                stretch_force<float>(rp[0], rp[1], rp[2], pr0.x, pr0.y, S2);
                 F[0] += -S2[0]; F[1] += -S2[1]; F[2] += -S2[2];
             }
-            // bending: triples centred on b-1, b, b+1
             if ((f0 & 2) && (fm & 2)) {
                 float r1[3], a1[3], a2[3];
                 pdiff(pm1, pm2, r1);
-                bend_force<float>(r1, rm, kbm, thm, a1, a2);
+                bend_force<float>(r1, rm, prm.z, prm.w, a1, a2);
                 F[0] += a2[0]; F[1] += a2[1]; F[2] += a2[2];
             }
             if ((f0 & 3) == 3) {
                 float a1[3], a2[3];
-                bend_force<float>(rm, rp, kb, th, a1, a2);
+                bend_force<float>(rm, rp, pr0.z, pr0.w, a1, a2);
                 F[0] += a1[0] - a2[0]; F[1] += a1[1] - a2[1]; F[2] += a1[2] - a2[2];
             }
             if ((f0 & 1) && (fp & 1)) {
                 float r2[3], a1[3], a2[3];
                 pdiff(pp2, pp1, r2);
-                bend_force<float>(rp, r2, kbp, thp, a1, a2);
+                bend_force<float>(rp, r2, prp.z, prp.w, a1, a2);
                 F[0] += -a1[0]; F[1] += -a1[1]; F[2] += -a1[2];
             }
+            const int c0 = S.csr[b - rg.cs], c1 = S.csr[b + 1 - rg.cs];
             for (int c = c0; c < c1; ++c) {
                 F[0] += n.contrib[3 * (size_t)c];
                 F[1] += n.contrib[3 * (size_t)c + 1];
                 F[2] += n.contrib[3 * (size_t)c + 2];
             }
             float* Fo = n.f[fb ^ 1] + 3 * (size_t)b;
-            const float* Fp = n.f[fb] + 3 * (size_t)b;
+            const float* Fq = S.fp + 3 * (b - rg.qs);
             Fo[0] = F[0];
             Fo[1] = F[1];
             Fo[2] = F[2];
             mx = fmaxf(mx, fmaxf(fmaxf(fabsf(F[0]), fabsf(F[1])), fabsf(F[2])));
             ff.add(bead_dot(F[0], F[1], F[2], F[0], F[1], F[2]));
-            ffp.add(bead_dot(F[0], F[1], F[2], Fp[0], Fp[1], Fp[2]));
+            ffp.add(bead_dot(F[0], F[1], F[2], Fq[0], Fq[1], Fq[2]));
         }
+        ++j;
+        __syncthreads();   // stage sidx fully read
+        if (s_abort) break;
+        if (threadIdx.x == 0) {
+            for (; pi < t1; ++pi)
+                if (tile_selected(n, pi, want)) {
+                    issue_force_stage(n, pi, &stage[issued % kBulkStages], &bar[issued % kBulkStages]);
+                    ++issued;
+                    ++pi;
+                    break;
+                }
+        }
+    }
+    if (s_abort) {
+        if (threadIdx.x == 0)
+            for (int q = max(j - 1, 0); q < issued; ++q)
+                mbar_wait_bounded(&bar[q % kBulkStages], (unsigned)((q / kBulkStages) & 1), kBulkWaitLimit);
+        return;
     }
     if (cnt) {
         double w[3] = {warp_max_lane0(mx), warp_sum_pair(ff), warp_sum_pair(ffp)};
@@ -921,7 +1147,7 @@ int launch_energy(const DevNet<Real>& n, int want, int trial, cudaStream_t s) {
         ++launched;
     }
     launched += launch_exvol_energy<Real>(n, want, trial, s);
-    if constexpr (sizeof(Real) == 4) k_fil_energy_mx<<<n.pgrid[0], kBlock, 0, s>>>(n, want, trial);
+    if constexpr (sizeof(Real) == 4) k_fil_energy_bulk<<<n.pgrid[0], kBlock, 0, s>>>(n, want, trial);
     else k_fil_energy<Real><<<n.n_ftiles, kBlock, 0, s>>>(n, want, trial);
     return launched + 1;
 }
@@ -936,7 +1162,7 @@ int launch_forces(const DevNet<Real>& n, int want, cudaStream_t s) {
         ++launched;
     }
     launched += launch_exvol_forces<Real>(n, want, s);
-    if constexpr (sizeof(Real) == 4) k_fil_force_mx<<<n.pgrid[1], kBlock, 0, s>>>(n, want);
+    if constexpr (sizeof(Real) == 4) k_fil_force_bulk<<<n.pgrid[1], kBlock, 0, s>>>(n, want);
     else k_fil_force<Real><<<n.n_ftiles, kBlock, 0, s>>>(n, want);
     return launched + 1;
 }
@@ -984,11 +1210,11 @@ int launch_part(const DevNet<Real>& n, int which, cudaStream_t s) {
     const int lm = n_lm_tiles(n, &ev_t, &bb_t);
     switch (which) {
         case 0:
-            if constexpr (sizeof(Real) == 4) k_fil_energy_mx<<<n.pgrid[0], kBlock, 0, s>>>(n, -1, 0);
+            if constexpr (sizeof(Real) == 4) k_fil_energy_bulk<<<n.pgrid[0], kBlock, 0, s>>>(n, -1, 0);
             else k_fil_energy<Real><<<n.n_ftiles, kBlock, 0, s>>>(n, -1, 0);
             return 1;
         case 1:
-            if constexpr (sizeof(Real) == 4) k_fil_force_mx<<<n.pgrid[1], kBlock, 0, s>>>(n, -1);
+            if constexpr (sizeof(Real) == 4) k_fil_force_bulk<<<n.pgrid[1], kBlock, 0, s>>>(n, -1);
             else k_fil_force<Real><<<n.n_ftiles, kBlock, 0, s>>>(n, -1);
             return 1;
         case 2: if (lm + bb_t > 0) { k_bond_bnd<Real><<<lm + bb_t, kBlock, 0, s>>>(n, -1, 0, 0, lm, ev_t); return 1; } return 0;
@@ -1003,8 +1229,8 @@ int persistent_blocks(int device, int which) {
     if (cached_dev != device) {
         int sms = 0, b[3] = {0, 0, 0};
         cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, device);
-        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b[0], k_fil_energy_mx, kBlock, 0);
-        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b[1], k_fil_force_mx, kBlock, 0);
+        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b[0], k_fil_energy_bulk, kBlock, 0);
+        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b[1], k_fil_force_bulk, kBlock, 0);
         cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b[2], k_direction_mx, kBlock, 0);
         for (int k = 0; k < 3; ++k) cached[k] = std::max(1, sms) * std::max(1, b[k]);
         cached_dev = device;

@@ -85,8 +85,18 @@ struct MechContext {
     DeviceBuffer rep_cell, rep_dims, rep_rmax2, rep_rmin2, rep_margin, rep_q, rep_ncyl, rep_plane, rep_cyl, rep_bcut,
         gather_idx, gather_out;
     DeviceBuffer perm_all, stage;   // caller -> internal bead map of all replicas; coordinate staging
+    // Hessian-vector products, adjoint and Newton solves (FP64 engine)
+    DeviceBuffer hv_a, hv_b, cg_x, cg_r, cg_p, cg_Ap, cg_scal, cg_part, cg_ticket;
     int n_ftiles = 0, n_stiles = 0;
     int sp_tiles[K_NUM_SPARSE] = {0, 0, 0, 0};
+    // host copies of the full tile lists, and the compacted view that a
+    // batched minimization switches to once most replicas have finished
+    std::vector<Tile> h_ftiles, h_stiles;
+    std::vector<int> h_skind;
+    DeviceBuffer ftile_c, stile_c, stile_kind_c, rt_c;
+    bool compact = false;
+    int n_ftiles_c = 0, n_stiles_c = 0;
+    int sp_tiles_c[K_NUM_SPARSE] = {0, 0, 0, 0};
     int slot_base[K_NUM_SPARSE + 1] = {0, 0, 0, 0, 0};
     std::vector<RepTiles> h_rt;
     CGState* h_st = nullptr;   // pinned mirror of the states
@@ -126,12 +136,12 @@ DevNet<Real> make_devnet(MechContext* c) {
     n.ev_energy = c->ev_energy.as<double>();
     n.bflag = c->bflag.as<uint8_t>();
     n.bpar = c->bpar.as<Real>();
-    n.n_ftiles = c->n_ftiles;
-    n.ftile = c->ftile.as<Tile>();
+    n.n_ftiles = c->compact ? c->n_ftiles_c : c->n_ftiles;
+    n.ftile = (c->compact ? c->ftile_c : c->ftile).as<Tile>();
     for (int k = 0; k < 3; ++k) {
-        n.pgrid[k] = std::max(1, std::min(c->n_ftiles, persistent_blocks(c->device, k)));
-        n.ptiles[k] = (c->n_ftiles + n.pgrid[k] - 1) / n.pgrid[k];
-        n.pgrid[k] = (c->n_ftiles + n.ptiles[k] - 1) / n.ptiles[k];
+        n.pgrid[k] = std::max(1, std::min(n.n_ftiles, persistent_blocks(c->device, k)));
+        n.ptiles[k] = (n.n_ftiles + n.pgrid[k] - 1) / n.pgrid[k];
+        n.pgrid[k] = (n.n_ftiles + n.ptiles[k] - 1) / n.ptiles[k];
     }
     n.n_lk = c->nlk;
     n.n_mt = c->nmt;
@@ -156,10 +166,10 @@ DevNet<Real> make_devnet(MechContext* c) {
     n.planes = c->planes.as<double>();
     n.bb_k = c->bb_k.as<Real>();
     n.bb_slen = c->bb_slen.as<Real>();
-    n.n_stiles = c->n_stiles;
-    n.stile = c->stile.as<Tile>();
-    n.stile_kind = c->stile_kind.as<int>();
-    for (int k = 0; k < K_NUM_SPARSE; ++k) n.sp_tiles[k] = c->sp_tiles[k];
+    n.n_stiles = c->compact ? c->n_stiles_c : c->n_stiles;
+    n.stile = (c->compact ? c->stile_c : c->stile).as<Tile>();
+    n.stile_kind = (c->compact ? c->stile_kind_c : c->stile_kind).as<int>();
+    for (int k = 0; k < K_NUM_SPARSE; ++k) n.sp_tiles[k] = c->compact ? c->sp_tiles_c[k] : c->sp_tiles[k];
     n.contrib = c->contrib.as<Real>();
     for (int k = 0; k <= K_NUM_SPARSE; ++k) n.slot_base[k] = c->slot_base[k];
     n.csr_off = c->cb.off.as<int>();
@@ -174,7 +184,7 @@ DevNet<Real> make_devnet(MechContext* c) {
     n.part_fil = c->part_fil.as<double>();
     n.part_sp = c->part_sp.as<double>();
     n.st = c->st.as<CGState>();
-    n.rt = c->rt.as<RepTiles>();
+    n.rt = (c->compact ? c->rt_c : c->rt).as<RepTiles>();
     n.ticket = c->ticket.as<int>();
     n.gticket = c->gticket.as<int>();
     n.err = c->err.as<unsigned>();
@@ -281,6 +291,10 @@ const int* perm_of(MechContext* c, int r) { return c->perm_all.as<int>() + c->re
 // ===========================================================================
 // network upload
 // ===========================================================================
+// bytes past the last bead of the position and direction buffers: bulk copies
+// round bead ranges outward to 16-byte multiples and may read into it
+static constexpr size_t kBulkPad = 256;
+
 static int set_networks(MechContext* c, int R, const MechNetwork* nets) {
     if (R <= 0 || !nets) return set_err(MECH_ERR_ARG, "no networks");
     c->reps.assign(R, ReplicaHost());
@@ -432,7 +446,7 @@ static int set_networks(MechContext* c, int R, const MechNetwork* nets) {
         std::vector<int> id(nb);
         for (int i = 0; i < nb; ++i) id[i] = i;
         if ((rc = upload(ident, id, s))) return rc;
-        CU(c->x[0].ensure(sizeof(double) * x.size()));
+        CU(c->x[0].ensure(sizeof(double) * x.size() + kBulkPad));
         if (c->precision == MECH_PREC_FP64)
             k_scatter_coords<double><<<(nb + 255) / 256, 256, 0, s>>>(xd.as<double>(), ident.as<int>(), nb, 0, c->x[0].as<double>());
         else
@@ -440,17 +454,18 @@ static int set_networks(MechContext* c, int R, const MechNetwork* nets) {
         CU(cudaGetLastError());
         CU(cudaStreamSynchronize(s));
     }
-    CU(c->x[1].ensure(sizeof(double) * x.size()));
+    CU(c->x[1].ensure(sizeof(double) * x.size() + kBulkPad));
     CU(cudaMemcpyAsync(c->x[1].p, c->x[0].p, sizeof(double) * x.size(), cudaMemcpyDeviceToDevice, s));
     CU(c->xbest.ensure(sizeof(double) * x.size()));
     CU(c->xinit.ensure(sizeof(double) * x.size()));
     CU(cudaMemcpyAsync(c->xinit.p, c->x[0].p, sizeof(double) * x.size(), cudaMemcpyDeviceToDevice, s));
-    CU(c->f[0].ensure(rs * x.size()));
-    CU(c->f[1].ensure(rs * x.size()));
-    CU(c->d.ensure(rs * x.size()));
+    CU(c->f[0].ensure(rs * x.size() + kBulkPad));
+    CU(c->f[1].ensure(rs * x.size() + kBulkPad));
+    CU(c->d.ensure(rs * x.size() + kBulkPad));
     CU(cudaMemsetAsync(c->f[0].p, 0, rs * x.size(), s));
     CU(cudaMemsetAsync(c->f[1].p, 0, rs * x.size(), s));
     CU(cudaMemsetAsync(c->d.p, 0, rs * x.size(), s));
+    flags.resize((size_t)nb + 32, 0);   // tail padding read by 16-byte-rounded bulk copies
     if ((rc = upload(c->bflag, flags, s))) return rc;
     {
         std::vector<double> par(4 * (size_t)nb);
@@ -487,6 +502,8 @@ static int set_networks(MechContext* c, int R, const MechNetwork* nets) {
         c->h_rt[r].fil_end = (int)ft.size();
     }
     c->n_ftiles = (int)ft.size();
+    c->h_ftiles = ft;
+    c->compact = false;
     if ((rc = upload(c->ftile, ft, s))) return rc;
     CU(c->part_fil.ensure(sizeof(double) * 4 * ft.size()));
     // states
@@ -517,6 +534,26 @@ static int set_networks(MechContext* c, int R, const MechNetwork* nets) {
 // ===========================================================================
 // neighbor lists
 // ===========================================================================
+// Bring every replica's current coordinates to x[0] (a replica whose last
+// accepted step left them in x[1] is copied back) and reset its xbuf.
+static int canonicalize_x(MechContext* c) {
+    cudaStream_t s = c->stream;
+    CU(cudaMemcpyAsync(c->h_st, c->st.p, sizeof(CGState) * c->R, cudaMemcpyDeviceToHost, s));
+    CU(cudaStreamSynchronize(s));
+    bool moved = false;
+    for (int r = 0; r < c->R; ++r) {
+        if (c->h_st[r].xbuf) {
+            const ReplicaHost& h = c->reps[r];
+            CU(cudaMemcpyAsync(c->x[0].as<char>() + 24 * (size_t)h.bead_begin, c->x[1].as<char>() + 24 * (size_t)h.bead_begin,
+                               24 * (size_t)h.nb, cudaMemcpyDeviceToDevice, s));
+            c->h_st[r].xbuf = 0;
+            moved = true;
+        }
+    }
+    if (moved) CU(cudaMemcpyAsync(c->st.p, c->h_st, sizeof(CGState) * c->R, cudaMemcpyHostToDevice, s));
+    return MECH_OK;
+}
+
 static int rebuild(MechContext* c, double cell_req, MechListInfo* info) {
     if (!c->have_net) return set_err(MECH_ERR_STATE, "no network");
     cudaStream_t s = c->stream;
@@ -581,19 +618,7 @@ static int rebuild(MechContext* c, double cell_req, MechListInfo* info) {
     in.ncells = ncells;
     // Current coordinates live in x[xbuf] per replica; canonicalize them to
     // x[0] (and reset xbuf) so the lists read one array.
-    CU(cudaMemcpyAsync(c->h_st, c->st.p, sizeof(CGState) * R, cudaMemcpyDeviceToHost, s));
-    CU(cudaStreamSynchronize(s));
-    bool moved = false;
-    for (int r = 0; r < R; ++r) {
-        if (c->h_st[r].xbuf) {
-            const ReplicaHost& h = c->reps[r];
-            CU(cudaMemcpyAsync(c->x[0].as<char>() + 24 * (size_t)h.bead_begin, c->x[1].as<char>() + 24 * (size_t)h.bead_begin,
-                               24 * (size_t)h.nb, cudaMemcpyDeviceToDevice, s));
-            c->h_st[r].xbuf = 0;
-            moved = true;
-        }
-    }
-    if (moved) CU(cudaMemcpyAsync(c->st.p, c->h_st, sizeof(CGState) * R, cudaMemcpyHostToDevice, s));
+    if ((rc = canonicalize_x(c))) return rc;
     in.x = c->x[0].p;
     in.mixed = c->precision == MECH_PREC_MIXED;
     long long P = 0;
@@ -713,6 +738,9 @@ static int rebuild(MechContext* c, double cell_req, MechListInfo* info) {
             c->sp_tiles[k] = (int)st.size() - t0;
         }
         c->n_stiles = (int)st.size();
+        c->h_stiles = st;
+        c->h_skind = kind;
+        c->compact = false;
         if ((rc = upload(c->stile, st, s)) || (rc = upload(c->stile_kind, kind, s)) || (rc = upload(c->rt, c->h_rt, s)))
             return rc;
         CU(c->part_sp.ensure(sizeof(double) * std::max<size_t>(st.size(), 1)));
@@ -757,6 +785,15 @@ static int pull_states(MechContext* c) {
     CU(cudaStreamSynchronize(c->stream));
     return MECH_OK;
 }
+// Status of the device error word's bits (kernels set them with atomicOr).
+static int err_status(unsigned bits) {
+    if (bits & 32u) return set_err(MECH_ERR_ITER_LIMIT, "a bulk shared-memory copy did not complete in time");
+    if (bits & 16u) return set_err(MECH_ERR_CUDA, "a bulk shared-memory copy range was misaligned");
+    if (bits & 1u) return set_err(MECH_ERR_NONFINITE, "excluded-volume numeric fallback failed");
+    if (bits & 8u) return set_err(MECH_ERR_NONFINITE, "non-finite excluded-volume Hessian term");
+    return set_err(MECH_ERR_CAPACITY, "excluded-volume work list overflow");
+}
+
 static int push_states(MechContext* c) {
     CU(cudaMemcpyAsync(c->st.p, c->h_st, sizeof(CGState) * c->R, cudaMemcpyHostToDevice, c->stream));
     return MECH_OK;
@@ -768,6 +805,7 @@ static int eval_energy(MechContext* c, int replica) {
     if ((rc = pull_states(c))) return rc;
     for (int r = 0; r < c->R; ++r) c->h_st[r].active = (replica < 0 || r == replica);
     if ((rc = push_states(c))) return rc;
+    CU(cudaMemsetAsync(c->err.p, 0, sizeof(unsigned), c->stream));
     const DevNet<Real> n = make_devnet<Real>(c);
     c->timing.launches += launch_energy<Real>(n, -1, 0, c->stream);
     CU(cudaGetLastError());
@@ -780,6 +818,7 @@ static int eval_forces(MechContext* c, int replica) {
     if ((rc = pull_states(c))) return rc;
     for (int r = 0; r < c->R; ++r) c->h_st[r].active = (replica < 0 || r == replica);
     if ((rc = push_states(c))) return rc;
+    CU(cudaMemsetAsync(c->err.p, 0, sizeof(unsigned), c->stream));
     const DevNet<Real> n = make_devnet<Real>(c);
     c->timing.launches += launch_forces<Real>(n, -1, c->stream);
     CU(cudaGetLastError());
@@ -811,8 +850,49 @@ static int capture_iteration_graph(MechContext* c, cudaGraphExec_t* exec, int* n
     return MECH_OK;
 }
 
+// Tile lists of the replicas still minimizing (in the same order, with the
+// same per-replica tile counts, so tickets and partial slots work unchanged);
+// finished replicas get empty ranges.  The kernels' grids then cover only the
+// remaining work.
+static int compact_tiles(MechContext* c, const std::vector<char>& active) {
+    std::vector<Tile> ft, st;
+    std::vector<int> kind;
+    std::vector<RepTiles> rt(c->R, RepTiles{});
+    for (int r = 0; r < c->R; ++r) {
+        if (!active[r]) continue;
+        const RepTiles& full = c->h_rt[r];
+        rt[r].fil_begin = (int)ft.size();
+        ft.insert(ft.end(), c->h_ftiles.begin() + full.fil_begin, c->h_ftiles.begin() + full.fil_end);
+        rt[r].fil_end = (int)ft.size();
+    }
+    for (int k = 0; k < K_NUM_SPARSE; ++k) {
+        const int t0 = (int)st.size();
+        for (int r = 0; r < c->R; ++r) {
+            if (!active[r]) continue;
+            const RepTiles& full = c->h_rt[r];
+            rt[r].sp_begin[k] = (int)st.size();
+            st.insert(st.end(), c->h_stiles.begin() + full.sp_begin[k], c->h_stiles.begin() + full.sp_end[k]);
+            kind.insert(kind.end(), (size_t)(full.sp_end[k] - full.sp_begin[k]), k);
+            rt[r].sp_end[k] = (int)st.size();
+        }
+        c->sp_tiles_c[k] = (int)st.size() - t0;
+    }
+    int rc;
+    if ((rc = upload(c->ftile_c, ft, c->stream)) || (rc = upload(c->stile_c, st, c->stream)) ||
+        (rc = upload(c->stile_kind_c, kind, c->stream)) || (rc = upload(c->rt_c, rt, c->stream)))
+        return rc;
+    c->n_ftiles_c = (int)ft.size();
+    c->n_stiles_c = (int)st.size();
+    c->compact = true;
+    return MECH_OK;
+}
+
 template <typename Real>
 static int minimize_impl(MechContext* c, const MechCGParams* p, MechResult* res) {
+    struct FullTilesOnExit {
+        MechContext* c;
+        ~FullTilesOnExit() { c->compact = false; }
+    } full_tiles_on_exit{c};
     if (!c->have_lists) {
         int rc = rebuild(c, 0.0, nullptr);
         if (rc) return rc;
@@ -843,7 +923,8 @@ static int minimize_impl(MechContext* c, const MechCGParams* p, MechResult* res)
     }
     if ((rc = push_states(c))) return rc;
     CU(cudaMemsetAsync(c->err.p, 0, sizeof(unsigned), s));
-    const DevNet<Real> n = make_devnet<Real>(c);
+    c->compact = false;
+    DevNet<Real> n = make_devnet<Real>(c);
     cudaEvent_t e0, e1;
     CU(cudaEventCreate(&e0));
     CU(cudaEventCreate(&e1));
@@ -872,8 +953,7 @@ static int minimize_impl(MechContext* c, const MechCGParams* p, MechResult* res)
         launches += per_graph;
         if ((rc = pull_states(c))) { cudaGraphExecDestroy(exec); return rc; }
         if (*c->h_err) {
-            status = (*c->h_err & 1u) ? set_err(MECH_ERR_NONFINITE, "excluded-volume numeric fallback failed")
-                                      : set_err(MECH_ERR_CAPACITY, "excluded-volume work list overflow");
+            status = err_status(*c->h_err);
             break;
         }
         bool all_done = true, recover = false;
@@ -887,12 +967,32 @@ static int minimize_impl(MechContext* c, const MechCGParams* p, MechResult* res)
             launches += launch_recover<Real>(n, s);
             CU(cudaGetLastError());
         }
+        // batched runs: once the replicas still minimizing hold at most half
+        // of the tiles in the current lists, relaunch over theirs only
+        if (c->R > 1) {
+            std::vector<char> act(c->R, 0);
+            long long live = 0;
+            for (int r = 0; r < c->R; ++r) {
+                const int ph = c->h_st[r].phase;
+                act[r] = ph != PH_DONE && ph != PH_ERROR;
+                if (act[r]) live += c->h_rt[r].fil_end - c->h_rt[r].fil_begin;
+            }
+            if (2 * live <= (long long)n.n_ftiles) {
+                cudaGraphExecDestroy(exec);
+                exec = nullptr;
+                if ((rc = compact_tiles(c, act))) { c->compact = false; return rc; }
+                n = make_devnet<Real>(c);
+                if ((rc = capture_iteration_graph<Real>(c, &exec, &per_graph))) { c->compact = false; return rc; }
+            }
+        }
         if (graphs > max_graphs) {
             status = set_err(MECH_ERR_ITER_LIMIT, "minimizer loop exceeded its iteration cap");
             break;
         }
     }
-    cudaGraphExecDestroy(exec);
+    if (exec) cudaGraphExecDestroy(exec);
+    c->compact = false;   // the full lists again for energiesAfter and later calls
+    n = make_devnet<Real>(c);
     // call-limit exit restores the minimum-energy backup (CGMethod.hpp:1589-1610)
     bool restore = false;
     for (int r = 0; r < c->R; ++r) {
@@ -1083,6 +1183,7 @@ int32_t mech_energy(MechContext* ctx, int32_t r, const double* coord, double* pe
     if (!ctx->have_lists && (rc = rebuild(ctx, 0.0, nullptr))) return rc;
     rc = ctx->precision == MECH_PREC_FP64 ? eval_energy<double>(ctx, r) : eval_energy<float>(ctx, r);
     if (rc) return rc;
+    if (*ctx->h_err & (2u | 4u | 16u | 32u)) return err_status(*ctx->h_err);
     const CGState& S = ctx->h_st[r];
     if (per_ff)
         for (int k = 0; k < MECH_NUM_FF; ++k) per_ff[k] = S.eval[k];
@@ -1098,7 +1199,7 @@ int32_t mech_forces(MechContext* ctx, int32_t r, const double* coord, double* f_
     if (!ctx->have_lists && (rc = rebuild(ctx, 0.0, nullptr))) return rc;
     rc = ctx->precision == MECH_PREC_FP64 ? eval_forces<double>(ctx, r) : eval_forces<float>(ctx, r);
     if (rc) return rc;
-    if (*ctx->h_err) return set_err(MECH_ERR_NONFINITE, "excluded-volume numeric fallback failed");
+    if (*ctx->h_err) return err_status(*ctx->h_err);
     return f_out ? mech_get_forces(ctx, r, f_out) : MECH_OK;
 }
 
@@ -1183,6 +1284,262 @@ static int profile_impl(MechContext* c, int iters, MechProfile* o) {
     o->n_slots = c->slot_base[K_NUM_SPARSE];
     return pull_states(c);
 }
+
+// ===========================================================================
+// Hessian-vector products, implicit adjoint, Newton refinement (FP64 engine)
+// ===========================================================================
+namespace {
+
+// caller-order vector of replica r -> internal slots of a full-length vector
+__global__ void k_scatter_vec(const double* in, const int* perm, int nb, int base, double* out) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= nb) return;
+    const size_t j = 3 * (size_t)(base + perm[i]);
+    out[j] = in[3 * (size_t)i];
+    out[j + 1] = in[3 * (size_t)i + 1];
+    out[j + 2] = in[3 * (size_t)i + 2];
+}
+
+// x = x0 + alpha dx
+__global__ void k_axpy_from(double* x, const double* x0, double alpha, const double* dx, long long n) {
+    for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x)
+        x[i] = x0[i] + alpha * dx[i];
+}
+
+}  // namespace
+
+// the solver's work vectors (3 * nb doubles each) and scalars
+static int hvp_buffers(MechContext* c, HvpCgWork* w) {
+    const size_t v = sizeof(double) * 3 * (size_t)std::max(c->nb, 1);
+    CU(c->hv_a.ensure(v));
+    CU(c->hv_b.ensure(std::max(v, sizeof(double) * 2 * (size_t)std::max(c->nlk, 1))));
+    CU(c->cg_x.ensure(v));
+    CU(c->cg_r.ensure(v));
+    CU(c->cg_p.ensure(v));
+    CU(c->cg_Ap.ensure(v));
+    CU(c->cg_scal.ensure(sizeof(double) * 8));
+    CU(c->cg_part.ensure(sizeof(double) * 512));
+    CU(c->cg_ticket.ensure(sizeof(unsigned) * 4));
+    w->r = c->cg_r.as<double>();
+    w->p = c->cg_p.as<double>();
+    w->Ap = c->cg_Ap.as<double>();
+    w->scal = c->cg_scal.as<double>();
+    w->part = c->cg_part.as<double>();
+    w->ticket = c->cg_ticket.as<unsigned>();
+    return MECH_OK;
+}
+
+static int hvp_ready(MechContext* c) {
+    if (c->precision != MECH_PREC_FP64)
+        return set_err(MECH_ERR_STATE, "Hessian-vector products, adjoint and Newton solves need an FP64 context");
+    int rc;
+    if (!c->have_lists && (rc = rebuild(c, 0.0, nullptr))) return rc;
+    return canonicalize_x(c);
+}
+
+// caller-order host vector of replica r -> full internal-order device vector (zero elsewhere)
+static int put_replica_vec(MechContext* c, int r, const double* host, DeviceBuffer& dst) {
+    const ReplicaHost& h = c->reps[r];
+    cudaStream_t s = c->stream;
+    CU(cudaMemsetAsync(dst.p, 0, sizeof(double) * 3 * (size_t)c->nb, s));
+    CU(cudaMemcpyAsync(c->stage.p, host, sizeof(double) * 3 * h.nb, cudaMemcpyHostToDevice, s));
+    k_scatter_vec<<<(h.nb + 255) / 256, 256, 0, s>>>(c->stage.as<double>(), perm_of(c, r), h.nb, h.bead_begin,
+                                                      dst.as<double>());
+    CU(cudaGetLastError());
+    return MECH_OK;
+}
+
+static int get_replica_vec(MechContext* c, int r, const DeviceBuffer& src, double* host) {
+    const ReplicaHost& h = c->reps[r];
+    cudaStream_t s = c->stream;
+    k_gather_coords<double><<<(h.nb + 255) / 256, 256, 0, s>>>(src.as<double>(), perm_of(c, r), h.nb, h.bead_begin,
+                                                               c->stage.as<double>());
+    CU(cudaMemcpyAsync(host, c->stage.p, sizeof(double) * 3 * h.nb, cudaMemcpyDeviceToHost, s));
+    CU(cudaStreamSynchronize(s));
+    return MECH_OK;
+}
+
+static void fill_info(MechSolveInfo* info, const HvpCgResult& cr) {
+    if (!info) return;
+    info->iterations = cr.iterations;
+    info->converged = cr.converged;
+    info->rel_residual = cr.rel_residual;
+    info->launches = cr.launches;
+    info->negative_curvature = cr.negative_curvature;
+}
+
+extern "C" {
+
+int32_t mech_hvp(MechContext* ctx, int32_t r, int32_t mode, const double* v, double* hv) {
+    int rc = check_replica(ctx, r);
+    if (rc) return rc;
+    if (!v || !hv) return set_err(MECH_ERR_ARG, "null vector");
+    if (mode != MECH_HVP_ENERGY && mode != MECH_HVP_FORCE_JACOBIAN) return set_err(MECH_ERR_ARG, "bad mode");
+    CU(cudaSetDevice(ctx->device));
+    if ((rc = hvp_ready(ctx))) return rc;
+    HvpCgWork w{};
+    if ((rc = hvp_buffers(ctx, &w))) return rc;
+    if ((rc = put_replica_vec(ctx, r, v, ctx->hv_a))) return rc;
+    CU(cudaMemsetAsync(ctx->err.p, 0, sizeof(unsigned), ctx->stream));
+    const DevNet<double> n = make_devnet<double>(ctx);
+    ctx->timing.launches += launch_hvp(n, ctx->hv_a.as<double>(), ctx->hv_b.as<double>(), 0.0,
+                                       mode == MECH_HVP_FORCE_JACOBIAN, ctx->stream);
+    CU(cudaGetLastError());
+    if ((rc = get_replica_vec(ctx, r, ctx->hv_b, hv))) return rc;
+    if ((rc = pull_states(ctx))) return rc;
+    if (*ctx->h_err & 8u) return set_err(MECH_ERR_NONFINITE, "non-finite excluded-volume Hessian term");
+    return MECH_OK;
+}
+
+int32_t mech_set_linker_params(MechContext* ctx, int32_t r, const double* k, const double* eq_length) {
+    int rc = check_replica(ctx, r);
+    if (rc) return rc;
+    CU(cudaSetDevice(ctx->device));
+    const ReplicaHost& h = ctx->reps[r];
+    if (h.nlk == 0) return MECH_OK;
+    const size_t rs = real_size(ctx);
+    auto put = [&](DeviceBuffer& dst, const double* src) -> int {
+        if (!src) return MECH_OK;
+        if (ctx->precision == MECH_PREC_FP64) {
+            CU(cudaMemcpyAsync(dst.as<double>() + h.lk_begin, src, sizeof(double) * h.nlk, cudaMemcpyHostToDevice,
+                               ctx->stream));
+        } else {
+            std::vector<float> f(src, src + h.nlk);
+            CU(cudaMemcpyAsync(dst.as<float>() + h.lk_begin, f.data(), rs * h.nlk, cudaMemcpyHostToDevice, ctx->stream));
+            CU(cudaStreamSynchronize(ctx->stream));
+        }
+        return MECH_OK;
+    };
+    if ((rc = put(ctx->lk_k, k)) || (rc = put(ctx->lk_l0, eq_length))) return rc;
+    CU(cudaStreamSynchronize(ctx->stream));
+    return MECH_OK;
+}
+
+int32_t mech_adjoint(MechContext* ctx, int32_t r, const double* dL_dx, double dL_dE, const MechSolveParams* sp,
+                     double* dL_dk, double* dL_dl0, MechSolveInfo* info) {
+    int rc = check_replica(ctx, r);
+    if (rc) return rc;
+    if (!dL_dx || !sp || !dL_dk || !dL_dl0) return set_err(MECH_ERR_ARG, "null argument");
+    if (!(sp->rel_tol > 0) || sp->max_iter <= 0) return set_err(MECH_ERR_ARG, "bad solve parameters");
+    CU(cudaSetDevice(ctx->device));
+    if ((rc = hvp_ready(ctx))) return rc;
+    HvpCgWork w{};
+    if ((rc = hvp_buffers(ctx, &w))) return rc;
+    if ((rc = put_replica_vec(ctx, r, dL_dx, ctx->hv_a))) return rc;
+    CU(cudaMemsetAsync(ctx->err.p, 0, sizeof(unsigned), ctx->stream));
+    const DevNet<double> n = make_devnet<double>(ctx);
+    HvpCgResult cr{};
+    CU(hvp_cg_solve(n, ctx->hv_a.as<double>(), ctx->cg_x.as<double>(), w, sp->rel_tol, sp->max_iter, sp->shift,
+                    ctx->stream, &cr));
+    ctx->timing.launches += cr.launches;
+    fill_info(info, cr);
+    const ReplicaHost& h = ctx->reps[r];
+    if (h.nlk > 0) {
+        double* dk = ctx->hv_b.as<double>();
+        launch_linker_grad(n, h.lk_begin, h.nlk, ctx->cg_x.as<double>(), dL_dE, dk, dk + h.nlk, ctx->stream);
+        CU(cudaGetLastError());
+        CU(cudaMemcpyAsync(dL_dk, dk, sizeof(double) * h.nlk, cudaMemcpyDeviceToHost, ctx->stream));
+        CU(cudaMemcpyAsync(dL_dl0, dk + h.nlk, sizeof(double) * h.nlk, cudaMemcpyDeviceToHost, ctx->stream));
+    }
+    if ((rc = pull_states(ctx))) return rc;
+    if (*ctx->h_err & 8u) return set_err(MECH_ERR_NONFINITE, "non-finite excluded-volume Hessian term");
+    if (!cr.converged) return set_err(MECH_ERR_ITER_LIMIT, "adjoint CG did not reach its tolerance");
+    return MECH_OK;
+}
+
+int32_t mech_newton_refine(MechContext* ctx, int32_t max_steps, double force_tol, const MechSolveParams* sp,
+                           MechSolveInfo* info) {
+    if (!ctx || !sp) return set_err(MECH_ERR_ARG, "null argument");
+    if (!ctx->have_net) return set_err(MECH_ERR_STATE, "no network");
+    if (!(sp->rel_tol > 0) || sp->max_iter <= 0 || max_steps < 0 || !(sp->shift >= 0))
+        return set_err(MECH_ERR_ARG, "bad solve parameters");
+    CU(cudaSetDevice(ctx->device));
+    int rc;
+    if ((rc = hvp_ready(ctx))) return rc;
+    HvpCgWork w{};
+    if ((rc = hvp_buffers(ctx, &w))) return rc;
+    cudaStream_t s = ctx->stream;
+    const long long N = 3LL * ctx->nb;
+    HvpCgResult total{};
+    int steps = 0;
+    // max |F| and total energy over the replicas at x[0]
+    auto evaluate = [&](double* m, double* e) -> int {
+        int r2;
+        if ((r2 = eval_energy<double>(ctx, -1))) return r2;
+        double E = 0.0;
+        for (int r = 0; r < ctx->R; ++r) E += ctx->h_st[r].eval[MECH_NUM_FF];
+        if ((r2 = eval_forces<double>(ctx, -1))) return r2;
+        if (*ctx->h_err) return err_status(*ctx->h_err);
+        double v = 0.0;
+        for (int r = 0; r < ctx->R; ++r) v = std::max(v, ctx->h_st[r].maxF);
+        *m = v;
+        *e = E;
+        return MECH_OK;
+    };
+    double maxF = 0.0, E = 0.0;
+    if ((rc = evaluate(&maxF, &E))) return rc;
+    // Levenberg-Marquardt damped Newton: dx = (H + mu I)^-1 F; mu grows tenfold
+    // when a solve meets non-positive curvature or no step length helps, and
+    // shrinks tenfold after an accepted step.  A step x + alpha dx (alpha
+    // halved from 1) is accepted when the energy drops or max |F| halves.
+    double mu = sp->shift;
+    constexpr double kMuFloor = 1e-6;   // pN/nm, first damping when mu starts at 0
+    while (maxF >= force_tol && steps < max_steps) {
+        for (int r = 0; r < ctx->R; ++r) {
+            const ReplicaHost& h = ctx->reps[r];
+            CU(cudaMemcpyAsync(ctx->hv_a.as<double>() + 3 * (size_t)h.bead_begin,
+                               ctx->f[ctx->h_st[r].fbuf].as<double>() + 3 * (size_t)h.bead_begin,
+                               sizeof(double) * 3 * h.nb, cudaMemcpyDeviceToDevice, s));
+        }
+        CU(cudaMemcpyAsync(ctx->hv_b.p, ctx->x[0].p, sizeof(double) * N, cudaMemcpyDeviceToDevice, s));
+        bool accepted = false;
+        double trialF = 0.0, trialE = 0.0;
+        for (int attempt = 0; attempt < 16 && !accepted; ++attempt) {
+            const DevNet<double> n = make_devnet<double>(ctx);
+            HvpCgResult cr{};
+            CU(hvp_cg_solve(n, ctx->hv_a.as<double>(), ctx->cg_x.as<double>(), w, sp->rel_tol, sp->max_iter, mu, s,
+                            &cr));
+            total.iterations += cr.iterations;
+            total.launches += cr.launches;
+            total.rel_residual = cr.rel_residual;
+            total.converged = cr.converged;
+            total.negative_curvature |= cr.negative_curvature;
+            if (!cr.negative_curvature) {
+                double alpha = 1.0;
+                for (int t = 0; t < 30; ++t, alpha *= 0.5) {
+                    k_axpy_from<<<304, 256, 0, s>>>(ctx->x[0].as<double>(), ctx->hv_b.as<double>(), alpha,
+                                                    ctx->cg_x.as<double>(), N);
+                    CU(cudaGetLastError());
+                    rc = evaluate(&trialF, &trialE);
+                    if (rc && rc != MECH_ERR_NONFINITE) return rc;
+                    if (rc == MECH_OK && (trialE < E || trialF < 0.5 * maxF)) {
+                        accepted = true;
+                        break;
+                    }
+                }
+            }
+            if (!accepted) mu = std::max(10.0 * mu, kMuFloor);
+        }
+        ++steps;
+        if (!accepted) {   // no progress even with strong damping: restore and stop
+            CU(cudaMemcpyAsync(ctx->x[0].p, ctx->hv_b.p, sizeof(double) * N, cudaMemcpyDeviceToDevice, s));
+            if ((rc = evaluate(&maxF, &E))) return rc;
+            break;
+        }
+        maxF = trialF;
+        E = trialE;
+        mu = mu < 10.0 * kMuFloor ? 0.0 : 0.1 * mu;
+    }
+    ctx->timing.launches += total.launches;
+    fill_info(info, total);
+    if (info) {
+        info->newton_steps = steps;
+        info->max_force = maxF;
+    }
+    return MECH_OK;
+}
+
+}  // extern "C"
 
 extern "C" {
 

@@ -187,6 +187,29 @@ int set_error_text(int code, const std::string& msg);
 template <typename Real> int launch_exvol_energy(const DevNet<Real>& n, int want, int trial, cudaStream_t s);
 template <typename Real> int launch_exvol_forces(const DevNet<Real>& n, int want, cudaStream_t s);
 
+// ---- Hessian-vector products and solves (mech_hvp.cu, FP64 engine) --------
+// hv = (H + shift I) v at the positions in x[0], v and hv in internal bead
+// order; H is the energy's Hessian, or with `jacobian` minus the Jacobian of
+// the force routine (which moves nearly coplanar excluded-volume pairs)
+int launch_hvp(const DevNet<double>& n, const double* v, double* hv, double shift, bool jacobian, cudaStream_t s);
+struct HvpCgWork {
+    double* r; double* p; double* Ap;   // [3 * nb] each
+    double* scal;                        // [8]: r.r, p.Ap, new r.r, b.b, curvature flag
+    double* part;                        // [304] per-block partial sums
+    unsigned* ticket;
+};
+struct HvpCgResult {
+    int iterations, converged, negative_curvature;
+    double rel_residual;
+    long long launches;
+};
+// (H + shift I) x = b by conjugate gradients from x = 0, to |r| <= rel_tol |b|
+cudaError_t hvp_cg_solve(const DevNet<double>& n, const double* b, double* x, const HvpCgWork& w, double rel_tol,
+                         int max_iter, double shift, cudaStream_t s, HvpCgResult* res);
+// adjoint gradient of linkers [lk0, lk0 + nlk) from the adjoint solution lambda
+void launch_linker_grad(const DevNet<double>& n, int lk0, int nlk, const double* lambda, double wE, double* dk,
+                        double* dl0, cudaStream_t s);
+
 struct DeviceBuffer {
     void* p = nullptr;
     size_t bytes = 0;

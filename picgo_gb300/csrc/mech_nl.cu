@@ -401,7 +401,8 @@ cudaError_t build_csr(const CsrInput& in, CsrBuild& cb, cudaStream_t s) {
     const int ns = in.base[4];
     if ((e = cb.cnt.ensure(sizeof(int) * (size_t)(in.nb + 1))) != cudaSuccess) return e;
     if ((e = cb.cursor.ensure(sizeof(int) * (size_t)(in.nb + 1))) != cudaSuccess) return e;
-    if ((e = cb.off.ensure(sizeof(int) * (size_t)(in.nb + 1))) != cudaSuccess) return e;
+    // offsets padded for bulk copies that round their ranges up to 16 bytes
+    if ((e = cb.off.ensure(sizeof(int) * (size_t)(in.nb + 1) + 64)) != cudaSuccess) return e;
     if ((e = cb.slots.ensure(sizeof(int) * (size_t)(ns > 0 ? ns : 1))) != cudaSuccess) return e;
     if ((e = cb.pos.ensure(sizeof(int) * (size_t)(ns > 0 ? ns : 1))) != cudaSuccess) return e;
     cudaMemsetAsync(cb.cnt.p, 0, sizeof(int) * (size_t)(in.nb + 1), s);

@@ -14,7 +14,8 @@ from typing import Sequence
 import numpy as np
 
 from . import _lib
-from ._lib import MechCGParams, MechListInfo, MechNetwork, MechProfile, MechResult, MechTiming, check
+from ._lib import (MechCGParams, MechListInfo, MechNetwork, MechProfile, MechResult, MechSolveInfo, MechSolveParams,
+                   MechTiming, check)
 
 _dp = C.POINTER(C.c_double)
 _i32p = C.POINTER(C.c_int32)
@@ -179,6 +180,42 @@ class Engine:
 
     def reset_coords(self) -> None:
         check(self._L.mech_reset_coords(self._ctx))
+
+    # -- second order (FP64 contexts) -----------------------------------------
+    def hvp(self, v: np.ndarray, replica: int = 0, jacobian: bool = False) -> np.ndarray:
+        """H v at the current coordinates (caller bead order): the energy's Hessian,
+        or with ``jacobian`` minus the Jacobian of the force routine."""
+        x = np.ascontiguousarray(v, dtype=np.float64).reshape(-1)
+        out = np.empty((self.nbeads[replica], 3))
+        check(self._L.mech_hvp(self._ctx, replica, 1 if jacobian else 0, _ptr(x, _dp), _ptr(out, _dp)))
+        return out
+
+    def set_linker_params(self, k=None, l0=None, replica: int = 0) -> None:
+        kk = None if k is None else np.ascontiguousarray(k, dtype=np.float64)
+        ll = None if l0 is None else np.ascontiguousarray(l0, dtype=np.float64)
+        check(self._L.mech_set_linker_params(self._ctx, replica, _ptr(kk, _dp), _ptr(ll, _dp)))
+
+    def adjoint(self, dL_dx: np.ndarray, dL_dE: float = 0.0, rel_tol: float = 1e-10, max_iter: int = 20000,
+                shift: float = 0.0, replica: int = 0):
+        """(dL/dk, dL/dl0, info) per linker at the current (equilibrium) coordinates."""
+        g = np.ascontiguousarray(dL_dx, dtype=np.float64).reshape(-1)
+        n = self.nlinkers[replica]
+        dk = np.zeros(n)
+        dl = np.zeros(n)
+        sp = MechSolveParams(rel_tol, max_iter, shift)
+        info = MechSolveInfo()
+        rc = self._L.mech_adjoint(self._ctx, replica, _ptr(g, _dp), float(dL_dE), C.byref(sp), _ptr(dk, _dp),
+                                  _ptr(dl, _dp), C.byref(info))
+        if rc not in (_lib.MECH_OK, -6):
+            check(rc)
+        return dk, dl, info.as_dict()
+
+    def newton_refine(self, max_steps: int = 20, force_tol: float = 1e-9, rel_tol: float = 1e-8,
+                      max_iter: int = 20000, shift: float = 0.0) -> dict:
+        sp = MechSolveParams(rel_tol, max_iter, shift)
+        info = MechSolveInfo()
+        check(self._L.mech_newton_refine(self._ctx, int(max_steps), float(force_tol), C.byref(sp), C.byref(info)))
+        return info.as_dict()
 
     def profile(self, iters: int = 20) -> dict:
         p = MechProfile()
