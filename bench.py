@@ -128,6 +128,7 @@ def run_ours(args, rank, world, dist):
 
     eng = Engine(args.precision, local)
     eng.set_network(net)
+    tuning = eng.autotune()   # launch geometry and bin edge, outside the timed region
 
     def step():
         eng.reset_coords()
@@ -218,7 +219,8 @@ def run_ours(args, rank, world, dist):
         "config": {"workload": "20,000 filaments x 50 cylinders (1M cylinders), 50k linkers, 5k motors, 10 um box",
                    "seed": SEED, "precision": args.precision, "cg": "Polak-Ribiere, backtracking, gradTol 1 pN, "
                    "maxDist 1, lambdaMax 0.01, energyRelTol 0 (run to 1 pN)",
-                   "l2": "flushed (256 MB write) between timed steps", "parallelism": f"replicas x{world}"},
+                   "l2": "flushed (256 MB write) between timed steps", "parallelism": f"replicas x{world}",
+                   "tuning": {k: (round(v, 4) if isinstance(v, float) else v) for k, v in tuning.items()}},
         "time_to_1pN_s": round(ms_per_step / 1e3, 4),
         "cg_iterations": results[-1]["num_iter"], "force_calls_per_step": results[-1]["num_force_call"],
         "final_max_force_pN": results[-1]["grad_inf_norm"],
@@ -242,6 +244,7 @@ def fp64_compare(args, net):
     from picgo_gb300 import Engine
     eng = Engine("fp64", int(os.environ.get("LOCAL_RANK", "0")))
     eng.set_network(net)
+    eng.autotune()
     eng.rebuild()
     r0 = eng.minimize(cg(energy_call_limit=200))[0]   # warm-up
     eng.reset_coords()

@@ -254,6 +254,27 @@ typedef struct MechProfile {
 int32_t mech_profile(MechContext* ctx, int32_t iters, MechProfile* out);
 
 /*
+ * Autotuner: times the candidate launch geometries of this context's kernels
+ * on its own networks and keeps the fastest (CUDA events; the neighbor-list
+ * bin edge by wall time of a rebuild, since any edge >= rMax gives the same
+ * pair list).  Results are cached per network shape for the process; a later
+ * context of the same shape reuses them unless MECH_TUNE_FORCE is given.  No
+ * reference counterpart (MEDYAN fixes its bin size in the input file).
+ */
+#define MECH_TUNE_KERNELS  1   /* tiles per block of the mixed filament kernels */
+#define MECH_TUNE_CELL     2   /* neighbor-list bin edge (scale of the default) */
+#define MECH_TUNE_FORCE    4   /* ignore the cache */
+typedef struct MechTuning {
+    int32_t energy_tiles_per_block;
+    int32_t force_tiles_per_block;
+    double cell_scale;              /* multiplier on the default bin edge */
+    double ms_energy, ms_force;     /* best filament-kernel times found (ms) */
+    double ms_rebuild;              /* best rebuild wall time found (ms) */
+} MechTuning;
+int32_t mech_autotune(MechContext* ctx, int32_t flags, MechTuning* out);
+int32_t mech_set_tuning(MechContext* ctx, const MechTuning* t);
+
+/*
  * Second-order calls (FP64 contexts; a mixed context returns MECH_ERR_STATE).
  * They replace ForceFieldManager::computeHessian's finite-difference Hessian
  * (Mechanics/ForceField/ForceFieldManager.cpp:354-489) with exact

@@ -33,7 +33,7 @@ EXPORTS = [
     "mech_set_coords", "mech_get_coords", "mech_rebuild_neighbors", "mech_get_pairs", "mech_energy",
     "mech_forces", "mech_minimize", "mech_get_forces", "mech_get_stretch_forces", "mech_get_timing",
     "mech_reset_coords", "mech_profile", "mech_filament_energy_device", "mech_hvp", "mech_set_linker_params",
-    "mech_adjoint", "mech_newton_refine",
+    "mech_adjoint", "mech_newton_refine", "mech_autotune", "mech_set_tuning",
 ]
 
 
@@ -108,6 +108,12 @@ class MechSolveInfo(C.Structure):
         return {k: getattr(self, k) for k, _ in self._fields_}
 
 
+class MechTuning(C.Structure):
+    _fields_ = [("energy_tiles_per_block", C.c_int32), ("force_tiles_per_block", C.c_int32),
+                ("cell_scale", C.c_double), ("ms_energy", C.c_double), ("ms_force", C.c_double),
+                ("ms_rebuild", C.c_double)]
+
+
 _lock = threading.Lock()
 _lib = None
 
@@ -150,6 +156,8 @@ def load(build_if_missing: bool = False):
         L.mech_profile.argtypes = [vp, C.c_int32, C.POINTER(MechProfile)]
         L.mech_filament_energy_device.argtypes = [C.c_int32, C.c_int32, vp, vp, vp, vp, vp, vp, vp, vp]
         L.mech_hvp.argtypes = [vp, C.c_int32, C.c_int32, _dp, _dp]
+        L.mech_autotune.argtypes = [vp, C.c_int32, C.POINTER(MechTuning)]
+        L.mech_set_tuning.argtypes = [vp, C.POINTER(MechTuning)]
         L.mech_set_linker_params.argtypes = [vp, C.c_int32, _dp, _dp]
         L.mech_adjoint.argtypes = [vp, C.c_int32, _dp, C.c_double, C.POINTER(MechSolveParams), _dp, _dp,
                                    C.POINTER(MechSolveInfo)]

@@ -29,11 +29,14 @@ def main(argv=None):
     ap.add_argument("--evals", type=int, default=0, help="profile mode: launches per evaluation kernel")
     ap.add_argument("--forces", type=int, default=0, help="only this many mech_forces calls")
     ap.add_argument("--energies", type=int, default=0, help="only this many mech_energy calls")
+    ap.add_argument("--autotune", action="store_true", help="run the autotuner first")
     args = ap.parse_args(argv)
     net = make_network(args.workload, seed=args.seed)
     out = {"workload": args.workload, "precision": args.precision, "n_beads": net.n_beads}
     with Engine(args.precision) as eng:
         eng.set_network(net)
+        if args.autotune:
+            out["tuning"] = eng.autotune()
         out["lists"] = eng.rebuild()
         if args.forces > 0 or args.energies > 0:
             for _ in range(args.forces):

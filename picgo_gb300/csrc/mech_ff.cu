@@ -444,17 +444,34 @@ __device__ __forceinline__ StageRange stage_range(int tb, int te, int nb, int ha
     return r;
 }
 
-// Issue the copies of tile ti into stage `st` (thread 0).  A range that fails
+// A block's tile descriptors, read once at kernel start (one thread per tile)
+// so the producing thread issues copies without chasing global pointers:
+// (begin, end, replica, bits) with bit 0 = selected by this launch, bit 1 =
+// xbuf, bit 2 = fbuf of the tile's replica, plus that replica's lambda.  A
+// replica's state cannot change while this block still holds unprocessed
+// tiles of it (its finalizer waits for every tile), so the copies stay valid.
+constexpr int kBulkMaxTiles = kFilBulkMaxTiles;
+
+__device__ __forceinline__ void load_descriptors(const DevNet<float>& n, int t0, int nt, int want, int4* desc,
+                                                 float* lf) {
+    for (int k = threadIdx.x; k < nt; k += blockDim.x) {
+        const Tile t = n.ftile[t0 + k];
+        const CGState& S = n.st[t.replica];
+        desc[k] = make_int4(t.begin, t.end, t.replica,
+                            (replica_selected(S, want) ? 1 : 0) | (S.xbuf << 1) | (S.fbuf << 2));
+        lf[k] = (float)S.lambda;
+    }
+}
+
+// Issue the copies of a tile into stage `st` (thread 0).  A range that fails
 // the alignment check is not copied: the barrier is completed without it and
 // the error word records it.
-__device__ void issue_energy_stage(const DevNet<float>& n, int ti, bool tr, EnergyStage* st, uint64_t* bar) {
-    const Tile t = n.ftile[ti];
-    const CGState& S = n.st[t.replica];
-    const float* X = n.x[S.xbuf];
-    const StageRange rg = stage_range(t.begin, t.end, n.nb, 1);
-    const void* src[4] = {X + 6 * (size_t)rg.xs, n.bpar + 4 * (size_t)t.begin, n.d + 3 * (size_t)rg.ds, n.bflag + rg.fs};
+__device__ void issue_energy_stage(const DevNet<float>& n, int4 t, bool tr, EnergyStage* st, uint64_t* bar) {
+    const float* X = n.x[(t.w >> 1) & 1];
+    const StageRange rg = stage_range(t.x, t.y, n.nb, 1);
+    const void* src[4] = {X + 6 * (size_t)rg.xs, n.bpar + 4 * (size_t)t.x, n.d + 3 * (size_t)rg.ds, n.bflag + rg.fs};
     void* dst[4] = {st->x, st->par, st->d, st->flag};
-    const unsigned bytes[4] = {24u * (unsigned)(rg.xe - rg.xs), 16u * (unsigned)(t.end - t.begin),
+    const unsigned bytes[4] = {24u * (unsigned)(rg.xe - rg.xs), 16u * (unsigned)(t.y - t.x),
                                tr ? 12u * (unsigned)(rg.de - rg.ds) : 0u, (unsigned)(rg.fe - rg.fs)};
     unsigned total = 0;
     bool ok = true;
@@ -474,29 +491,33 @@ __device__ void issue_energy_stage(const DevNet<float>& n, int ti, bool tr, Ener
         if (bytes[k]) bulk_copy_g2s(dst[k], src[k], bytes[k], bar);
 }
 
-__device__ __forceinline__ bool tile_selected(const DevNet<float>& n, int ti, int want) {
-    return replica_selected(n.st[n.ftile[ti].replica], want);
-}
-
 __global__ void __launch_bounds__(kBlock) k_fil_energy_bulk(DevNet<float> n, int want, int trial) {
     __shared__ EnergyStage stage[kBulkStages];
     __shared__ __align__(8) uint64_t bar[kBulkStages];
+    __shared__ int4 s_desc[kBulkMaxTiles];
+    __shared__ float s_lf[kBulkMaxTiles];
     __shared__ double sh[32 * MECH_NUM_FF];
     __shared__ int s_flag, s_abort;
     const int t0 = blockIdx.x * n.ptiles[0], t1 = min(t0 + n.ptiles[0], n.n_ftiles);
+    const int nt = t1 - t0;
     const bool tr = trial != 0;
     if (threadIdx.x == 0) {
         for (int k = 0; k < kBulkStages; ++k) mbar_init(&bar[k], 1);
         mbar_init_fence();
         s_abort = 0;
     }
+    if (nt > kBulkMaxTiles) {   // the launch geometry caps tiles per block; refuse rather than overrun
+        if (threadIdx.x == 0) atomicOr(n.err, 16u);
+        return;
+    }
+    load_descriptors(n, t0, nt, want, s_desc, s_lf);
     __syncthreads();
     // producer state (thread 0): next tile to consider, copies issued
-    int pi = t0, issued = 0;
+    int pi = 0, issued = 0;
     if (threadIdx.x == 0) {
-        for (; pi < t1 && issued < kBulkStages; ++pi)
-            if (tile_selected(n, pi, want)) {
-                issue_energy_stage(n, pi, tr, &stage[issued % kBulkStages], &bar[issued % kBulkStages]);
+        for (; pi < nt && issued < kBulkStages; ++pi)
+            if (s_desc[pi].w & 1) {
+                issue_energy_stage(n, s_desc[pi], tr, &stage[issued % kBulkStages], &bar[issued % kBulkStages]);
                 ++issued;
             }
     }
@@ -505,22 +526,21 @@ __global__ void __launch_bounds__(kBlock) k_fil_energy_bulk(DevNet<float> n, int
     float lf = 0.f;
     FF es, eb;
     const int ops[2] = {0, 0};
-    for (int ti = t0; ti < t1; ++ti) {
-        const Tile t = n.ftile[ti];
-        if (t.replica != cur) {
+    for (int k = 0; k < nt; ++k) {
+        const int4 t = s_desc[k];
+        if (t.z != cur) {
             if (cnt) {
                 double w[2] = {warp_sum_pair(es), warp_sum_pair(eb)};
                 if (flush_run<2>(n, cur, first, cnt, w, ops, sh, &s_flag)) finalize_energy(n, cur, trial, sh);
             }
-            cur = t.replica;
-            first = ti;
+            cur = t.z;
+            first = t0 + k;
             cnt = 0;
             es = FF();
             eb = FF();
-            const CGState& S = n.st[cur];
-            go = replica_selected(S, want);
-            xb = S.xbuf;
-            lf = (float)S.lambda;
+            go = t.w & 1;
+            xb = (t.w >> 1) & 1;
+            lf = s_lf[k];
         }
         if (!go) continue;
         ++cnt;
@@ -530,9 +550,9 @@ __global__ void __launch_bounds__(kBlock) k_fil_energy_bulk(DevNet<float> n, int
             s_abort = 1;
         }
         const EnergyStage& S = stage[sidx];
-        const int b = t.begin + threadIdx.x;
-        if (b < t.end) {
-            const StageRange rg = stage_range(t.begin, t.end, n.nb, 1);
+        const int b = t.x + threadIdx.x;
+        if (b < t.y) {
+            const StageRange rg = stage_range(t.x, t.y, n.nb, 1);
             const int fl = S.flag[b - rg.fs];
             Pos<float> p0 = load_pos(S.x, b - rg.xs);
             Pos<float> pp = fl & 1 ? load_pos(S.x, b + 1 - rg.xs) : p0;
@@ -543,7 +563,7 @@ __global__ void __launch_bounds__(kBlock) k_fil_energy_bulk(DevNet<float> n, int
                 if (fl & 2) pm = moved_f(pm, S.d, b - 1 - rg.ds, lf);
                 store_pos(n.x[xb ^ 1], b, p0);   // materialize the owned trial position
             }
-            const float4 pr = S.par[b - t.begin];
+            const float4 pr = S.par[b - t.x];
             if (fl & 1) {
                 float r2[3];
                 pdiff(pp, p0, r2);
@@ -559,9 +579,9 @@ __global__ void __launch_bounds__(kBlock) k_fil_energy_bulk(DevNet<float> n, int
         __syncthreads();   // stage sidx fully read
         if (s_abort) break;
         if (threadIdx.x == 0) {
-            for (; pi < t1; ++pi)
-                if (tile_selected(n, pi, want)) {
-                    issue_energy_stage(n, pi, tr, &stage[issued % kBulkStages], &bar[issued % kBulkStages]);
+            for (; pi < nt; ++pi)
+                if (s_desc[pi].w & 1) {
+                    issue_energy_stage(n, s_desc[pi], tr, &stage[issued % kBulkStages], &bar[issued % kBulkStages]);
                     ++issued;
                     ++pi;
                     break;
@@ -621,12 +641,10 @@ __device__ __forceinline__ ForceRange force_range(int tb, int te, int nb) {
     return r;
 }
 
-__device__ void issue_force_stage(const DevNet<float>& n, int ti, ForceStage* st, uint64_t* bar) {
-    const Tile t = n.ftile[ti];
-    const CGState& S = n.st[t.replica];
-    const float* X = n.x[S.xbuf];
-    const float* Fp = n.f[S.fbuf];
-    const ForceRange rg = force_range(t.begin, t.end, n.nb);
+__device__ void issue_force_stage(const DevNet<float>& n, int4 t, ForceStage* st, uint64_t* bar) {
+    const float* X = n.x[(t.w >> 1) & 1];
+    const float* Fp = n.f[(t.w >> 2) & 1];
+    const ForceRange rg = force_range(t.x, t.y, n.nb);
     const void* src[5] = {X + 6 * (size_t)rg.xs, n.bpar + 4 * (size_t)rg.ps, Fp + 3 * (size_t)rg.qs, n.csr_off + rg.cs,
                           n.bflag + rg.fs};
     void* dst[5] = {st->x, st->par, st->fp, st->csr, st->flag};
@@ -654,20 +672,28 @@ __device__ void issue_force_stage(const DevNet<float>& n, int ti, ForceStage* st
 __global__ void __launch_bounds__(kBlock) k_fil_force_bulk(DevNet<float> n, int want) {
     __shared__ ForceStage stage[kBulkStages];
     __shared__ __align__(8) uint64_t bar[kBulkStages];
+    __shared__ int4 s_desc[kBulkMaxTiles];
+    __shared__ float s_lf[kBulkMaxTiles];
     __shared__ double sh[32 * 3];
     __shared__ int s_flag, s_abort;
     const int t0 = blockIdx.x * n.ptiles[1], t1 = min(t0 + n.ptiles[1], n.n_ftiles);
+    const int nt = t1 - t0;
     if (threadIdx.x == 0) {
         for (int k = 0; k < kBulkStages; ++k) mbar_init(&bar[k], 1);
         mbar_init_fence();
         s_abort = 0;
     }
+    if (nt > kBulkMaxTiles) {   // the launch geometry caps tiles per block; refuse rather than overrun
+        if (threadIdx.x == 0) atomicOr(n.err, 16u);
+        return;
+    }
+    load_descriptors(n, t0, nt, want, s_desc, s_lf);
     __syncthreads();
-    int pi = t0, issued = 0;
+    int pi = 0, issued = 0;
     if (threadIdx.x == 0) {
-        for (; pi < t1 && issued < kBulkStages; ++pi)
-            if (tile_selected(n, pi, want)) {
-                issue_force_stage(n, pi, &stage[issued % kBulkStages], &bar[issued % kBulkStages]);
+        for (; pi < nt && issued < kBulkStages; ++pi)
+            if (s_desc[pi].w & 1) {
+                issue_force_stage(n, s_desc[pi], &stage[issued % kBulkStages], &bar[issued % kBulkStages]);
                 ++issued;
             }
     }
@@ -676,22 +702,21 @@ __global__ void __launch_bounds__(kBlock) k_fil_force_bulk(DevNet<float> n, int 
     float mx = 0.f;
     FF ff, ffp;
     const int ops[3] = {1, 0, 0};
-    for (int ti = t0; ti < t1; ++ti) {
-        const Tile t = n.ftile[ti];
-        if (t.replica != cur) {
+    for (int k = 0; k < nt; ++k) {
+        const int4 t = s_desc[k];
+        if (t.z != cur) {
             if (cnt) {
                 double w[3] = {warp_max_lane0(mx), warp_sum_pair(ff), warp_sum_pair(ffp)};
                 if (flush_run<3>(n, cur, first, cnt, w, ops, sh, &s_flag)) finalize_force(n, cur, sh);
             }
-            cur = t.replica;
-            first = ti;
+            cur = t.z;
+            first = t0 + k;
             cnt = 0;
             mx = 0.f;
             ff = FF();
             ffp = FF();
-            const CGState& S = n.st[cur];
-            go = replica_selected(S, want);
-            fb = S.fbuf;
+            go = t.w & 1;
+            fb = (t.w >> 2) & 1;
         }
         if (!go) continue;
         ++cnt;
@@ -701,9 +726,9 @@ __global__ void __launch_bounds__(kBlock) k_fil_force_bulk(DevNet<float> n, int 
             s_abort = 1;
         }
         const ForceStage& S = stage[sidx];
-        const int b = t.begin + threadIdx.x;
-        if (b < t.end) {
-            const ForceRange rg = force_range(t.begin, t.end, n.nb);
+        const int b = t.x + threadIdx.x;
+        if (b < t.y) {
+            const ForceRange rg = force_range(t.x, t.y, n.nb);
             const int f0 = S.flag[b - rg.fs];
             const int fm = (f0 & 2) ? S.flag[b - 1 - rg.fs] : 0;
             const int fp = (f0 & 1) ? S.flag[b + 1 - rg.fs] : 0;
@@ -765,9 +790,9 @@ __global__ void __launch_bounds__(kBlock) k_fil_force_bulk(DevNet<float> n, int 
         __syncthreads();   // stage sidx fully read
         if (s_abort) break;
         if (threadIdx.x == 0) {
-            for (; pi < t1; ++pi)
-                if (tile_selected(n, pi, want)) {
-                    issue_force_stage(n, pi, &stage[issued % kBulkStages], &bar[issued % kBulkStages]);
+            for (; pi < nt; ++pi)
+                if (s_desc[pi].w & 1) {
+                    issue_force_stage(n, s_desc[pi], &stage[issued % kBulkStages], &bar[issued % kBulkStages]);
                     ++issued;
                     ++pi;
                     break;

@@ -9,6 +9,7 @@
 #include <cstdio>
 #include <cstring>
 #include <limits>
+#include <map>
 #include <mutex>
 #include <string>
 #include <vector>
@@ -96,6 +97,10 @@ struct MechContext {
     DeviceBuffer ftile_c, stile_c, stile_kind_c, rt_c;
     bool compact = false;
     int n_ftiles_c = 0, n_stiles_c = 0;
+    // tuning (mech_autotune): tiles per block of the mixed filament energy and
+    // force kernels, and a multiplier on the default neighbor-list bin edge
+    int tile_cap[2] = {kFilBulkMaxTiles, kFilBulkMaxTiles};
+    double cell_scale = 1.0;
     int sp_tiles_c[K_NUM_SPARSE] = {0, 0, 0, 0};
     int slot_base[K_NUM_SPARSE + 1] = {0, 0, 0, 0, 0};
     std::vector<RepTiles> h_rt;
@@ -141,6 +146,8 @@ DevNet<Real> make_devnet(MechContext* c) {
     for (int k = 0; k < 3; ++k) {
         n.pgrid[k] = std::max(1, std::min(n.n_ftiles, persistent_blocks(c->device, k)));
         n.ptiles[k] = (n.n_ftiles + n.pgrid[k] - 1) / n.pgrid[k];
+        // the bulk-staged energy/force kernels keep a block's tile descriptors in shared memory
+        if (k < 2) n.ptiles[k] = std::max(1, std::min(n.ptiles[k], c->tile_cap[k]));
         n.pgrid[k] = (n.n_ftiles + n.ptiles[k] - 1) / n.ptiles[k];
     }
     n.n_lk = c->nlk;
@@ -569,7 +576,7 @@ static int rebuild(MechContext* c, double cell_req, MechListInfo* info) {
         const double vol = std::max(1.0, h.box[0] * h.box[1] * h.box[2]);
         if (cell <= 0) {
             // about half a cylinder per cell; never below the reference's 1.125 rMax
-            cell = std::max(1.125 * h.rmax, std::cbrt(vol / std::max(1, h.ncyl)) * 0.7937);
+            cell = std::max(1.125 * h.rmax, std::cbrt(vol / std::max(1, h.ncyl)) * 0.7937) * c->cell_scale;
         }
         cell = std::max(cell, h.rmax);
         auto g = [&](double L) { return std::max(1, (int)std::ceil(std::max(L, cell) / cell)); };
@@ -1286,6 +1293,111 @@ static int profile_impl(MechContext* c, int iters, MechProfile* o) {
 }
 
 // ===========================================================================
+// autotuner: tiles per block of the mixed filament kernels, bin-edge scale
+// ===========================================================================
+namespace {
+
+struct TuneKey {
+    int precision, nb, nftiles, R;
+    long long nev;
+    bool operator<(const TuneKey& o) const {
+        if (precision != o.precision) return precision < o.precision;
+        if (nb != o.nb) return nb < o.nb;
+        if (nftiles != o.nftiles) return nftiles < o.nftiles;
+        if (R != o.R) return R < o.R;
+        return nev < o.nev;
+    }
+};
+std::mutex g_tune_mu;
+std::map<TuneKey, MechTuning> g_tune_cache;
+
+}  // namespace
+
+template <typename Real>
+static int autotune_impl(MechContext* c, int flags, MechTuning* out) {
+    int rc;
+    if (!c->have_lists && (rc = rebuild(c, 0.0, nullptr))) return rc;
+    const TuneKey key{c->precision, c->nb, c->n_ftiles, c->R, c->nev};
+    if (!(flags & MECH_TUNE_FORCE)) {
+        std::lock_guard<std::mutex> lk(g_tune_mu);
+        auto it = g_tune_cache.find(key);
+        if (it != g_tune_cache.end()) {
+            *out = it->second;
+            c->tile_cap[0] = out->energy_tiles_per_block;
+            c->tile_cap[1] = out->force_tiles_per_block;
+            c->cell_scale = out->cell_scale;
+            return MECH_OK;
+        }
+    }
+    MechTuning t{};
+    t.energy_tiles_per_block = c->tile_cap[0];
+    t.force_tiles_per_block = c->tile_cap[1];
+    t.cell_scale = c->cell_scale;
+    cudaStream_t s = c->stream;
+    if ((rc = pull_states(c))) return rc;
+    for (int r = 0; r < c->R; ++r) c->h_st[r].active = 1;
+    if ((rc = push_states(c))) return rc;
+    if ((flags & MECH_TUNE_KERNELS) && c->precision == MECH_PREC_MIXED) {
+        cudaEvent_t e0, e1;
+        CU(cudaEventCreate(&e0));
+        CU(cudaEventCreate(&e1));
+        const int cands[] = {1, 2, 3, 4, 6, 8, 12, 16, 24, 32, 48, 64};
+        for (int which = 0; which < 2; ++which) {
+            double best = 1e300;
+            int best_cap = c->tile_cap[which];
+            for (int cap : cands) {
+                if (cap > kFilBulkMaxTiles) continue;
+                c->tile_cap[which] = cap;
+                const DevNet<Real> n = make_devnet<Real>(c);
+                launch_part<Real>(n, which, s);   // warm
+                cudaEventRecord(e0, s);
+                for (int i = 0; i < 10; ++i) launch_part<Real>(n, which, s);
+                cudaEventRecord(e1, s);
+                CU(cudaEventSynchronize(e1));
+                float ms = 0.f;
+                cudaEventElapsedTime(&ms, e0, e1);
+                if (ms / 10 < best) {
+                    best = ms / 10;
+                    best_cap = cap;
+                }
+            }
+            c->tile_cap[which] = best_cap;
+            if (which == 0) { t.energy_tiles_per_block = best_cap; t.ms_energy = best; }
+            else { t.force_tiles_per_block = best_cap; t.ms_force = best; }
+        }
+        cudaEventDestroy(e0);
+        cudaEventDestroy(e1);
+        CU(cudaGetLastError());
+    }
+    if (flags & MECH_TUNE_CELL) {
+        const double cands[] = {0.6, 0.8, 1.0, 1.3, 1.7, 2.2, 3.0};
+        double best = 1e300, best_scale = c->cell_scale;
+        for (double sc : cands) {
+            c->cell_scale = sc;
+            double tmin = 1e300;
+            for (int rep = 0; rep < 3; ++rep) {
+                const auto a = std::chrono::steady_clock::now();
+                if ((rc = rebuild(c, 0.0, nullptr))) return rc;
+                tmin = std::min(tmin, std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - a).count());
+            }
+            if (tmin < best) {
+                best = tmin;
+                best_scale = sc;
+            }
+        }
+        c->cell_scale = best_scale;
+        t.cell_scale = best_scale;
+        t.ms_rebuild = best;
+        if ((rc = rebuild(c, 0.0, nullptr))) return rc;   // leave the lists of the chosen edge
+    }
+    if ((rc = pull_states(c))) return rc;
+    *out = t;
+    std::lock_guard<std::mutex> lk(g_tune_mu);
+    g_tune_cache[key] = t;
+    return MECH_OK;
+}
+
+// ===========================================================================
 // Hessian-vector products, implicit adjoint, Newton refinement (FP64 engine)
 // ===========================================================================
 namespace {
@@ -1548,6 +1660,24 @@ int32_t mech_profile(MechContext* ctx, int32_t iters, MechProfile* out) {
     if (!ctx->have_net) return set_err(MECH_ERR_STATE, "no network");
     CU(cudaSetDevice(ctx->device));
     return ctx->precision == MECH_PREC_FP64 ? profile_impl<double>(ctx, iters, out) : profile_impl<float>(ctx, iters, out);
+}
+
+int32_t mech_autotune(MechContext* ctx, int32_t flags, MechTuning* out) {
+    if (!ctx || !out) return set_err(MECH_ERR_ARG, "null argument");
+    if (!ctx->have_net) return set_err(MECH_ERR_STATE, "no network");
+    CU(cudaSetDevice(ctx->device));
+    return ctx->precision == MECH_PREC_FP64 ? autotune_impl<double>(ctx, flags, out) : autotune_impl<float>(ctx, flags, out);
+}
+
+int32_t mech_set_tuning(MechContext* ctx, const MechTuning* t) {
+    if (!ctx || !t) return set_err(MECH_ERR_ARG, "null argument");
+    if (t->energy_tiles_per_block < 1 || t->energy_tiles_per_block > kFilBulkMaxTiles || t->force_tiles_per_block < 1 ||
+        t->force_tiles_per_block > kFilBulkMaxTiles || !(t->cell_scale > 0))
+        return set_err(MECH_ERR_ARG, "tuning out of range");
+    ctx->tile_cap[0] = t->energy_tiles_per_block;
+    ctx->tile_cap[1] = t->force_tiles_per_block;
+    ctx->cell_scale = t->cell_scale;
+    return MECH_OK;
 }
 
 int32_t mech_get_timing(MechContext* ctx, MechTiming* t) {

@@ -339,19 +339,40 @@ cudaError_t hvp_cg_solve(const DevNet<double>& n, const double* b, double* x, co
         return cudaSuccess;
     }
     const double tol2 = rel_tol * rel_tol * bb;
+    // kCheck iterations per CUDA graph launch; the host reads the residual between launches
     constexpr int kCheck = 16;
+    int per_iter = 0;
+    auto iteration = [&]() {
+        per_iter = launch_hvp(n, w.p, w.Ap, shift, false, s);
+        k_dot<<<G, B, 0, s>>>(w.p, w.Ap, N, w.part, w.ticket, w.scal + 1);
+        k_cg_step<<<G, B, 0, s>>>(x, w.r, w.p, w.Ap, N, w.scal, w.part, w.ticket);
+        k_cg_dir<<<G, B, 0, s>>>(w.p, w.r, N, w.scal);
+        k_cg_roll<<<1, 32, 0, s>>>(w.scal);
+        per_iter += 4;
+    };
+    cudaGraph_t graph = nullptr;
+    cudaGraphExec_t exec = nullptr;
+    if ((e = cudaStreamBeginCapture(s, cudaStreamCaptureModeThreadLocal)) != cudaSuccess) return e;
+    for (int j = 0; j < kCheck; ++j) iteration();
+    e = cudaStreamEndCapture(s, &graph);
+    if (e == cudaSuccess) e = cudaGraphInstantiate(&exec, graph, 0);
+    if (graph) cudaGraphDestroy(graph);
+    if (e != cudaSuccess) return e;
     for (int it = 0; it < max_iter;) {
-        for (int j = 0; j < kCheck && it < max_iter; ++j, ++it) {
-            res->launches += launch_hvp(n, w.p, w.Ap, shift, false, s);
-            k_dot<<<G, B, 0, s>>>(w.p, w.Ap, N, w.part, w.ticket, w.scal + 1);
-            k_cg_step<<<G, B, 0, s>>>(x, w.r, w.p, w.Ap, N, w.scal, w.part, w.ticket);
-            k_cg_dir<<<G, B, 0, s>>>(w.p, w.r, N, w.scal);
-            k_cg_roll<<<1, 32, 0, s>>>(w.scal);
-            res->launches += 4;
+        if (max_iter - it >= kCheck) {
+            e = cudaGraphLaunch(exec, s);
+            it += kCheck;
+            res->launches += (long long)kCheck * per_iter;
+        } else {
+            for (; it < max_iter; ++it) {
+                iteration();
+                res->launches += per_iter;
+            }
+            e = cudaGetLastError();
         }
-        if ((e = cudaGetLastError()) != cudaSuccess) return e;
-        if ((e = cudaMemcpyAsync(h, w.scal, sizeof(h), cudaMemcpyDeviceToHost, s)) != cudaSuccess) return e;
-        if ((e = cudaStreamSynchronize(s)) != cudaSuccess) return e;
+        if (e != cudaSuccess) break;
+        if ((e = cudaMemcpyAsync(h, w.scal, sizeof(h), cudaMemcpyDeviceToHost, s)) != cudaSuccess) break;
+        if ((e = cudaStreamSynchronize(s)) != cudaSuccess) break;
         res->iterations = it;
         res->rel_residual = sqrt(h[0] / bb);
         if (h[4] != 0.0) {   // non-positive curvature met: the iterate stopped there
@@ -363,6 +384,8 @@ cudaError_t hvp_cg_solve(const DevNet<double>& n, const double* b, double* x, co
             break;
         }
     }
+    cudaGraphExecDestroy(exec);
+    if (e != cudaSuccess) return e;
     return cudaGetLastError();
 }
 

@@ -31,6 +31,7 @@ namespace mech {
 
 constexpr int kFilTile = 256;     // beads per filament tile (one block)
 constexpr int kSparseTile = 256;  // interactions per sparse tile (one block)
+constexpr int kFilBulkMaxTiles = 64;   // filament tiles per block of the bulk-staged mixed kernels
 constexpr int kExvolFallbackCap = 4096;
 constexpr int kFbChunks = 64;       // work split of one numeric force fallback
 

@@ -15,7 +15,7 @@ import numpy as np
 
 from . import _lib
 from ._lib import (MechCGParams, MechListInfo, MechNetwork, MechProfile, MechResult, MechSolveInfo, MechSolveParams,
-                   MechTiming, check)
+                   MechTiming, MechTuning, check)
 
 _dp = C.POINTER(C.c_double)
 _i32p = C.POINTER(C.c_int32)
@@ -216,6 +216,17 @@ class Engine:
         info = MechSolveInfo()
         check(self._L.mech_newton_refine(self._ctx, int(max_steps), float(force_tol), C.byref(sp), C.byref(info)))
         return info.as_dict()
+
+    def autotune(self, kernels: bool = True, cell: bool = True, force: bool = False) -> dict:
+        """Time candidate launch geometries / bin edges on this context's networks and keep the fastest."""
+        t = MechTuning()
+        flags = (1 if kernels else 0) | (2 if cell else 0) | (4 if force else 0)
+        check(self._L.mech_autotune(self._ctx, flags, C.byref(t)))
+        return {k: getattr(t, k) for k, _ in t._fields_}
+
+    def set_tuning(self, tuning: dict) -> None:
+        t = MechTuning(*[tuning[k] for k, _ in MechTuning._fields_])
+        check(self._L.mech_set_tuning(self._ctx, C.byref(t)))
 
     def profile(self, iters: int = 20) -> dict:
         p = MechProfile()
