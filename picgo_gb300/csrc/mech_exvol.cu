@@ -80,11 +80,12 @@ __device__ __forceinline__ double r2_at(const Quad& q, double s, double t) {
 __device__ __forceinline__ double node(int i, int N) { return i == 0 ? 0.0 : (i == N ? 1.0 : (double)(i + 1) / N); }
 __device__ __forceinline__ double weight(int i, int N) { return (i == 0 || i == N) ? 1.0 : ((i & 1) ? 4.0 : 2.0); }
 
+// Simpson energies of the flagged pairs: block `blk` of `nblk` takes entries
+// blk, blk + nblk, ...
 template <typename Real>
-__global__ void __launch_bounds__(kBlock) k_exvol_fb_energy(DevNet<Real> n) {
-    __shared__ double sh[32];
+__device__ void fb_energy_blocks(const DevNet<Real>& n, int blk, int nblk, double* sh) {
     const int cnt = min(*n.ev_fb_count, kExvolFallbackCap);
-    for (int k = blockIdx.x; k < cnt; k += gridDim.x) {
+    for (int k = blk; k < cnt; k += nblk) {
         const int pr = n.ev_fb_list[2 * k + 1];
         const int4 bs = n.ev_bead[pr];
         const CGState& S = n.st[n.ev_fb_list[2 * k]];
@@ -379,11 +380,19 @@ __global__ void __launch_bounds__(128) k_exvol_fp64(DevNet<Real> n, int trial, i
     }
 }
 
-// Mixed engine: deterministic per-tile sums of the per-pair energies.
+// The end of an energy evaluation's excluded-volume chain, one launch:
+// blocks [0, kFbEnergyBlocks) compute the Simpson energies of flagged pairs;
+// in the mixed engine the following blocks form the deterministic per-tile
+// sums of the per-pair energies (one block per exvol tile).
+constexpr int kFbEnergyBlocks = 64;
 template <typename Real>
-__global__ void __launch_bounds__(kBlock) k_exvol_tilesum(DevNet<Real> n, int want, int tile_off) {
+__global__ void __launch_bounds__(kBlock) k_exvol_energy_tail(DevNet<Real> n, int want, int tile_off) {
     __shared__ double sh[32];
-    const int ti = tile_off + blockIdx.x;
+    if ((int)blockIdx.x < kFbEnergyBlocks) {
+        fb_energy_blocks(n, blockIdx.x, kFbEnergyBlocks, sh);
+        return;
+    }
+    const int ti = tile_off + (int)blockIdx.x - kFbEnergyBlocks;
     const Tile t = n.stile[ti];
     const CGState& S = n.st[t.replica];
     const bool go = want < 0 ? (S.active != 0) : (S.phase == want);
@@ -392,6 +401,18 @@ __global__ void __launch_bounds__(kBlock) k_exvol_tilesum(DevNet<Real> n, int wa
     double e = i < t.end ? n.ev_energy[i] : 0.0;
     e = block_sum(e, sh);
     if (threadIdx.x == 0) n.part_sp[ti] = e;
+}
+
+// zero the FP64-pass and fallback work-list counts (one memset when they are
+// neighbours in one buffer)
+template <typename Real>
+static inline void reset_counts(const DevNet<Real>& n, cudaStream_t s) {
+    if (n.ev_fb_count == n.ev_list_count + 2) {
+        cudaMemsetAsync(n.ev_list_count, 0, 4 * sizeof(int), s);
+    } else {
+        cudaMemsetAsync(n.ev_list_count, 0, sizeof(int), s);
+        cudaMemsetAsync(n.ev_fb_count, 0, sizeof(int), s);
+    }
 }
 
 template <typename Real>
@@ -405,21 +426,15 @@ int launch_exvol_energy(const DevNet<Real>& n, int want, int trial, cudaStream_t
     int off = 0;
     const int nt = ev_tiles_of(n, &off);
     if (nt == 0) return 0;
-    cudaMemsetAsync(n.ev_list_count, 0, sizeof(int), s);
-    cudaMemsetAsync(n.ev_fb_count, 0, sizeof(int), s);
+    reset_counts(n, s);
     k_exvol<Real><<<nt, kBlock, 0, s>>>(n, want, trial, 0, off);
     int k = 1;
     if (sizeof(Real) == 4) {
         k_exvol_fp64<Real><<<2 * 152, 128, 0, s>>>(n, trial, 0);
         ++k;
     }
-    k_exvol_fb_energy<Real><<<64, kBlock, 0, s>>>(n);
-    ++k;
-    if (sizeof(Real) == 4) {
-        k_exvol_tilesum<Real><<<nt, kBlock, 0, s>>>(n, want, off);
-        ++k;
-    }
-    return k;
+    k_exvol_energy_tail<Real><<<kFbEnergyBlocks + (sizeof(Real) == 4 ? nt : 0), kBlock, 0, s>>>(n, want, off);
+    return k + 1;
 }
 
 template <typename Real>
@@ -427,8 +442,7 @@ int launch_exvol_forces(const DevNet<Real>& n, int want, cudaStream_t s) {
     int off = 0;
     const int nt = ev_tiles_of(n, &off);
     if (nt == 0) return 0;
-    cudaMemsetAsync(n.ev_list_count, 0, sizeof(int), s);
-    cudaMemsetAsync(n.ev_fb_count, 0, sizeof(int), s);
+    reset_counts(n, s);
     k_exvol<Real><<<nt, kBlock, 0, s>>>(n, want, 0, 1, off);
     int k = 1;
     if (sizeof(Real) == 4) {

@@ -156,7 +156,7 @@ __device__ void finalize_energy(const DevNet<Real>& n, int r, int trial, double*
 template <typename Real>
 __device__ void finalize_force(const DevNet<Real>& n, int r, double* sh) {
     const RepTiles rt = n.rt[r];
-    const int stride = sizeof(Real) == 4 ? n.ptiles[1] : 1;
+    const int stride = 1;   // k_force_gather writes one slot per tile
     const int nslot = run_slots(rt.fil_begin, rt.fil_end, stride);
     double a_mx = 0.0, a_ff = 0.0, a_ffp = 0.0;
 #pragma unroll 8
@@ -215,7 +215,7 @@ template <typename Real>
 __global__ void __launch_bounds__(kBlock) k_fil_energy(DevNet<Real> n, int want, int trial) {
     __shared__ Pos<Real> xs[kFilTile + 4];
     __shared__ double sh[32 * MECH_NUM_FF];
-    __shared__ int s_go, s_xb, s_flag;
+    __shared__ int s_go, s_xb;
     __shared__ double s_lam;
     const Tile t = n.ftile[blockIdx.x];
     const int r = t.replica;
@@ -261,13 +261,12 @@ __global__ void __launch_bounds__(kBlock) k_fil_energy(DevNet<Real> n, int want,
             n.part_fil[4 * (size_t)blockIdx.x + 0] = red[0];
             n.part_fil[4 * (size_t)blockIdx.x + 1] = red[1];
         }
-        const RepTiles rt = n.rt[r];
-        if (last_tile(n.ticket, r, rt.fil_end - rt.fil_begin, &s_flag)) finalize_energy(n, r, trial, sh);
     }
 }
 
 // ---------------------------------------------------------------------------
-// filament forces + CSR gather of the sparse contributions + CG partials
+// filament forces of the tile's own beads (the sparse force fields' shares are
+// added by k_force_gather once they are written)
 // ---------------------------------------------------------------------------
 template <typename Real>
 __global__ void __launch_bounds__(kBlock) k_fil_force(DevNet<Real> n, int want) {
@@ -275,8 +274,7 @@ __global__ void __launch_bounds__(kBlock) k_fil_force(DevNet<Real> n, int want) 
     __shared__ Real fs[(kFilTile + 2) * 3];    // stretch force on the second bead
     __shared__ Real f1[(kFilTile + 2) * 3];    // bending Fr1
     __shared__ Real f2[(kFilTile + 2) * 3];    // bending Fr2
-    __shared__ double sh[32 * 3];
-    __shared__ int s_go, s_xb, s_fb, s_flag;
+    __shared__ int s_go, s_xb, s_fb;
     const Tile t = n.ftile[blockIdx.x];
     const int r = t.replica;
     if (threadIdx.x == 0) {
@@ -286,83 +284,116 @@ __global__ void __launch_bounds__(kBlock) k_fil_force(DevNet<Real> n, int want) 
         s_fb = S.fbuf;
     }
     __syncthreads();
-    if (s_go) {
-        const int T = t.end - t.begin;
-        const Real* X = n.x[s_xb];
-        for (int i = threadIdx.x; i < T + 4; i += blockDim.x) {
-            const int b = t.begin - 2 + i;
-            if (b >= 0 && b < n.nb) xs[i] = load_pos(X, b);
-        }
-        __syncthreads();
-        // interaction slots s in [0, T + 2): bead j = begin - 1 + s, shared index s + 1
-        for (int s = threadIdx.x; s < T + 2; s += blockDim.x) {
-            const int j = t.begin - 1 + s;
-            Real a[3] = {0, 0, 0}, b1[3] = {0, 0, 0}, b2[3] = {0, 0, 0};
-            if (j >= 0 && j < n.nb) {
-                const int fl = n.bflag[j];
-                if (fl & 1) {
-                    Real ks, l0, kb, t0;
-                    load_par(n.bpar, j, ks, l0, kb, t0);
-                    Real r2[3];
-                    pdiff(xs[s + 2], xs[s + 1], r2);
-                    stretch_force<Real>(r2[0], r2[1], r2[2], ks, l0, a);
-                    if (fl & 2) {
-                        Real r1[3];
-                        pdiff(xs[s + 1], xs[s], r1);
-                        bend_force<Real>(r1, r2, kb, t0, b1, b2);
-                    }
+    if (!s_go) return;
+    const int T = t.end - t.begin;
+    const Real* X = n.x[s_xb];
+    for (int i = threadIdx.x; i < T + 4; i += blockDim.x) {
+        const int b = t.begin - 2 + i;
+        if (b >= 0 && b < n.nb) xs[i] = load_pos(X, b);
+    }
+    __syncthreads();
+    // interaction slots s in [0, T + 2): bead j = begin - 1 + s, shared index s + 1
+    for (int s = threadIdx.x; s < T + 2; s += blockDim.x) {
+        const int j = t.begin - 1 + s;
+        Real a[3] = {0, 0, 0}, b1[3] = {0, 0, 0}, b2[3] = {0, 0, 0};
+        if (j >= 0 && j < n.nb) {
+            const int fl = n.bflag[j];
+            if (fl & 1) {
+                Real ks, l0, kb, t0;
+                load_par(n.bpar, j, ks, l0, kb, t0);
+                Real r2[3];
+                pdiff(xs[s + 2], xs[s + 1], r2);
+                stretch_force<Real>(r2[0], r2[1], r2[2], ks, l0, a);
+                if (fl & 2) {
+                    Real r1[3];
+                    pdiff(xs[s + 1], xs[s], r1);
+                    bend_force<Real>(r1, r2, kb, t0, b1, b2);
                 }
             }
+        }
 #pragma unroll
-            for (int q = 0; q < 3; ++q) {
-                fs[3 * s + q] = a[q];
-                f1[3 * s + q] = b1[q];
-                f2[3 * s + q] = b2[q];
-            }
+        for (int q = 0; q < 3; ++q) {
+            fs[3 * s + q] = a[q];
+            f1[3 * s + q] = b1[q];
+            f2[3 * s + q] = b2[q];
         }
-        __syncthreads();
-        Real mx = 0, ff = 0, ffp = 0;
-        const int i = threadIdx.x;
-        if (i < T) {
-            const int b = t.begin + i;
-            Real F[3];
-#pragma unroll
-            for (int q = 0; q < 3; ++q) {
-                // stretching: cylinder (b-1, b) then (b, b+1); bending: triples
-                // centred on b-1, b, b+1 (the reference's interaction order)
-                Real v = fs[3 * i + q];
-                v += -fs[3 * (i + 1) + q];
-                v += f2[3 * i + q];
-                v += f1[3 * (i + 1) + q] - f2[3 * (i + 1) + q];
-                v += -f1[3 * (i + 2) + q];
-                F[q] = v;
-            }
-            const int c0 = n.csr_off[b], c1 = n.csr_off[b + 1];
-            for (int c = c0; c < c1; ++c) {
-                F[0] += n.contrib[3 * (size_t)c];
-                F[1] += n.contrib[3 * (size_t)c + 1];
-                F[2] += n.contrib[3 * (size_t)c + 2];
-            }
-            Real* Fo = n.f[s_fb ^ 1] + 3 * (size_t)b;
-            const Real* Fp = n.f[s_fb] + 3 * (size_t)b;
-            Fo[0] = F[0];
-            Fo[1] = F[1];
-            Fo[2] = F[2];
-            mx = fmax(fmax(fabs(F[0]), fabs(F[1])), fabs(F[2]));
-            ff = bead_dot(F[0], F[1], F[2], F[0], F[1], F[2]);
-            ffp = bead_dot(F[0], F[1], F[2], Fp[0], Fp[1], Fp[2]);
-        }
-        double red[3] = {warp_max_r(mx), warp_sum_r(ff), warp_sum_r(ffp)};
-        const int ops[3] = {1, 0, 0};
-        block_combine<3>(red, ops, sh);
-        if (threadIdx.x == 0) {
-            n.part_fil[4 * (size_t)blockIdx.x + 0] = red[0];
-            n.part_fil[4 * (size_t)blockIdx.x + 1] = red[1];
-            n.part_fil[4 * (size_t)blockIdx.x + 2] = red[2];
-        }
-        const RepTiles rt = n.rt[r];
-        if (last_tile(n.ticket, r, rt.fil_end - rt.fil_begin, &s_flag)) finalize_force(n, r, sh);
     }
+    __syncthreads();
+    const int i = threadIdx.x;
+    if (i < T) {
+        const int b = t.begin + i;
+        Real* Fo = n.f[s_fb ^ 1] + 3 * (size_t)b;
+#pragma unroll
+        for (int q = 0; q < 3; ++q) {
+            // stretching: cylinder (b-1, b) then (b, b+1); bending: triples
+            // centred on b-1, b, b+1 (the reference's interaction order)
+            Real v = fs[3 * i + q];
+            v += -fs[3 * (i + 1) + q];
+            v += f2[3 * i + q];
+            v += f1[3 * (i + 1) + q] - f2[3 * (i + 1) + q];
+            v += -f1[3 * (i + 2) + q];
+            Fo[q] = v;
+        }
+    }
+}
+
+// ---------------------------------------------------------------------------
+// Every bead adds its sparse contributions (contiguous, in the CSR order) to
+// its filament force, then the CG partials: max |F|, F.F, F.Fprev per tile;
+// the last tile of a replica (ticket) reduces them (finalize_force).
+// ---------------------------------------------------------------------------
+template <typename Real>
+__global__ void __launch_bounds__(kBlock) k_force_gather(DevNet<Real> n, int want) {
+    __shared__ double sh[32 * 3];
+    __shared__ int s_go, s_fb, s_flag;
+    const Tile t = n.ftile[blockIdx.x];
+    const int r = t.replica;
+    if (threadIdx.x == 0) {
+        const CGState& S = n.st[r];
+        s_go = replica_selected(S, want);
+        s_fb = S.fbuf;
+    }
+    __syncthreads();
+    if (!s_go) return;
+    Real mx = 0, ff = 0, ffp = 0;
+    const int b = t.begin + threadIdx.x;
+    if (b < t.end) {
+        Real* Fo = n.f[s_fb ^ 1] + 3 * (size_t)b;
+        const Real* Fp = n.f[s_fb] + 3 * (size_t)b;
+        Real F[3] = {Fo[0], Fo[1], Fo[2]};
+        const int c0 = n.csr_off[b], c1 = n.csr_off[b + 1];
+        for (int c = c0; c < c1; ++c) {
+            F[0] += n.contrib[3 * (size_t)c];
+            F[1] += n.contrib[3 * (size_t)c + 1];
+            F[2] += n.contrib[3 * (size_t)c + 2];
+        }
+        Fo[0] = F[0];
+        Fo[1] = F[1];
+        Fo[2] = F[2];
+        mx = fmax(fmax(fabs(F[0]), fabs(F[1])), fabs(F[2]));
+        ff = bead_dot(F[0], F[1], F[2], F[0], F[1], F[2]);
+        ffp = bead_dot(F[0], F[1], F[2], Fp[0], Fp[1], Fp[2]);
+    }
+    double red[3] = {warp_max_r(mx), warp_sum_r(ff), warp_sum_r(ffp)};
+    const int ops[3] = {1, 0, 0};
+    block_combine<3>(red, ops, sh);
+    if (threadIdx.x == 0) {
+        n.part_fil[4 * (size_t)blockIdx.x + 0] = red[0];
+        n.part_fil[4 * (size_t)blockIdx.x + 1] = red[1];
+        n.part_fil[4 * (size_t)blockIdx.x + 2] = red[2];
+    }
+    const RepTiles rt = n.rt[r];
+    if (last_tile(n.ticket, r, rt.fil_end - rt.fil_begin, &s_flag)) finalize_force(n, r, sh);
+}
+
+// One block per replica: the energy reduction and the line-search step, after
+// every kernel of the evaluation has written its partial sums.
+template <typename Real>
+__global__ void __launch_bounds__(kBlock) k_finalize_energy(DevNet<Real> n, int want, int trial) {
+    __shared__ double sh[32 * MECH_NUM_FF];
+    const int r = blockIdx.x;
+    if (!replica_selected(n.st[r], want)) return;
+    finalize_energy(n, r, trial, sh);
 }
 
 // ---------------------------------------------------------------------------
@@ -374,27 +405,17 @@ __global__ void __launch_bounds__(kBlock) k_fil_force(DevNet<Real> n, int want) 
 // reduces once per run of tiles of the same replica.
 // ---------------------------------------------------------------------------
 
-// Close a run of `cnt` tiles of replica r that starts at tile `first`: reduce
-// the block's lane-0 warp results, store the partials in the run's first tile
-// slot (zeros in the others), count the tiles; true in every thread of the
-// block that completed the replica.
+
+// Store a run's partial sums (lane-0 warp results) in the slot of its first
+// tile; the reduction kernel that follows the evaluation reads them.
 template <int N>
-__device__ bool flush_run(const DevNet<float>& n, int r, int first, int cnt, double (&w)[N], const int (&ops)[N],
-                          double* sh, int* s_flag) {
+__device__ __forceinline__ void write_run(const DevNet<float>& n, int first, double (&w)[N], const int (&ops)[N],
+                                          double* sh) {
     block_combine<N>(w, ops, sh);
     if (threadIdx.x == 0) {
 #pragma unroll
         for (int k = 0; k < N; ++k) n.part_fil[4 * (size_t)first + k] = w[k];
-        __threadfence();
-        const RepTiles rt = n.rt[r];
-        const int old = atomicAdd(n.ticket + r, cnt);
-        *s_flag = (old + cnt == rt.fil_end - rt.fil_begin);
-        if (*s_flag) n.ticket[r] = 0;
     }
-    __syncthreads();
-    const bool last = *s_flag != 0;
-    if (last) __threadfence();
-    return last;
 }
 
 __device__ __forceinline__ Pos<float> pos_at(const DevNet<float>& n, const float* X, int b, bool tr, float lf) {
@@ -405,7 +426,7 @@ __device__ __forceinline__ Pos<float> pos_at(const DevNet<float>& n, const float
 
 // ---------------------------------------------------------------------------
 // Mixed engine, bulk-staged filament energy: a persistent walk over runs of
-// tiles with run-start partial slots (see flush_run), where each selected
+// tiles with run-start partial slots (see write_run), where each selected
 // tile's positions (with a one-bead halo),
 // constants, flags and (for a trial) search direction arrive in shared memory
 // by cp.async.bulk on a three-stage mbarrier ring, so a block keeps several
@@ -496,8 +517,8 @@ __global__ void __launch_bounds__(kBlock) k_fil_energy_bulk(DevNet<float> n, int
     __shared__ __align__(8) uint64_t bar[kBulkStages];
     __shared__ int4 s_desc[kBulkMaxTiles];
     __shared__ float s_lf[kBulkMaxTiles];
-    __shared__ double sh[32 * MECH_NUM_FF];
-    __shared__ int s_flag, s_abort;
+    __shared__ double sh[32 * 2];
+    __shared__ int s_abort;
     const int t0 = blockIdx.x * n.ptiles[0], t1 = min(t0 + n.ptiles[0], n.n_ftiles);
     const int nt = t1 - t0;
     const bool tr = trial != 0;
@@ -531,7 +552,7 @@ __global__ void __launch_bounds__(kBlock) k_fil_energy_bulk(DevNet<float> n, int
         if (t.z != cur) {
             if (cnt) {
                 double w[2] = {warp_sum_pair(es), warp_sum_pair(eb)};
-                if (flush_run<2>(n, cur, first, cnt, w, ops, sh, &s_flag)) finalize_energy(n, cur, trial, sh);
+                write_run<2>(n, first, w, ops, sh);
             }
             cur = t.z;
             first = t0 + k;
@@ -597,7 +618,7 @@ __global__ void __launch_bounds__(kBlock) k_fil_energy_bulk(DevNet<float> n, int
     }
     if (cnt) {
         double w[2] = {warp_sum_pair(es), warp_sum_pair(eb)};
-        if (flush_run<2>(n, cur, first, cnt, w, ops, sh, &s_flag)) finalize_energy(n, cur, trial, sh);
+        write_run<2>(n, first, w, ops, sh);
     }
 }
 
@@ -611,19 +632,15 @@ __global__ void __launch_bounds__(kBlock) k_fil_energy_bulk(DevNet<float> n, int
 // ---------------------------------------------------------------------------
 constexpr int kBulkFXBeads = kFilTile + 8;    // tile + 2-bead halo, even-aligned ends
 constexpr int kBulkFPar = kFilTile + 4;       // constants of beads tb - 1 .. te
-constexpr int kBulkFPrev = kFilTile + 4;      // previous forces, 4-bead aligned ends
-constexpr int kBulkCsr = kFilTile + 8;        // CSR offsets tb .. te, 4-entry aligned ends
 
 struct __align__(16) ForceStage {
     float x[6 * kBulkFXBeads];
     float4 par[kBulkFPar];
-    float fp[3 * kBulkFPrev];
-    int csr[kBulkCsr];
     uint8_t flag[kBulkFlags];
 };
 
 struct ForceRange {
-    int xs, xe, ps, pe, qs, qe, cs, ce, fs, fe;
+    int xs, xe, ps, pe, fs, fe;
 };
 __device__ __forceinline__ ForceRange force_range(int tb, int te, int nb) {
     ForceRange r;
@@ -632,10 +649,6 @@ __device__ __forceinline__ ForceRange force_range(int tb, int te, int nb) {
     r.xe = (hi2 + 1) & ~1;
     r.ps = max(tb - 1, 0);
     r.pe = min(te + 1, nb);
-    r.qs = tb & ~3;
-    r.qe = (te + 3) & ~3;
-    r.cs = tb & ~3;
-    r.ce = (te + 1 + 3) & ~3;
     r.fs = lo2 & ~15;
     r.fe = (hi2 + 15) & ~15;
     return r;
@@ -643,17 +656,14 @@ __device__ __forceinline__ ForceRange force_range(int tb, int te, int nb) {
 
 __device__ void issue_force_stage(const DevNet<float>& n, int4 t, ForceStage* st, uint64_t* bar) {
     const float* X = n.x[(t.w >> 1) & 1];
-    const float* Fp = n.f[(t.w >> 2) & 1];
     const ForceRange rg = force_range(t.x, t.y, n.nb);
-    const void* src[5] = {X + 6 * (size_t)rg.xs, n.bpar + 4 * (size_t)rg.ps, Fp + 3 * (size_t)rg.qs, n.csr_off + rg.cs,
-                          n.bflag + rg.fs};
-    void* dst[5] = {st->x, st->par, st->fp, st->csr, st->flag};
-    const unsigned bytes[5] = {24u * (unsigned)(rg.xe - rg.xs), 16u * (unsigned)(rg.pe - rg.ps),
-                               12u * (unsigned)(rg.qe - rg.qs), 4u * (unsigned)(rg.ce - rg.cs),
+    const void* src[3] = {X + 6 * (size_t)rg.xs, n.bpar + 4 * (size_t)rg.ps, n.bflag + rg.fs};
+    void* dst[3] = {st->x, st->par, st->flag};
+    const unsigned bytes[3] = {24u * (unsigned)(rg.xe - rg.xs), 16u * (unsigned)(rg.pe - rg.ps),
                                (unsigned)(rg.fe - rg.fs)};
     unsigned total = 0;
     bool ok = true;
-    for (int k = 0; k < 5; ++k) {
+    for (int k = 0; k < 3; ++k) {
         if (!bytes[k]) continue;
         if (!aligned16(src[k], bytes[k]) || !aligned16(dst[k], bytes[k])) ok = false;
         total += bytes[k];
@@ -665,17 +675,21 @@ __device__ void issue_force_stage(const DevNet<float>& n, int4 t, ForceStage* st
         return;
     }
     mbar_arrive_expect_tx(bar, total);
-    for (int k = 0; k < 5; ++k)
+    for (int k = 0; k < 3; ++k)
         if (bytes[k]) bulk_copy_g2s(dst[k], src[k], bytes[k], bar);
 }
 
+// Mixed engine, bulk-staged filament forces: each selected tile's positions
+// (two-bead halo), the constants and flags of its beads and their neighbours
+// arrive by cp.async.bulk like k_fil_energy_bulk; every bead's filament force
+// is written to the force buffer, where k_force_gather adds the bead's sparse
+// contributions and forms the CG partials.
 __global__ void __launch_bounds__(kBlock) k_fil_force_bulk(DevNet<float> n, int want) {
     __shared__ ForceStage stage[kBulkStages];
     __shared__ __align__(8) uint64_t bar[kBulkStages];
     __shared__ int4 s_desc[kBulkMaxTiles];
     __shared__ float s_lf[kBulkMaxTiles];
-    __shared__ double sh[32 * 3];
-    __shared__ int s_flag, s_abort;
+    __shared__ int s_abort;
     const int t0 = blockIdx.x * n.ptiles[1], t1 = min(t0 + n.ptiles[1], n.n_ftiles);
     const int nt = t1 - t0;
     if (threadIdx.x == 0) {
@@ -697,29 +711,11 @@ __global__ void __launch_bounds__(kBlock) k_fil_force_bulk(DevNet<float> n, int 
                 ++issued;
             }
     }
-    int cur = -1, first = 0, cnt = 0, fb = 0, j = 0;
-    bool go = false;
-    float mx = 0.f;
-    FF ff, ffp;
-    const int ops[3] = {1, 0, 0};
+    int j = 0;
     for (int k = 0; k < nt; ++k) {
         const int4 t = s_desc[k];
-        if (t.z != cur) {
-            if (cnt) {
-                double w[3] = {warp_max_lane0(mx), warp_sum_pair(ff), warp_sum_pair(ffp)};
-                if (flush_run<3>(n, cur, first, cnt, w, ops, sh, &s_flag)) finalize_force(n, cur, sh);
-            }
-            cur = t.z;
-            first = t0 + k;
-            cnt = 0;
-            mx = 0.f;
-            ff = FF();
-            ffp = FF();
-            go = t.w & 1;
-            fb = (t.w >> 2) & 1;
-        }
-        if (!go) continue;
-        ++cnt;
+        if (!(t.w & 1)) continue;
+        const int fb = (t.w >> 2) & 1;
         const int sidx = j % kBulkStages;
         if (!mbar_wait_bounded(&bar[sidx], (unsigned)((j / kBulkStages) & 1), kBulkWaitLimit)) {
             atomicOr(n.err, 32u);
@@ -744,6 +740,7 @@ __global__ void __launch_bounds__(kBlock) k_fil_force_bulk(DevNet<float> n, int 
             float rm[3] = {0, 0, 0}, rp[3] = {0, 0, 0};
             if (f0 & 2) pdiff(p0, pm1, rm);
             if (f0 & 1) pdiff(pp1, p0, rp);
+            // stretching: cylinder (b-1, b) then (b, b+1); bending: triples centred on b-1, b, b+1
             if (f0 & 2) {
                 float S1[3];
                 stretch_force<float>(rm[0], rm[1], rm[2], prm.x, prm.y, S1);
@@ -771,20 +768,10 @@ __global__ void __launch_bounds__(kBlock) k_fil_force_bulk(DevNet<float> n, int 
                 bend_force<float>(rp, r2, prp.z, prp.w, a1, a2);
                 F[0] += -a1[0]; F[1] += -a1[1]; F[2] += -a1[2];
             }
-            const int c0 = S.csr[b - rg.cs], c1 = S.csr[b + 1 - rg.cs];
-            for (int c = c0; c < c1; ++c) {
-                F[0] += n.contrib[3 * (size_t)c];
-                F[1] += n.contrib[3 * (size_t)c + 1];
-                F[2] += n.contrib[3 * (size_t)c + 2];
-            }
             float* Fo = n.f[fb ^ 1] + 3 * (size_t)b;
-            const float* Fq = S.fp + 3 * (b - rg.qs);
             Fo[0] = F[0];
             Fo[1] = F[1];
             Fo[2] = F[2];
-            mx = fmaxf(mx, fmaxf(fmaxf(fabsf(F[0]), fabsf(F[1])), fabsf(F[2])));
-            ff.add(bead_dot(F[0], F[1], F[2], F[0], F[1], F[2]));
-            ffp.add(bead_dot(F[0], F[1], F[2], Fq[0], Fq[1], Fq[2]));
         }
         ++j;
         __syncthreads();   // stage sidx fully read
@@ -799,16 +786,9 @@ __global__ void __launch_bounds__(kBlock) k_fil_force_bulk(DevNet<float> n, int 
                 }
         }
     }
-    if (s_abort) {
-        if (threadIdx.x == 0)
-            for (int q = max(j - 1, 0); q < issued; ++q)
-                mbar_wait_bounded(&bar[q % kBulkStages], (unsigned)((q / kBulkStages) & 1), kBulkWaitLimit);
-        return;
-    }
-    if (cnt) {
-        double w[3] = {warp_max_lane0(mx), warp_sum_pair(ff), warp_sum_pair(ffp)};
-        if (flush_run<3>(n, cur, first, cnt, w, ops, sh, &s_flag)) finalize_force(n, cur, sh);
-    }
+    if (s_abort && threadIdx.x == 0)   // drain copies still in flight before shared memory is released
+        for (int q = max(j - 1, 0); q < issued; ++q)
+            mbar_wait_bounded(&bar[q % kBulkStages], (unsigned)((q / kBulkStages) & 1), kBulkWaitLimit);
 }
 
 // Mixed engine: persistent direction update d = F + beta d with the d.F partials.
@@ -1162,34 +1142,53 @@ static int n_lm_tiles(const DevNet<Real>& n, int* ev_tiles, int* bb_tiles) {
     return n.sp_tiles[K_LINKER] + n.sp_tiles[K_MOTOR];
 }
 
+// The excluded-volume chain and the linker/motor/boundary kernel on side
+// lanes, the filament kernel on the main lane, then (after the joins) the
+// reduction on the main lane.
 template <typename Real>
-int launch_energy(const DevNet<Real>& n, int want, int trial, cudaStream_t s) {
+int launch_energy(const DevNet<Real>& n, int want, int trial, const Lanes& L) {
     int ev_t = 0, bb_t = 0;
     const int lm = n_lm_tiles(n, &ev_t, &bb_t);
     int launched = 0;
+    cudaEventRecord(L.fork, L.main);
+    cudaStreamWaitEvent(L.side, L.fork, 0);
+    cudaStreamWaitEvent(L.side2, L.fork, 0);
+    launched += launch_exvol_energy<Real>(n, want, trial, L.side);
+    cudaEventRecord(L.join, L.side);
     if (lm + bb_t > 0) {
-        k_bond_bnd<Real><<<lm + bb_t, kBlock, 0, s>>>(n, want, trial, 0, lm, ev_t);
+        k_bond_bnd<Real><<<lm + bb_t, kBlock, 0, L.side2>>>(n, want, trial, 0, lm, ev_t);
         ++launched;
     }
-    launched += launch_exvol_energy<Real>(n, want, trial, s);
-    if constexpr (sizeof(Real) == 4) k_fil_energy_bulk<<<n.pgrid[0], kBlock, 0, s>>>(n, want, trial);
-    else k_fil_energy<Real><<<n.n_ftiles, kBlock, 0, s>>>(n, want, trial);
-    return launched + 1;
+    cudaEventRecord(L.join2, L.side2);
+    if constexpr (sizeof(Real) == 4) k_fil_energy_bulk<<<n.pgrid[0], kBlock, 0, L.main>>>(n, want, trial);
+    else k_fil_energy<Real><<<n.n_ftiles, kBlock, 0, L.main>>>(n, want, trial);
+    cudaStreamWaitEvent(L.main, L.join, 0);
+    cudaStreamWaitEvent(L.main, L.join2, 0);
+    k_finalize_energy<Real><<<n.R, kBlock, 0, L.main>>>(n, want, trial);
+    return launched + 2;
 }
 
 template <typename Real>
-int launch_forces(const DevNet<Real>& n, int want, cudaStream_t s) {
+int launch_forces(const DevNet<Real>& n, int want, const Lanes& L) {
     int ev_t = 0, bb_t = 0;
     const int lm = n_lm_tiles(n, &ev_t, &bb_t);
     int launched = 0;
+    cudaEventRecord(L.fork, L.main);
+    cudaStreamWaitEvent(L.side, L.fork, 0);
+    cudaStreamWaitEvent(L.side2, L.fork, 0);
+    launched += launch_exvol_forces<Real>(n, want, L.side);
+    cudaEventRecord(L.join, L.side);
     if (lm + bb_t > 0) {
-        k_bond_bnd<Real><<<lm + bb_t, kBlock, 0, s>>>(n, want, 0, 1, lm, ev_t);
+        k_bond_bnd<Real><<<lm + bb_t, kBlock, 0, L.side2>>>(n, want, 0, 1, lm, ev_t);
         ++launched;
     }
-    launched += launch_exvol_forces<Real>(n, want, s);
-    if constexpr (sizeof(Real) == 4) k_fil_force_bulk<<<n.pgrid[1], kBlock, 0, s>>>(n, want);
-    else k_fil_force<Real><<<n.n_ftiles, kBlock, 0, s>>>(n, want);
-    return launched + 1;
+    cudaEventRecord(L.join2, L.side2);
+    if constexpr (sizeof(Real) == 4) k_fil_force_bulk<<<n.pgrid[1], kBlock, 0, L.main>>>(n, want);
+    else k_fil_force<Real><<<n.n_ftiles, kBlock, 0, L.main>>>(n, want);
+    cudaStreamWaitEvent(L.main, L.join, 0);
+    cudaStreamWaitEvent(L.main, L.join2, 0);
+    k_force_gather<Real><<<n.n_ftiles, kBlock, 0, L.main>>>(n, want);
+    return launched + 2;
 }
 
 template <typename Real>
@@ -1212,14 +1211,14 @@ int launch_dispatch_failed(const DevNet<Real>& n, cudaStream_t s) {
 }
 
 template <typename Real>
-int launch_recover(const DevNet<Real>& n, cudaStream_t s) {
+int launch_recover(const DevNet<Real>& n, const Lanes& L) {
     int k = 0;
-    k_recover_maxabs<Real><<<n.n_ftiles, kBlock, 0, s>>>(n);
-    k_recover_move<Real><<<n.n_ftiles, kBlock, 0, s>>>(n);
+    k_recover_maxabs<Real><<<n.n_ftiles, kBlock, 0, L.main>>>(n);
+    k_recover_move<Real><<<n.n_ftiles, kBlock, 0, L.main>>>(n);
     k += 2;
-    k += launch_forces<Real>(n, PH_RECOVER_FORCE, s);
-    k += launch_energy<Real>(n, PH_RECOVER_ENERGY, 0, s);
-    k += launch_reset<Real>(n, s);
+    k += launch_forces<Real>(n, PH_RECOVER_FORCE, L);
+    k += launch_energy<Real>(n, PH_RECOVER_ENERGY, 0, L);
+    k += launch_reset<Real>(n, L.main);
     return k;
 }
 
@@ -1241,7 +1240,8 @@ int launch_part(const DevNet<Real>& n, int which, cudaStream_t s) {
         case 1:
             if constexpr (sizeof(Real) == 4) k_fil_force_bulk<<<n.pgrid[1], kBlock, 0, s>>>(n, -1);
             else k_fil_force<Real><<<n.n_ftiles, kBlock, 0, s>>>(n, -1);
-            return 1;
+            k_force_gather<Real><<<n.n_ftiles, kBlock, 0, s>>>(n, -1);
+            return 2;
         case 2: if (lm + bb_t > 0) { k_bond_bnd<Real><<<lm + bb_t, kBlock, 0, s>>>(n, -1, 0, 0, lm, ev_t); return 1; } return 0;
         case 3: if (lm + bb_t > 0) { k_bond_bnd<Real><<<lm + bb_t, kBlock, 0, s>>>(n, -1, 0, 1, lm, ev_t); return 1; } return 0;
     }
@@ -1265,12 +1265,12 @@ int persistent_blocks(int device, int which) {
 
 #define MECH_INSTANTIATE(R)                                                             \
     template int launch_part<R>(const DevNet<R>&, int, cudaStream_t);                   \
-    template int launch_energy<R>(const DevNet<R>&, int, int, cudaStream_t);            \
-    template int launch_forces<R>(const DevNet<R>&, int, cudaStream_t);                 \
+    template int launch_energy<R>(const DevNet<R>&, int, int, const Lanes&);            \
+    template int launch_forces<R>(const DevNet<R>&, int, const Lanes&);                 \
     template int launch_direction<R>(const DevNet<R>&, cudaStream_t);                   \
     template int launch_reset<R>(const DevNet<R>&, cudaStream_t);                       \
     template int launch_dispatch_failed<R>(const DevNet<R>&, cudaStream_t);             \
-    template int launch_recover<R>(const DevNet<R>&, cudaStream_t);                     \
+    template int launch_recover<R>(const DevNet<R>&, const Lanes&);                     \
     template int launch_backup_restore<R>(const DevNet<R>&, cudaStream_t);
 MECH_INSTANTIATE(double)
 MECH_INSTANTIATE(float)

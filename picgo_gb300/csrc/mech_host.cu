@@ -61,6 +61,9 @@ struct MechContext {
     int device = 0;
     int precision = MECH_PREC_FP64;
     cudaStream_t stream = nullptr;
+    cudaStream_t side = nullptr, side2 = nullptr;      // lanes of the sparse force fields
+    cudaEvent_t fork = nullptr, join = nullptr, join2 = nullptr;
+    Lanes lanes() const { return Lanes{stream, side, side2, fork, join, join2}; }
     int R = 0;
     int nb = 0, ncyl = 0, nlk = 0, nmt = 0, nplanes = 0;
     long long nev = 0, nbb = 0;
@@ -112,6 +115,11 @@ struct MechContext {
     ~MechContext() {
         if (h_st) cudaFreeHost(h_st);
         if (h_err) cudaFreeHost(h_err);
+        if (fork) cudaEventDestroy(fork);
+        if (join) cudaEventDestroy(join);
+        if (join2) cudaEventDestroy(join2);
+        if (side) cudaStreamDestroy(side);
+        if (side2) cudaStreamDestroy(side2);
         if (stream) cudaStreamDestroy(stream);
     }
 };
@@ -183,7 +191,8 @@ DevNet<Real> make_devnet(MechContext* c) {
     n.slot_pos = c->cb.pos.as<int>();
     n.lk_sf = c->lk_sf.as<double>();
     n.mt_sf = c->mt_sf.as<double>();
-    n.ev_fb_count = c->ev_fb_count.as<int>();
+    // the fallback count sits beside the FP64-pass count once the lists exist (one reset for both)
+    n.ev_fb_count = c->ev_list_count.p ? c->ev_list_count.as<int>() + 2 : c->ev_fb_count.as<int>();
     n.ev_fb_list = c->ev_fb_list.as<int>();
     n.ev_fb_energy = c->ev_fb_energy.as<double>();
     n.fb_moments = c->fb_moments.as<double>();
@@ -814,7 +823,7 @@ static int eval_energy(MechContext* c, int replica) {
     if ((rc = push_states(c))) return rc;
     CU(cudaMemsetAsync(c->err.p, 0, sizeof(unsigned), c->stream));
     const DevNet<Real> n = make_devnet<Real>(c);
-    c->timing.launches += launch_energy<Real>(n, -1, 0, c->stream);
+    c->timing.launches += launch_energy<Real>(n, -1, 0, c->lanes());
     CU(cudaGetLastError());
     return pull_states(c);
 }
@@ -827,7 +836,7 @@ static int eval_forces(MechContext* c, int replica) {
     if ((rc = push_states(c))) return rc;
     CU(cudaMemsetAsync(c->err.p, 0, sizeof(unsigned), c->stream));
     const DevNet<Real> n = make_devnet<Real>(c);
-    c->timing.launches += launch_forces<Real>(n, -1, c->stream);
+    c->timing.launches += launch_forces<Real>(n, -1, c->lanes());
     CU(cudaGetLastError());
     return pull_states(c);
 }
@@ -842,8 +851,8 @@ static int capture_iteration_graph(MechContext* c, cudaGraphExec_t* exec, int* n
     CU(cudaStreamBeginCapture(c->stream, cudaStreamCaptureModeThreadLocal));
     int k = 0;
     for (int b = 0; b < kBlocksPerGraph; ++b) {
-        for (int t = 0; t < kTrialsPerBlock; ++t) k += launch_energy<Real>(n, PH_LS_TRIAL, 1, c->stream);
-        k += launch_forces<Real>(n, PH_FORCE, c->stream);
+        for (int t = 0; t < kTrialsPerBlock; ++t) k += launch_energy<Real>(n, PH_LS_TRIAL, 1, c->lanes());
+        k += launch_forces<Real>(n, PH_FORCE, c->lanes());
         k += launch_direction<Real>(n, c->stream);
         k += launch_dispatch_failed<Real>(n, c->stream);
         k += launch_reset<Real>(n, c->stream);
@@ -938,8 +947,8 @@ static int minimize_impl(MechContext* c, const MechCGParams* p, MechResult* res)
     CU(cudaEventRecord(e0, s));
     // energiesBefore, initial forces, resetCGParams, loop head
     long long launches = 0;
-    launches += launch_energy<Real>(n, -1, 0, s);
-    launches += launch_forces<Real>(n, -1, s);
+    launches += launch_energy<Real>(n, -1, 0, c->lanes());
+    launches += launch_forces<Real>(n, -1, c->lanes());
     k_cg_init<<<(c->R + 127) / 128, 128, 0, s>>>(n.st, c->R);
     launches += 1 + launch_reset<Real>(n, s);
     CU(cudaGetLastError());
@@ -971,7 +980,7 @@ static int minimize_impl(MechContext* c, const MechCGParams* p, MechResult* res)
         }
         if (all_done) break;
         if (recover) {
-            launches += launch_recover<Real>(n, s);
+            launches += launch_recover<Real>(n, c->lanes());
             CU(cudaGetLastError());
         }
         // batched runs: once the replicas still minimizing hold at most half
@@ -1012,7 +1021,7 @@ static int minimize_impl(MechContext* c, const MechCGParams* p, MechResult* res)
     }
     if ((rc = push_states(c))) return rc;
     if (restore) launches += launch_backup_restore<Real>(n, s);
-    launches += launch_energy<Real>(n, -1, 0, s);   // energiesAfter
+    launches += launch_energy<Real>(n, -1, 0, c->lanes());   // energiesAfter
     CU(cudaEventRecord(e1, s));
     if ((rc = pull_states(c))) return rc;
     float ms = 0.f;
@@ -1074,6 +1083,11 @@ int32_t mech_ctx_create(int32_t precision, int32_t device, MechContext** out) {
     c->device = device;
     c->precision = precision;
     cudaError_t e = cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking);
+    if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&c->side, cudaStreamNonBlocking);
+    if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&c->side2, cudaStreamNonBlocking);
+    if (e == cudaSuccess) e = cudaEventCreateWithFlags(&c->fork, cudaEventDisableTiming);
+    if (e == cudaSuccess) e = cudaEventCreateWithFlags(&c->join, cudaEventDisableTiming);
+    if (e == cudaSuccess) e = cudaEventCreateWithFlags(&c->join2, cudaEventDisableTiming);
     if (e != cudaSuccess) {
         delete c;
         return set_err(MECH_ERR_CUDA, cudaGetErrorString(e));
@@ -1085,6 +1099,8 @@ int32_t mech_ctx_create(int32_t precision, int32_t device, MechContext** out) {
 int32_t mech_ctx_destroy(MechContext* ctx) {
     if (!ctx) return MECH_OK;
     cudaSetDevice(ctx->device);
+    cudaStreamSynchronize(ctx->side);
+    cudaStreamSynchronize(ctx->side2);
     cudaStreamSynchronize(ctx->stream);
     delete ctx;
     return MECH_OK;
@@ -1267,8 +1283,8 @@ static int profile_impl(MechContext* c, int iters, MechProfile* o) {
         cudaEventElapsedTime(&ms, e0, e1);
         return ms / iters;
     };
-    o->ms_energy_eval = timeit([&] { launch_energy<Real>(n, -1, 0, s); });
-    o->ms_force_eval = timeit([&] { launch_forces<Real>(n, -1, s); });
+    o->ms_energy_eval = timeit([&] { launch_energy<Real>(n, -1, 0, c->lanes()); });
+    o->ms_force_eval = timeit([&] { launch_forces<Real>(n, -1, c->lanes()); });
     o->ms_fil_energy = timeit([&] { launch_part<Real>(n, 0, s); });
     o->ms_fil_force = timeit([&] { launch_part<Real>(n, 1, s); });
     o->ms_bond_energy = timeit([&] { launch_part<Real>(n, 2, s); });

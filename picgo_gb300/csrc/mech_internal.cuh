@@ -168,12 +168,20 @@ __device__ __forceinline__ Real* slot_ptr(const DevNet<Real>& n, int slot) {
 // `want` selects the replicas a launch works on: replicas whose phase equals
 // `want`, or every replica with active != 0 when want < 0.  `trial` evaluates
 // at x + lambda d instead of x.  Each returns the number of kernels launched.
-template <typename Real> int launch_energy(const DevNet<Real>& n, int want, int trial, cudaStream_t s);
-template <typename Real> int launch_forces(const DevNet<Real>& n, int want, cudaStream_t s);
+// An evaluation runs the excluded-volume chain on `side` and the linker,
+// motor and boundary kernel on `side2` while the filament kernel runs on
+// `main`; `fork` starts them, `join` / `join2` end them, then the reduction
+// runs on `main`.
+struct Lanes {
+    cudaStream_t main, side, side2;
+    cudaEvent_t fork, join, join2;
+};
+template <typename Real> int launch_energy(const DevNet<Real>& n, int want, int trial, const Lanes& L);
+template <typename Real> int launch_forces(const DevNet<Real>& n, int want, const Lanes& L);
 template <typename Real> int launch_direction(const DevNet<Real>& n, cudaStream_t s);
 template <typename Real> int launch_reset(const DevNet<Real>& n, cudaStream_t s);
 template <typename Real> int launch_dispatch_failed(const DevNet<Real>& n, cudaStream_t s);
-template <typename Real> int launch_recover(const DevNet<Real>& n, cudaStream_t s);
+template <typename Real> int launch_recover(const DevNet<Real>& n, const Lanes& L);
 template <typename Real> int launch_backup_restore(const DevNet<Real>& n, cudaStream_t s);
 // single kernel families in plain-evaluation mode, for profiling:
 // 0 filament energy, 1 filament force, 2 bond/boundary energy, 3 bond/boundary force
