@@ -304,6 +304,66 @@ def c3_report(seed: int = 20261203 + 1):
     return out
 
 
+def c5_report(n_params: int = 8, seed: int = 20261203 + 5):
+    """Implicit adjoint on the 2,000 x 30 network with 5,000 linkers (k ~ U(4, 12),
+    l0 ~ U(20, 40)): L = E(x*) + mean over filaments |end - start|^2; the adjoint
+    gradient of L in per-linker k and l0 against central differences
+    (h = 1e-4 relative, each side re-equilibrated from x*) on `n_params` random
+    parameters, FP64 engine."""
+    import numpy as np
+    from picgo_gb300 import Engine, make_network
+    from picgo_gb300.autograd import EquilibriumOptions, equilibrate
+    net = make_network("c5", seed=seed)
+    fcs = np.asarray(net.fil_cyl_start)
+    first, last = net.cyl_b1[fcs[:-1]], net.cyl_b2[fcs[1:] - 1]
+
+    def loss(x):
+        d = x[last] - x[first]
+        g = np.zeros_like(x)
+        np.add.at(g, last, 2.0 * d / len(first))
+        np.add.at(g, first, -2.0 * d / len(first))
+        return float((d * d).sum(1).mean()), g
+
+    k0 = np.asarray(net.lk_k, dtype=np.float64)
+    l00 = np.asarray(net.lk_l0, dtype=np.float64)
+    out = {"workload": "2,000 filaments x 30 cylinders (60,000 cylinders), 5,000 linkers k~U(4,12) l0~U(20,40)",
+           "seed": seed, "n_params": n_params}
+    with Engine("fp64") as eng:
+        eng.set_network(net)
+        t0 = time.perf_counter()
+        xs, es, info = equilibrate(eng, net.coord, k0, l00, EquilibriumOptions())
+        out["equilibrate_s"] = round(time.perf_counter() - t0, 2)
+        out["equilibrium_max_force_pN"] = info["max_force"]
+        lx, g = loss(xs)
+        t0 = time.perf_counter()
+        gk, gl, ainfo = eng.adjoint(g, 1.0)
+        out["adjoint_s"] = round(time.perf_counter() - t0, 3)
+        out["adjoint_cg"] = {k: ainfo[k] for k in ("iterations", "converged", "rel_residual")}
+        rng = np.random.default_rng(seed)
+        picks = rng.choice(len(k0), size=max(1, n_params // 2), replace=False)
+        fd_opts = EquilibriumOptions(rebuild_at_minimum=False)
+        rows, worst = [], 0.0
+        for j in picks:
+            for which in ("k", "l0"):
+                base = k0 if which == "k" else l00
+                h = 1e-4 * base[j]
+                vals = []
+                for sgn in (1, -1):
+                    p = base.copy()
+                    p[j] += sgn * h
+                    kk, ll = (p, l00) if which == "k" else (k0, p)
+                    xe, ee, _ = equilibrate(eng, xs, kk, ll, fd_opts)
+                    vals.append(ee + loss(xe)[0])
+                fd = (vals[0] - vals[1]) / (2 * h)
+                adj = float((gk if which == "k" else gl)[j])
+                rel = abs(adj - fd) / max(abs(fd), 1e-12)
+                worst = max(worst, rel)
+                rows.append({"param": f"{which}[{int(j)}]", "adjoint": adj, "fd": fd, "rel_err": rel})
+        out["checks"] = rows
+        out["max_rel_err"] = worst
+    return out
+
+
 def c4_report(n_replicas: int, precision: str = "mixed"):
     """Batched ensemble: `n_replicas` independent networks of uneven size
     (filaments log-uniform on 50-5,000, 20-50 cylinders each, C1 density)
@@ -417,6 +477,8 @@ def main():
     ap.add_argument("--no-fp64", action="store_true")
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--no-c3", action="store_true", help="skip the mixed-vs-FP64 end-state report on the small network")
+    ap.add_argument("--c5", type=int, default=0, metavar="P",
+                    help="only run the implicit-adjoint check on P parameters of the 2,000 x 30 network")
     ap.add_argument("--c4", type=int, default=0, metavar="R",
                     help="only run the batched-ensemble comparison on R replicas and print its JSON line")
     args = ap.parse_args()
@@ -427,6 +489,10 @@ def main():
         import torch.distributed as tdist
         tdist.init_process_group("nccl" if args.impl == "ours" else "gloo")
         dist = tdist
+    if args.c5 > 0:
+        if rank == 0:
+            print(json.dumps({"c5": c5_report(args.c5)}))
+        return
     if args.c4 > 0:
         if rank == 0:
             print(json.dumps({"c4": c4_report(args.c4, args.precision)}))
