@@ -339,13 +339,14 @@ __global__ void __launch_bounds__(kBlock) k_fil_force(DevNet<Real> n, int want) 
 
 // ---------------------------------------------------------------------------
 // Every bead adds its sparse contributions (contiguous, in the CSR order) to
-// its filament force, then the CG partials: max |F|, F.F, F.Fprev per tile;
-// the last tile of a replica (ticket) reduces them (finalize_force).
+// its filament force, then the CG partials: max |F|, F.F, F.Fprev per tile,
+// reduced by k_finalize_force (a per-tile completion ticket on one address
+// per replica would serialize thousands of atomics).
 // ---------------------------------------------------------------------------
 template <typename Real>
 __global__ void __launch_bounds__(kBlock) k_force_gather(DevNet<Real> n, int want) {
     __shared__ double sh[32 * 3];
-    __shared__ int s_go, s_fb, s_flag;
+    __shared__ int s_go, s_fb;
     const Tile t = n.ftile[blockIdx.x];
     const int r = t.replica;
     if (threadIdx.x == 0) {
@@ -382,8 +383,15 @@ __global__ void __launch_bounds__(kBlock) k_force_gather(DevNet<Real> n, int wan
         n.part_fil[4 * (size_t)blockIdx.x + 1] = red[1];
         n.part_fil[4 * (size_t)blockIdx.x + 2] = red[2];
     }
-    const RepTiles rt = n.rt[r];
-    if (last_tile(n.ticket, r, rt.fil_end - rt.fil_begin, &s_flag)) finalize_force(n, r, sh);
+}
+
+// One block per replica: max |F|, the dots and the CG step logic after the gather.
+template <typename Real>
+__global__ void __launch_bounds__(kBlock) k_finalize_force(DevNet<Real> n, int want) {
+    __shared__ double sh[32 * 3];
+    const int r = blockIdx.x;
+    if (!replica_selected(n.st[r], want)) return;
+    finalize_force(n, r, sh);
 }
 
 // One block per replica: the energy reduction and the line-search step, after
@@ -1188,7 +1196,8 @@ int launch_forces(const DevNet<Real>& n, int want, const Lanes& L) {
     cudaStreamWaitEvent(L.main, L.join, 0);
     cudaStreamWaitEvent(L.main, L.join2, 0);
     k_force_gather<Real><<<n.n_ftiles, kBlock, 0, L.main>>>(n, want);
-    return launched + 2;
+    k_finalize_force<Real><<<n.R, kBlock, 0, L.main>>>(n, want);
+    return launched + 3;
 }
 
 template <typename Real>
@@ -1241,7 +1250,8 @@ int launch_part(const DevNet<Real>& n, int which, cudaStream_t s) {
             if constexpr (sizeof(Real) == 4) k_fil_force_bulk<<<n.pgrid[1], kBlock, 0, s>>>(n, -1);
             else k_fil_force<Real><<<n.n_ftiles, kBlock, 0, s>>>(n, -1);
             k_force_gather<Real><<<n.n_ftiles, kBlock, 0, s>>>(n, -1);
-            return 2;
+            k_finalize_force<Real><<<n.R, kBlock, 0, s>>>(n, -1);
+            return 3;
         case 2: if (lm + bb_t > 0) { k_bond_bnd<Real><<<lm + bb_t, kBlock, 0, s>>>(n, -1, 0, 0, lm, ev_t); return 1; } return 0;
         case 3: if (lm + bb_t > 0) { k_bond_bnd<Real><<<lm + bb_t, kBlock, 0, s>>>(n, -1, 0, 1, lm, ev_t); return 1; } return 0;
     }
