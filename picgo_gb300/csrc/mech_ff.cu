@@ -802,49 +802,17 @@ __global__ void __launch_bounds__(kBlock) k_fil_force_bulk(DevNet<float> n, int 
 // Mixed engine: persistent direction update d = F + beta d with the d.F partials.
 __global__ void __launch_bounds__(kBlock) k_direction_mx(DevNet<float> n) {
     __shared__ double sh[32];
-    __shared__ int s_flag;
     const int t0 = blockIdx.x * n.ptiles[2], t1 = min(t0 + n.ptiles[2], n.n_ftiles);
     int cur = -1, first = 0, cnt = 0, fb = 0, xb = 0, bk = 0;
     bool go = false;
     float beta = 0.f;
     FF dF;
     const int ops[1] = {0};
-    auto finish = [&](int r) {
+    // the run's partial goes to slot 3 of its first tile
+    auto finish = [&](int) {
         double w[1] = {warp_sum_pair(dF)};
-        // the run's partial goes to slot 3 of its first tile (zeros elsewhere)
         block_combine<1>(w, ops, sh);
-        if (threadIdx.x == 0) {
-            n.part_fil[4 * (size_t)first + 3] = w[0];
-            __threadfence();
-            const RepTiles rt = n.rt[r];
-            const int old = atomicAdd(n.ticket + r, cnt);
-            s_flag = (old + cnt == rt.fil_end - rt.fil_begin);
-            if (s_flag) n.ticket[r] = 0;
-        }
-        __syncthreads();
-        if (s_flag) {
-            __threadfence();
-            const RepTiles rt = n.rt[r];
-            double a = 0.0;
-            const int nslot = run_slots(rt.fil_begin, rt.fil_end, n.ptiles[2]);
-            for (int k = threadIdx.x; k < nslot; k += blockDim.x)
-                a += __ldcg(n.part_fil + 4 * (size_t)run_slot(rt.fil_begin, n.ptiles[2], k) + 3);
-            const double slope = block_sum(a, sh);
-            if (threadIdx.x == 0) {
-                CGState& S = n.st[r];
-                if (S.backupPending) {
-                    S.backupValid = 1;
-                    S.backupPending = 0;
-                }
-                if (slope <= 0) {
-                    S.phase = PH_RESET;
-                } else {
-                    S.slope = slope;
-                    if (S.method >= 1) S.lastFdotF = S.newGrad;
-                    begin_iteration(S);
-                }
-            }
-        }
+        if (threadIdx.x == 0) n.part_fil[4 * (size_t)first + 3] = w[0];
     };
     for (int ti = t0; ti < t1; ++ti) {
         const Tile t = n.ftile[ti];
@@ -969,7 +937,7 @@ __global__ void __launch_bounds__(kBlock) k_bond_bnd(DevNet<Real> n, int want, i
 template <typename Real>
 __global__ void __launch_bounds__(kBlock) k_direction(DevNet<Real> n) {
     __shared__ double sh[32];
-    __shared__ int s_go, s_fb, s_xb, s_bk, s_flag;
+    __shared__ int s_go, s_fb, s_xb, s_bk;
     __shared__ double s_beta;
     const Tile t = n.ftile[blockIdx.x];
     const int r = t.replica;
@@ -998,22 +966,38 @@ __global__ void __launch_bounds__(kBlock) k_direction(DevNet<Real> n) {
     }
     const double sdF = block_sum_r(dF, sh);
     if (threadIdx.x == 0) n.part_fil[4 * (size_t)blockIdx.x + 3] = sdF;
+}
+
+// One block per replica after the direction update: the slope d.F, the
+// conjugacy test and the next iteration's start (CGMethod.hpp:1553-1560).
+template <typename Real>
+__global__ void __launch_bounds__(kBlock) k_finalize_direction(DevNet<Real> n) {
+    __shared__ double sh[32];
+    const int r = blockIdx.x;
+    if (n.st[r].phase != PH_DIR) return;
     const RepTiles rt = n.rt[r];
-    if (last_tile(n.ticket, r, rt.fil_end - rt.fil_begin, &s_flag)) {
-        const double slope = sum_slots(n.part_fil, 4, 3, rt.fil_begin, rt.fil_end, sh);
-        if (threadIdx.x == 0) {
-            CGState& S = n.st[r];
-            if (S.backupPending) {
-                S.backupValid = 1;
-                S.backupPending = 0;
-            }
-            if (slope <= 0) {          // conjugacy lost: reset to steepest descent
-                S.phase = PH_RESET;
-            } else {
-                S.slope = slope;
-                if (S.method >= 1) S.lastFdotF = S.newGrad;
-                begin_iteration(S);
-            }
+    double slope;
+    if constexpr (sizeof(Real) == 8) {
+        slope = sum_slots(n.part_fil, 4, 3, rt.fil_begin, rt.fil_end, sh);
+    } else {
+        double a = 0.0;
+        const int nslot = run_slots(rt.fil_begin, rt.fil_end, n.ptiles[2]);
+        for (int k = threadIdx.x; k < nslot; k += blockDim.x)
+            a += __ldcg(n.part_fil + 4 * (size_t)run_slot(rt.fil_begin, n.ptiles[2], k) + 3);
+        slope = block_sum(a, sh);
+    }
+    if (threadIdx.x == 0) {
+        CGState& S = n.st[r];
+        if (S.backupPending) {
+            S.backupValid = 1;
+            S.backupPending = 0;
+        }
+        if (slope <= 0) {          // conjugacy lost: reset to steepest descent
+            S.phase = PH_RESET;
+        } else {
+            S.slope = slope;
+            if (S.method >= 1) S.lastFdotF = S.newGrad;
+            begin_iteration(S);
         }
     }
 }
@@ -1204,7 +1188,8 @@ template <typename Real>
 int launch_direction(const DevNet<Real>& n, cudaStream_t s) {
     if constexpr (sizeof(Real) == 4) k_direction_mx<<<n.pgrid[2], kBlock, 0, s>>>(n);
     else k_direction<Real><<<n.n_ftiles, kBlock, 0, s>>>(n);
-    return 1;
+    k_finalize_direction<Real><<<n.R, kBlock, 0, s>>>(n);
+    return 2;
 }
 
 template <typename Real>
