@@ -274,9 +274,8 @@ struct FF {
         fast_two_sum(s, lo, h, l);
     }
 };
-// warp sum of (h, l) pairs; the double value is formed in lane 0 only
-__device__ __forceinline__ double warp_sum_pair(FF a) {
-    float s = a.h, e = a.l;
+// warp sum of (h, l) pairs in place, result in lane 0
+__device__ __forceinline__ void warp_reduce_pair(float& s, float& e) {
 #pragma unroll
     for (int o = 16; o > 0; o >>= 1) {
         const float s2 = __shfl_down_sync(0xffffffffu, s, o), e2 = __shfl_down_sync(0xffffffffu, e, o);
@@ -285,9 +284,52 @@ __device__ __forceinline__ double warp_sum_pair(FF a) {
         te = __fadd_rn(te, __fadd_rn(e, e2));
         fast_two_sum(t, te, s, e);
     }
+}
+// warp sum of (h, l) pairs; the double value is formed in lane 0 only
+__device__ __forceinline__ double warp_sum_pair(FF a) {
+    float s = a.h, e = a.l;
+    warp_reduce_pair(s, e);
     double r = 0.0;
     if ((threadIdx.x & 31) == 0) r = (double)s + (double)e;
     return r;
+}
+__device__ __forceinline__ float warp_max_f(float v) {
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) v = fmaxf(v, __shfl_down_sync(0xffffffffu, v, o));
+    return v;
+}
+// Block reduction with no double arithmetic: N compensated pairs and M maxima
+// of non-negative floats, in a fixed order; results valid in thread 0.  The
+// FP64 pipe runs at 1/64 of the FP32 rate on this part, so a per-tile double
+// tree costs more than the tile's loads.  `sh` holds 32 * (2N + M) floats.
+template <int N, int M>
+__device__ __forceinline__ void block_reduce_pairs(FF (&a)[N], float (&m)[M], float* sh) {
+    const int wi = threadIdx.x >> 5, l = threadIdx.x & 31, nw = blockDim.x >> 5;
+#pragma unroll
+    for (int k = 0; k < N; ++k) warp_reduce_pair(a[k].h, a[k].l);
+#pragma unroll
+    for (int k = 0; k < M; ++k) m[k] = warp_max_f(m[k]);
+    __syncthreads();
+    if (l == 0) {
+#pragma unroll
+        for (int k = 0; k < N; ++k) {
+            sh[(2 * k) * 32 + wi] = a[k].h;
+            sh[(2 * k + 1) * 32 + wi] = a[k].l;
+        }
+#pragma unroll
+        for (int k = 0; k < M; ++k) sh[(2 * N + k) * 32 + wi] = m[k];
+    }
+    __syncthreads();
+    if (wi == 0) {
+#pragma unroll
+        for (int k = 0; k < N; ++k) {
+            a[k].h = l < nw ? sh[(2 * k) * 32 + l] : 0.f;
+            a[k].l = l < nw ? sh[(2 * k + 1) * 32 + l] : 0.f;
+            warp_reduce_pair(a[k].h, a[k].l);
+        }
+#pragma unroll
+        for (int k = 0; k < M; ++k) m[k] = warp_max_f(l < nw ? sh[(2 * N + k) * 32 + l] : 0.f);
+    }
 }
 __device__ __forceinline__ double warp_max_lane0(float v) {
 #pragma unroll

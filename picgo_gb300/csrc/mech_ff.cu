@@ -158,21 +158,47 @@ __device__ void finalize_force(const DevNet<Real>& n, int r, double* sh) {
     const RepTiles rt = n.rt[r];
     const int stride = 1;   // k_force_gather writes one slot per tile
     const int nslot = run_slots(rt.fil_begin, rt.fil_end, stride);
-    double a_mx = 0.0, a_ff = 0.0, a_ffp = 0.0;
+    double mx, ff, ffp;
+    if constexpr (sizeof(Real) == 4) {
+        // mixed slots hold float maxima and (hi, lo) pairs; sum them compensated
+        // in single precision and form the doubles in thread 0 only
+        FF a[2];
+        float m[1] = {0.f};
 #pragma unroll 8
-    for (int k = threadIdx.x; k < nslot; k += blockDim.x) {
-        const int i = run_slot(rt.fil_begin, stride, k);
-        const double2 v = __ldcg(reinterpret_cast<const double2*>(n.part_fil + 4 * (size_t)i));
-        const double w = __ldcg(n.part_fil + 4 * (size_t)i + 2);
-        a_mx = fmax(a_mx, v.x);
-        a_ff += v.y;
-        a_ffp += w;
+        for (int k = threadIdx.x; k < nslot; k += blockDim.x) {
+            const float* p = reinterpret_cast<const float*>(n.part_fil + 4 * (size_t)run_slot(rt.fil_begin, stride, k));
+            const float4 v = __ldcg(reinterpret_cast<const float4*>(p));
+            const float w = __ldcg(p + 4);
+            m[0] = fmaxf(m[0], v.x);
+            a[0].add(v.y);
+            a[0].add(v.z);
+            a[1].add(v.w);
+            a[1].add(w);
+        }
+        block_reduce_pairs<2, 1>(a, m, reinterpret_cast<float*>(sh));
+        if (threadIdx.x != 0) return;
+        mx = (double)m[0];
+        ff = (double)a[0].h + (double)a[0].l;
+        ffp = (double)a[1].h + (double)a[1].l;
+    } else {
+        double a_mx = 0.0, a_ff = 0.0, a_ffp = 0.0;
+#pragma unroll 8
+        for (int k = threadIdx.x; k < nslot; k += blockDim.x) {
+            const int i = run_slot(rt.fil_begin, stride, k);
+            const double2 v = __ldcg(reinterpret_cast<const double2*>(n.part_fil + 4 * (size_t)i));
+            const double w = __ldcg(n.part_fil + 4 * (size_t)i + 2);
+            a_mx = fmax(a_mx, v.x);
+            a_ff += v.y;
+            a_ffp += w;
+        }
+        double red[3] = {warp_max(a_mx), warp_sum(a_ff), warp_sum(a_ffp)};
+        const int ops[3] = {1, 0, 0};
+        block_combine<3>(red, ops, sh);
+        mx = red[0];
+        ff = red[1];
+        ffp = red[2];
+        if (threadIdx.x != 0) return;
     }
-    double red[3] = {warp_max(a_mx), warp_sum(a_ff), warp_sum(a_ffp)};
-    const int ops[3] = {1, 0, 0};
-    block_combine<3>(red, ops, sh);
-    const double mx = red[0], ff = red[1], ffp = red[2];
-    if (threadIdx.x != 0) return;
     CGState& S = n.st[r];
     const int ph = S.phase;
     if (ph == PH_FORCE || ph == PH_RECOVER_FORCE) S.numForceCall++;
@@ -371,17 +397,34 @@ __global__ void __launch_bounds__(kBlock) k_force_gather(DevNet<Real> n, int wan
         Fo[0] = F[0];
         Fo[1] = F[1];
         Fo[2] = F[2];
-        mx = fmax(fmax(fabs(F[0]), fabs(F[1])), fabs(F[2]));
+        // a non-finite component makes the bead's max infinite (fmax would drop a NaN)
+        const bool fin = F[0] - F[0] == 0 && F[1] - F[1] == 0 && F[2] - F[2] == 0;
+        mx = fin ? fmax(fmax(fabs(F[0]), fabs(F[1])), fabs(F[2])) : Real(1.0 / 0.0);
         ff = bead_dot(F[0], F[1], F[2], F[0], F[1], F[2]);
         ffp = bead_dot(F[0], F[1], F[2], Fp[0], Fp[1], Fp[2]);
     }
-    double red[3] = {warp_max_r(mx), warp_sum_r(ff), warp_sum_r(ffp)};
-    const int ops[3] = {1, 0, 0};
-    block_combine<3>(red, ops, sh);
-    if (threadIdx.x == 0) {
-        n.part_fil[4 * (size_t)blockIdx.x + 0] = red[0];
-        n.part_fil[4 * (size_t)blockIdx.x + 1] = red[1];
-        n.part_fil[4 * (size_t)blockIdx.x + 2] = red[2];
+    if constexpr (sizeof(Real) == 4) {
+        // mixed: the tile's max and compensated (hi, lo) dot sums as floats in
+        // the tile's slots 0-2: {max, F.F hi, F.F lo, F.Fprev hi, F.Fprev lo}
+        FF a[2];
+        a[0].h = ff;
+        a[1].h = ffp;
+        float m[1] = {mx};
+        block_reduce_pairs<2, 1>(a, m, reinterpret_cast<float*>(sh));
+        if (threadIdx.x == 0) {
+            float* p = reinterpret_cast<float*>(n.part_fil + 4 * (size_t)blockIdx.x);
+            *reinterpret_cast<float4*>(p) = make_float4(m[0], a[0].h, a[0].l, a[1].h);
+            p[4] = a[1].l;
+        }
+    } else {
+        double red[3] = {warp_max_r(mx), warp_sum_r(ff), warp_sum_r(ffp)};
+        const int ops[3] = {1, 0, 0};
+        block_combine<3>(red, ops, sh);
+        if (threadIdx.x == 0) {
+            n.part_fil[4 * (size_t)blockIdx.x + 0] = red[0];
+            n.part_fil[4 * (size_t)blockIdx.x + 1] = red[1];
+            n.part_fil[4 * (size_t)blockIdx.x + 2] = red[2];
+        }
     }
 }
 
