@@ -248,8 +248,8 @@ typedef struct MechProfile {
     double ms_exvol_energy;        /* excluded volume (with its fallback check) */
     double ms_exvol_force;
     int64_t n_beads, n_exvol_pairs, n_boundary, n_linkers, n_motors, n_slots;
-    int64_t n_exvol_fp64_energy;   /* mixed engine: pairs its last energy pass sent to FP64 */
-    int64_t n_exvol_fp64_force;    /* and its last force pass */
+    int64_t n_exvol_ext_energy;    /* mixed engine: pairs its last energy pass sent to the extended-precision pass */
+    int64_t n_exvol_ext_force;     /* and its last force pass */
 } MechProfile;
 int32_t mech_profile(MechContext* ctx, int32_t iters, MechProfile* out);
 

@@ -91,8 +91,8 @@ class MechProfile(C.Structure):
                 ("ms_fil_force", C.c_double), ("ms_bond_energy", C.c_double), ("ms_bond_force", C.c_double),
                 ("ms_exvol_energy", C.c_double), ("ms_exvol_force", C.c_double), ("n_beads", C.c_int64),
                 ("n_exvol_pairs", C.c_int64), ("n_boundary", C.c_int64), ("n_linkers", C.c_int64),
-                ("n_motors", C.c_int64), ("n_slots", C.c_int64), ("n_exvol_fp64_energy", C.c_int64),
-                ("n_exvol_fp64_force", C.c_int64)]
+                ("n_motors", C.c_int64), ("n_slots", C.c_int64), ("n_exvol_ext_energy", C.c_int64),
+                ("n_exvol_ext_force", C.c_int64)]
 
 
 class MechSolveParams(C.Structure):

@@ -11,13 +11,16 @@
 // cross-product forms of the invariants; the 1/JJ * (sum) form still loses
 // accuracy as the normalized triple product q = |(v12 x v34) . v31| /
 // (|v12| |v34| |v31|) goes to zero (nearly coplanar or nearly touching
-// segments), so pairs with q under a threshold are evaluated in FP64 by a
-// second pass over a compacted list.  The reference's coplanarity move (forces
-// only) is decided and applied in single precision, except for pairs whose
-// test lies within rounding of its threshold, which go to the FP64 pass.
+// segments), so pairs with q under a threshold are evaluated again by an
+// extended-precision pass over a compacted list, in double-float arithmetic
+// (mech_df.cuh) rather than FP64, whose pipe is the slow one on this GPU.  The
+// reference's coplanarity move (forces only) is decided and applied in single
+// precision, except for pairs whose test lies within rounding of its
+// threshold, which go to the extended pass.
 #include <cuda_runtime.h>
 
 #include "mech_device.cuh"
+#include "mech_df.cuh"
 #include "mech_exvol_math.cuh"
 
 #ifndef MECH_EXVOL_REAL
@@ -29,14 +32,13 @@ namespace mech {
 constexpr int kFbNodesEnergy = 400;       // Simpson intervals, energy (:929-930)
 constexpr int kFbNodesForce = 10000;      // Simpson intervals, forces (:1041-1042)
 
-// `ref` selects the reference's forms (the FP64 engine, for parity);
-// otherwise the cancellation-free forms (the mixed engine's FP64 pass).
-static __device__ double pair_energy_d(const double* c1, const double* c2, const double* c3, const double* c4, double kRep,
-                                       bool ref = true) {
+// FP64 engine: the reference's forms, for parity.
+static __device__ double pair_energy_d(const double* c1, const double* c2, const double* c3, const double* c4,
+                                       double kRep) {
     double v12[3], v34[3], v31[3], v14[3], v32[3], v24[3];
     diffs_of(c1, c2, c3, c4, v12, v34, v31, v14, v32, v24);
     PairInv<double> p;
-    pair_inv(v12, v34, v31, v14, v32, v24, p, !ref);
+    pair_inv(v12, v34, v31, v14, v32, v24, p, false);
     return energy_from(p, kRep);
 }
 
@@ -44,7 +46,7 @@ static __device__ double pair_energy_d(const double* c1, const double* c2, const
 // FP64 forces of a pair at double positions, with the reference's coplanar
 // move of c2 (:610-626, force path only).
 static __device__ bool pair_forces_d(const double* c1, const double* c2in, const double* c3, const double* c4, double kRep,
-                                     double out[4][3], bool ref = true) {
+                                     double out[4][3]) {
     double moved2[3];
     const double* c2 = c2in;
     if (coplanarity<double>(c1, c2in, c3, c4) < 0.1) {
@@ -54,8 +56,8 @@ static __device__ bool pair_forces_d(const double* c1, const double* c2in, const
     double v12[3], v34[3], v31[3], v14[3], v32[3], v24[3];
     diffs_of(c1, c2, c3, c4, v12, v34, v31, v14, v32, v24);
     PairInv<double> p;
-    pair_inv(v12, v34, v31, v14, v32, v24, p, !ref);
-    return ref ? forces_from<false>(p, v12, v34, v31, kRep, out) : forces_from<true>(p, v12, v34, v31, kRep, out);
+    pair_inv(v12, v34, v31, v14, v32, v24, p, false);
+    return forces_from<false>(p, v12, v34, v31, kRep, out);
 }
 
 // ---------------------------------------------------------------------------
@@ -208,10 +210,10 @@ __device__ __forceinline__ void flag_fallback(const DevNet<Real>& n, int r, int 
     }
 }
 
-constexpr float kMixedTauEnergy = 0.005f;  // FP64 below this normalized triple product (energy)
+constexpr float kMixedTauEnergy = 0.005f;  // extended pass below this normalized triple product (energy)
 constexpr float kMixedTauForce = 0.02f;    // (forces, whose formula loses more to cancellation)
 
-// Warp-aggregated append of (replica, pair) to the FP64 pair list.
+// Warp-aggregated append of (replica, pair) to the extended-pass pair list.
 template <typename Real>
 __device__ __forceinline__ void append_fp64(const DevNet<Real>& n, bool need, int r, int pr) {
     const unsigned m = __ballot_sync(0xffffffffu, need);
@@ -296,7 +298,7 @@ __global__ void __launch_bounds__(kBlock) k_exvol(DevNet<Real> n, int want, int 
                 // the reference moves c2 0.01 nm along the unit normal of (c1, c2, c3)
                 // when it judges the pair coplanar (|n . v3| < 0.1 with
                 // n = (c2-c1) x (c3-c1), v3 = c4 - c1; :610-626).  Pairs whose test
-                // single precision cannot decide go to FP64; the others are moved
+                // single precision cannot decide go to the extended pass; the others are moved
                 // here (with q >= kMixedTauForce the move leaves them well conditioned).
                 const float nx = v12[1] * v31[2] - v12[2] * v31[1], ny = v12[2] * v31[0] - v12[0] * v31[2],
                             nz = v12[0] * v31[1] - v12[1] * v31[0];   // = -n
@@ -341,41 +343,80 @@ __global__ void __launch_bounds__(kBlock) k_exvol(DevNet<Real> n, int want, int 
     }
 }
 
-// Mixed engine: the listed pairs in FP64 with the reference's formulas.
+// Mixed engine's extended-precision pass: the listed pairs in double-float
+// arithmetic (about 48 bits, on the FP32 pipe) from the float-float positions,
+// with the cancellation-free invariants, the reference's coplanar move of c2
+// (:610-626, forces only; decided without divisions: |n . v3| < 0.1 |n| |v3|
+// squared) and the analytic formulas.  Pair k goes to warp k % W, lane k / W of
+// the W warps of the grid, so a short list spreads over every SM sub-partition.
+constexpr int kExtBlocks = 152;   // one 4-warp block per SM
 template <typename Real>
-__global__ void __launch_bounds__(128) k_exvol_fp64(DevNet<Real> n, int trial, int force) {
+__global__ void __launch_bounds__(128) k_exvol_ext(DevNet<Real> n, int trial, int force) {
     const int cnt = min(*n.ev_list_count, n.n_ev);
-    // pair k goes to block k % gridDim.x: a short list still spreads over every
-    // SM, whose FP64 pipes (not the threads) bound this kernel
-    for (int k = blockIdx.x + gridDim.x * threadIdx.x; k < cnt; k += gridDim.x * blockDim.x) {
+    const int W = (gridDim.x * blockDim.x) >> 5;
+    const int gw = (blockIdx.x * blockDim.x + threadIdx.x) >> 5, lane = threadIdx.x & 31;
+    for (int k = gw + W * lane; k < cnt; k += W * 32) {
         const int r = n.ev_list[2 * k], i = n.ev_list[2 * k + 1];
         const CGState& S = n.st[r];
         const Real* X = n.x[S.xbuf];
         const bool tr = trial != 0;
-        const double lam = S.lambda;
+        const float lf = (float)S.lambda;
         const int4 bs = n.ev_bead[i];
-        double c1[3], c2[3], c3[3], c4[3];
-        to_double(bead_at(X, n.d, bs.x, tr, lam), c1);
-        to_double(bead_at(X, n.d, bs.y, tr, lam), c2);
-        to_double(bead_at(X, n.d, bs.z, tr, lam), c3);
-        to_double(bead_at(X, n.d, bs.w, tr, lam), c4);
-        const double kRepD = (double)n.ev_k[i] * (double)n.ev_la[i] * (double)n.ev_lb[i];
-        if (!force) {
-            const double u = pair_energy_d(c1, c2, c3, c4, kRepD, false);
+        const int bead[4] = {bs.x, bs.y, bs.z, bs.w};
+        df c[4][3];
+#pragma unroll
+        for (int a = 0; a < 4; ++a) {
+            Pos<float> p = load_pos(X, bead[a]);
+            if (tr) p = moved_f(p, n.d, bead[a], lf);
+#pragma unroll
+            for (int q = 0; q < 3; ++q) c[a][q] = df(p.h[q], p.l[q]);
+        }
+        df v12[3], v34[3], v31[3], v14[3], v32[3], v24[3];
+#pragma unroll
+        for (int q = 0; q < 3; ++q) {
+            v12[q] = c[1][q] - c[0][q];
+            v34[q] = c[3][q] - c[2][q];
+            v31[q] = c[0][q] - c[2][q];
+            v14[q] = c[3][q] - c[0][q];
+            v32[q] = c[1][q] - c[2][q];
+            v24[q] = c[3][q] - c[1][q];
+        }
+        const df kRep = df(n.ev_k[i]) * df(n.ev_la[i]) * df(n.ev_lb[i]);
+        if (force) {
+            // n = (c2 - c1) x (c3 - c1) = -(v12 x v31), v3 = c4 - c1 = v14
+            const df nx = v12[2] * v31[1] - v12[1] * v31[2], ny = v12[0] * v31[2] - v12[2] * v31[0],
+                     nz = v12[1] * v31[0] - v12[0] * v31[1];
+            const df nn = nx * nx + ny * ny + nz * nz;
+            const df nv = nx * v14[0] + ny * v14[1] + nz * v14[2];
+            if (nv * nv < df(0.01) * nn * dot3(v14, v14)) {
+                const df s = df(0.01) / sqrt(nn);
+                const df dn[3] = {s * nx, s * ny, s * nz};
+#pragma unroll
+                for (int q = 0; q < 3; ++q) {
+                    v12[q] = v12[q] + dn[q];
+                    v32[q] = v32[q] + dn[q];
+                    v24[q] = v24[q] - dn[q];
+                }
+            }
+            PairInv<df> p;
+            pair_inv(v12, v34, v31, v14, v32, v24, p, true);
+            df out[4][3];
+            const bool ok = forces_from<true>(p, v12, v34, v31, kRep, out);
+            for (int a = 0; a < 4; ++a) {
+                Real* cdst = slot_ptr(n, n.slot_base[K_EXVOL] + 4 * i + a);
+                for (int q = 0; q < 3; ++q) cdst[q] = (Real)out[a][q].to_float();
+            }
+            if (!ok) flag_fallback(n, r, i, 0.0);
+        } else {
+            PairInv<df> p;
+            pair_inv(v12, v34, v31, v14, v32, v24, p, true);
+            const double u = energy_from(p, kRep);
             if (u != u) {
-                flag_fallback(n, r, i, tr ? lam : 0.0);
+                flag_fallback(n, r, i, tr ? S.lambda : 0.0);
                 n.ev_energy[i] = 0.0;
             } else {
                 n.ev_energy[i] = u;
             }
-        } else {
-            double out[4][3];
-            const bool ok = pair_forces_d(c1, c2, c3, c4, kRepD, out, false);
-            for (int a = 0; a < 4; ++a) {
-                Real* cdst = slot_ptr(n, n.slot_base[K_EXVOL] + 4 * i + a);
-                for (int q = 0; q < 3; ++q) cdst[q] = (Real)out[a][q];
-            }
-            if (!ok) flag_fallback(n, r, i, 0.0);
         }
     }
 }
@@ -403,7 +444,7 @@ __global__ void __launch_bounds__(kBlock) k_exvol_energy_tail(DevNet<Real> n, in
     if (threadIdx.x == 0) n.part_sp[ti] = e;
 }
 
-// zero the FP64-pass and fallback work-list counts (one memset when they are
+// zero the extended-pass and fallback work-list counts (one memset when they are
 // neighbours in one buffer)
 template <typename Real>
 static inline void reset_counts(const DevNet<Real>& n, cudaStream_t s) {
@@ -429,8 +470,8 @@ int launch_exvol_energy(const DevNet<Real>& n, int want, int trial, cudaStream_t
     reset_counts(n, s);
     k_exvol<Real><<<nt, kBlock, 0, s>>>(n, want, trial, 0, off);
     int k = 1;
-    if (sizeof(Real) == 4) {
-        k_exvol_fp64<Real><<<2 * 152, 128, 0, s>>>(n, trial, 0);
+    if constexpr (sizeof(Real) == 4) {
+        k_exvol_ext<Real><<<kExtBlocks, 128, 0, s>>>(n, trial, 0);
         ++k;
     }
     k_exvol_energy_tail<Real><<<kFbEnergyBlocks + (sizeof(Real) == 4 ? nt : 0), kBlock, 0, s>>>(n, want, off);
@@ -445,8 +486,8 @@ int launch_exvol_forces(const DevNet<Real>& n, int want, cudaStream_t s) {
     reset_counts(n, s);
     k_exvol<Real><<<nt, kBlock, 0, s>>>(n, want, 0, 1, off);
     int k = 1;
-    if (sizeof(Real) == 4) {
-        k_exvol_fp64<Real><<<2 * 152, 128, 0, s>>>(n, 0, 1);
+    if constexpr (sizeof(Real) == 4) {
+        k_exvol_ext<Real><<<kExtBlocks, 128, 0, s>>>(n, 0, 1);
         ++k;
     }
     k_exvol_fb_force<Real><<<4 * 152, kBlock, 0, s>>>(n, n.fb_moments, n.fb_tickets);

@@ -1273,14 +1273,31 @@ static int profile_impl(MechContext* c, int iters, MechProfile* o) {
     cudaEvent_t e0, e1;
     CU(cudaEventCreate(&e0));
     CU(cudaEventCreate(&e1));
+    // Each evaluation is captured once as a CUDA graph and replayed, the way
+    // the minimizer runs it: direct launches of a three-lane evaluation are
+    // bound by the host's launch rate, not by the device.
+    cudaError_t gerr = cudaSuccess;
     auto timeit = [&](auto&& fn) -> double {
-        fn();   // warm
-        cudaEventRecord(e0, s);
-        for (int i = 0; i < iters; ++i) fn();
-        cudaEventRecord(e1, s);
-        cudaEventSynchronize(e1);
+        cudaGraph_t g = nullptr;
+        cudaGraphExec_t ge = nullptr;
+        cudaError_t e = cudaStreamBeginCapture(s, cudaStreamCaptureModeThreadLocal);
+        if (e == cudaSuccess) {
+            fn();
+            e = cudaStreamEndCapture(s, &g);
+        }
+        if (e == cudaSuccess) e = cudaGraphInstantiate(&ge, g, 0);
         float ms = 0.f;
-        cudaEventElapsedTime(&ms, e0, e1);
+        if (e == cudaSuccess) e = cudaGraphLaunch(ge, s);   // warm
+        if (e == cudaSuccess) {
+            cudaEventRecord(e0, s);
+            for (int i = 0; i < iters && e == cudaSuccess; ++i) e = cudaGraphLaunch(ge, s);
+            cudaEventRecord(e1, s);
+            if (e == cudaSuccess) e = cudaEventSynchronize(e1);
+            if (e == cudaSuccess) cudaEventElapsedTime(&ms, e0, e1);
+        }
+        if (ge) cudaGraphExecDestroy(ge);
+        if (g) cudaGraphDestroy(g);
+        if (e != cudaSuccess && gerr == cudaSuccess) gerr = e;
         return ms / iters;
     };
     o->ms_energy_eval = timeit([&] { launch_energy<Real>(n, -1, 0, c->lanes()); });
@@ -1292,12 +1309,13 @@ static int profile_impl(MechContext* c, int iters, MechProfile* o) {
     int cnt = 0;
     o->ms_exvol_energy = timeit([&] { launch_exvol_energy<Real>(n, -1, 0, s); });
     cudaMemcpy(&cnt, c->ev_list_count.p, sizeof(int), cudaMemcpyDeviceToHost);
-    o->n_exvol_fp64_energy = c->precision == MECH_PREC_MIXED ? cnt : c->nev;
+    o->n_exvol_ext_energy = c->precision == MECH_PREC_MIXED ? cnt : c->nev;
     o->ms_exvol_force = timeit([&] { launch_exvol_forces<Real>(n, -1, s); });
     cudaMemcpy(&cnt, c->ev_list_count.p, sizeof(int), cudaMemcpyDeviceToHost);
-    o->n_exvol_fp64_force = c->precision == MECH_PREC_MIXED ? cnt : c->nev;
+    o->n_exvol_ext_force = c->precision == MECH_PREC_MIXED ? cnt : c->nev;
     cudaEventDestroy(e0);
     cudaEventDestroy(e1);
+    CU(gerr);
     CU(cudaGetLastError());
     o->n_beads = c->nb;
     o->n_exvol_pairs = c->nev;
