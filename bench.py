@@ -223,6 +223,8 @@ def run_ours(args, rank, world, dist):
                    "tuning": {k: (round(v, 4) if isinstance(v, float) else v) for k, v in tuning.items()}},
         "time_to_1pN_s": round(ms_per_step / 1e3, 4),
         "cg_iterations": results[-1]["num_iter"], "force_calls_per_step": results[-1]["num_force_call"],
+        "energy_evals_per_step": results[-1]["num_energy_eval"],
+        "line_search_trials_per_step": results[-1]["num_line_search_trials"],
         "final_max_force_pN": results[-1]["grad_inf_norm"],
         "e2e": {"value": round(e2e_value * world, 2), "unit": UNIT, "h2d_bytes_per_step": int(net.n_beads * 24),
                 "d2h_bytes_per_step": int(net.n_beads * 24)},

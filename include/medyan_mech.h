@@ -234,9 +234,10 @@ int32_t mech_reset_coords(MechContext* ctx);
 
 /*
  * Average device time per launch (milliseconds, CUDA events on the context's
- * stream) of the evaluation kernels at the current coordinates, each launched
- * `iters` times in plain-evaluation mode: a full energy evaluation, a full
- * force evaluation, and their parts.
+ * stream) of the evaluation kernels at the current coordinates, each captured
+ * once as a CUDA graph and replayed `iters` times in plain-evaluation mode: a
+ * full energy evaluation, a full force evaluation, their parts, and an idle
+ * iteration block.
  */
 typedef struct MechProfile {
     double ms_energy_eval;         /* all kernels of one energy evaluation */
@@ -250,6 +251,12 @@ typedef struct MechProfile {
     int64_t n_beads, n_exvol_pairs, n_boundary, n_linkers, n_motors, n_slots;
     int64_t n_exvol_ext_energy;    /* mixed engine: pairs its last energy pass sent to the extended-precision pass */
     int64_t n_exvol_ext_force;     /* and its last force pass */
+    double ms_iteration_idle;      /* one minimizer iteration block (two line-search trials, forces,
+                                      direction, failure dispatch, reset) with no replica selected:
+                                      the cost of the launches that find nothing to do */
+    double ms_trial_energy_eval;   /* one line-search trial: energy at x + lambda d, trial positions written */
+    int64_t n_exvol_fallback_energy;   /* pairs the last energy pass sent to the Simpson fallback */
+    int64_t n_exvol_fallback_force;    /* and the last force pass */
 } MechProfile;
 int32_t mech_profile(MechContext* ctx, int32_t iters, MechProfile* out);
 

@@ -92,7 +92,9 @@ class MechProfile(C.Structure):
                 ("ms_exvol_energy", C.c_double), ("ms_exvol_force", C.c_double), ("n_beads", C.c_int64),
                 ("n_exvol_pairs", C.c_int64), ("n_boundary", C.c_int64), ("n_linkers", C.c_int64),
                 ("n_motors", C.c_int64), ("n_slots", C.c_int64), ("n_exvol_ext_energy", C.c_int64),
-                ("n_exvol_ext_force", C.c_int64)]
+                ("n_exvol_ext_force", C.c_int64), ("ms_iteration_idle", C.c_double),
+                ("ms_trial_energy_eval", C.c_double), ("n_exvol_fallback_energy", C.c_int64),
+                ("n_exvol_fallback_force", C.c_int64)]
 
 
 class MechSolveParams(C.Structure):

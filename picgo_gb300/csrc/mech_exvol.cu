@@ -11,16 +11,14 @@
 // cross-product forms of the invariants; the 1/JJ * (sum) form still loses
 // accuracy as the normalized triple product q = |(v12 x v34) . v31| /
 // (|v12| |v34| |v31|) goes to zero (nearly coplanar or nearly touching
-// segments), so pairs with q under a threshold are evaluated again by an
-// extended-precision pass over a compacted list, in double-float arithmetic
-// (mech_df.cuh) rather than FP64, whose pipe is the slow one on this GPU.  The
-// reference's coplanarity move (forces only) is decided and applied in single
-// precision, except for pairs whose test lies within rounding of its
-// threshold, which go to the extended pass.
+// segments), so pairs with q under a threshold are evaluated again in FP64 by
+// an extended pass over a compacted list (k_exvol_ext, shaped around this
+// GPU's FP64 pipe).  The reference's coplanarity move (forces only) is decided
+// and applied in single precision, except for pairs whose test lies within
+// rounding of its threshold, which go to the extended pass.
 #include <cuda_runtime.h>
 
 #include "mech_device.cuh"
-#include "mech_df.cuh"
 #include "mech_exvol_math.cuh"
 
 #ifndef MECH_EXVOL_REAL
@@ -238,6 +236,7 @@ __global__ void __launch_bounds__(kBlock) k_exvol(DevNet<Real> n, int want, int 
     __shared__ double sh[32];
     __shared__ int s_go, s_xb;
     __shared__ double s_lam;
+    __shared__ float s_lf;   // the step rounded once (mixed engine)
     const int ti = tile_off + blockIdx.x;
     const Tile t = n.stile[ti];
     const int r = t.replica;
@@ -246,6 +245,7 @@ __global__ void __launch_bounds__(kBlock) k_exvol(DevNet<Real> n, int want, int 
         s_go = want < 0 ? (S.active != 0) : (S.phase == want);
         s_xb = S.xbuf;
         s_lam = S.lambda;
+        s_lf = (float)S.lambda;
     }
     __syncthreads();
     if (!s_go) return;
@@ -257,10 +257,17 @@ __global__ void __launch_bounds__(kBlock) k_exvol(DevNet<Real> n, int want, int 
     bool need64 = false;
     if (valid) {
         const int4 bs = n.ev_bead[i];
-        const Pos<Real> p1 = bead_at(X, n.d, bs.x, tr, s_lam), p2 = bead_at(X, n.d, bs.y, tr, s_lam);
-        const Pos<Real> p3 = bead_at(X, n.d, bs.z, tr, s_lam), p4 = bead_at(X, n.d, bs.w, tr, s_lam);
-        const double kRepD = (double)n.ev_k[i] * (double)n.ev_la[i] * (double)n.ev_lb[i];
+        auto pos = [&](int b) -> Pos<Real> {
+            if constexpr (sizeof(Real) == 4) {
+                const Pos<float> p = load_pos(X, b);
+                return tr ? moved_f(p, n.d, b, s_lf) : p;
+            } else {
+                return bead_at(X, n.d, b, tr, s_lam);
+            }
+        };
+        const Pos<Real> p1 = pos(bs.x), p2 = pos(bs.y), p3 = pos(bs.z), p4 = pos(bs.w);
         if constexpr (sizeof(Real) == 8) {
+            const double kRepD = (double)n.ev_k[i] * (double)n.ev_la[i] * (double)n.ev_lb[i];
             // FP64 engine: the reference's formulas, every pair
             double c1[3], c2[3], c3[3], c4[3];
             to_double(p1, c1);
@@ -282,6 +289,7 @@ __global__ void __launch_bounds__(kBlock) k_exvol(DevNet<Real> n, int want, int 
             }
         } else {
             // mixed engine: single precision unless the pair is ill-conditioned
+            const float kRep = n.ev_k[i] * n.ev_la[i] * n.ev_lb[i];
             float v12[3], v34[3], v31[3], v14[3], v32[3], v24[3];
             pdiff(p2, p1, v12);
             pdiff(p4, p3, v34);
@@ -318,12 +326,12 @@ __global__ void __launch_bounds__(kBlock) k_exvol(DevNet<Real> n, int want, int 
                 PairInv<float> pi;
                 pair_inv(v12, v34, v31, v14, v32, v24, pi, true);
                 if (!force) {
-                    const double u = energy_from(pi, (float)kRepD);
+                    const double u = energy_from(pi, kRep);
                     if (u != u) need64 = true;
                     else e = u;
                 } else {
                     float out[4][3];
-                    if (forces_from<true>(pi, v12, v34, v31, (float)kRepD, out)) {
+                    if (forces_from<true>(pi, v12, v34, v31, kRep, out)) {
                         for (int a = 0; a < 4; ++a) {
                             Real* cdst = slot_ptr(n, n.slot_base[K_EXVOL] + 4 * i + a);
                             for (int k = 0; k < 3; ++k) cdst[k] = (Real)out[a][k];
@@ -343,81 +351,217 @@ __global__ void __launch_bounds__(kBlock) k_exvol(DevNet<Real> n, int want, int 
     }
 }
 
-// Mixed engine's extended-precision pass: the listed pairs in double-float
-// arithmetic (about 48 bits, on the FP32 pipe) from the float-float positions,
-// with the cancellation-free invariants, the reference's coplanar move of c2
-// (:610-626, forces only; decided without divisions: |n . v3| < 0.1 |n| |v3|
-// squared) and the analytic formulas.  Pair k goes to warp k % W, lane k / W of
-// the W warps of the grid, so a short list spreads over every SM sub-partition.
-constexpr int kExtBlocks = 152;   // one 4-warp block per SM
+// Mixed engine's extended pass: the listed (ill-conditioned) pairs in FP64,
+// split over the four warps of a block.  On this GPU a warp's FP64
+// instruction holds its SM sub-partition's FP64 pipe for ~78 cycles whatever
+// the number of active lanes, so the time of the pass is the FP64 instruction
+// count of one warp's path, not the pair count: one pair's ~1,000 FP64
+// operations in one warp took ~35 us.  Here lane l of every warp takes pair
+// 32 g + l of the block's group g, and warp w evaluates the w-th of the four
+// arctangent terms of the integral (A, E, B, F below: cross product, norm,
+// numerator, arctangent and, for forces, its partial derivatives); the shared
+// invariants are formed by every warp, the six entries of the G matrix are
+// split over the warps, and warp w forms the force on bead w.  Partial results
+// pass through shared memory.  The cancellation-free forms of pair_inv
+// (cross = true) and forces_from<true> are followed term by term, with the
+// reference's coplanar move of c2 (:610-626, forces only, decided without
+// divisions: (n . v3)^2 < 0.01 |n|^2 |v3|^2).
+constexpr int kExtBlocks = 152;   // one 4-warp block per SM: one warp per sub-partition
+
+// per-term operands: cross product u x v, arctangent argument p . q (negated for B, F),
+// and the two arctangent abscissae alpha, beta (A: a+e, e; E: a+e-d, e-d; B: F, F-b; F: d+F, d+F-b)
+struct ExtTerm {
+    double N, rY, ATG, tN, tXr, tlo, thi, S;
+};
+
 template <typename Real>
 __global__ void __launch_bounds__(128) k_exvol_ext(DevNet<Real> n, int trial, int force) {
+    __shared__ double s_c[4][32][3];       // bead positions
+    __shared__ double s_N[3][32];          // CC, GG, DD for the F term's HH
+    __shared__ ExtTerm s_t[4][32];
+    __shared__ double s_G[6][32];
+    __shared__ int s_bad[32];
     const int cnt = min(*n.ev_list_count, n.n_ev);
-    const int W = (gridDim.x * blockDim.x) >> 5;
-    const int gw = (blockIdx.x * blockDim.x + threadIdx.x) >> 5, lane = threadIdx.x & 31;
-    for (int k = gw + W * lane; k < cnt; k += W * 32) {
-        const int r = n.ev_list[2 * k], i = n.ev_list[2 * k + 1];
-        const CGState& S = n.st[r];
-        const Real* X = n.x[S.xbuf];
-        const bool tr = trial != 0;
-        const float lf = (float)S.lambda;
-        const int4 bs = n.ev_bead[i];
-        const int bead[4] = {bs.x, bs.y, bs.z, bs.w};
-        df c[4][3];
-#pragma unroll
-        for (int a = 0; a < 4; ++a) {
-            Pos<float> p = load_pos(X, bead[a]);
-            if (tr) p = moved_f(p, n.d, bead[a], lf);
-#pragma unroll
-            for (int q = 0; q < 3; ++q) c[a][q] = df(p.h[q], p.l[q]);
+    const int w = threadIdx.x >> 5, l = threadIdx.x & 31;
+    const int ngroups = (cnt + 31) >> 5;
+    for (int g = blockIdx.x; g < ngroups; g += gridDim.x) {
+        const int k = 32 * g + l;
+        const bool valid = k < cnt;
+        int r = 0, i = 0;
+        if (valid) {
+            r = n.ev_list[2 * k];
+            i = n.ev_list[2 * k + 1];
         }
-        df v12[3], v34[3], v31[3], v14[3], v32[3], v24[3];
-#pragma unroll
-        for (int q = 0; q < 3; ++q) {
-            v12[q] = c[1][q] - c[0][q];
-            v34[q] = c[3][q] - c[2][q];
-            v31[q] = c[0][q] - c[2][q];
-            v14[q] = c[3][q] - c[0][q];
-            v32[q] = c[1][q] - c[2][q];
-            v24[q] = c[3][q] - c[1][q];
+        // ---- positions: warp w converts bead w of every pair
+        if (valid) {
+            const CGState& S = n.st[r];
+            const int4 bs = n.ev_bead[i];
+            const int bead = w == 0 ? bs.x : w == 1 ? bs.y : w == 2 ? bs.z : bs.w;
+            double c[3];
+            to_double(bead_at(n.x[S.xbuf], n.d, bead, trial != 0, S.lambda), c);
+            s_c[w][l][0] = c[0];
+            s_c[w][l][1] = c[1];
+            s_c[w][l][2] = c[2];
         }
-        const df kRep = df(n.ev_k[i]) * df(n.ev_la[i]) * df(n.ev_lb[i]);
-        if (force) {
-            // n = (c2 - c1) x (c3 - c1) = -(v12 x v31), v3 = c4 - c1 = v14
-            const df nx = v12[2] * v31[1] - v12[1] * v31[2], ny = v12[0] * v31[2] - v12[2] * v31[0],
-                     nz = v12[1] * v31[0] - v12[0] * v31[1];
-            const df nn = nx * nx + ny * ny + nz * nz;
-            const df nv = nx * v14[0] + ny * v14[1] + nz * v14[2];
-            if (nv * nv < df(0.01) * nn * dot3(v14, v14)) {
-                const df s = df(0.01) / sqrt(nn);
-                const df dn[3] = {s * nx, s * ny, s * nz};
+        if (w == 0) s_bad[l] = 0;
+        __syncthreads();
+        double v12[3], v34[3], v31[3], v14[3], v32[3], v24[3];
+        double a = 0, b = 0, c = 0, d = 0, e = 0, F = 0, JJ = 1, kRep = 0;
+        double x21[3] = {0, 0, 0};
+        if (valid) {
 #pragma unroll
-                for (int q = 0; q < 3; ++q) {
-                    v12[q] = v12[q] + dn[q];
-                    v32[q] = v32[q] + dn[q];
-                    v24[q] = v24[q] - dn[q];
+            for (int q = 0; q < 3; ++q) {
+                const double c1 = s_c[0][l][q], c2 = s_c[1][l][q], c3 = s_c[2][l][q], c4 = s_c[3][l][q];
+                v12[q] = c2 - c1;
+                v34[q] = c4 - c3;
+                v31[q] = c1 - c3;
+                v14[q] = c4 - c1;
+                v32[q] = c2 - c3;
+                v24[q] = c4 - c2;
+            }
+            if (force) {
+                // n = (c2 - c1) x (c3 - c1) = -(v12 x v31), v3 = c4 - c1 = v14
+                const double nx = v12[2] * v31[1] - v12[1] * v31[2], ny = v12[0] * v31[2] - v12[2] * v31[0],
+                             nz = v12[1] * v31[0] - v12[0] * v31[1];
+                const double nn = nx * nx + ny * ny + nz * nz, nv = nx * v14[0] + ny * v14[1] + nz * v14[2];
+                if (nv * nv < 0.01 * nn * dot3(v14, v14)) {
+                    const double sc = 0.01 / sqrt(nn);
+                    const double dn[3] = {sc * nx, sc * ny, sc * nz};
+#pragma unroll
+                    for (int q = 0; q < 3; ++q) {
+                        v12[q] += dn[q];
+                        v32[q] += dn[q];
+                        v24[q] -= dn[q];
+                    }
                 }
             }
-            PairInv<df> p;
-            pair_inv(v12, v34, v31, v14, v32, v24, p, true);
-            df out[4][3];
-            const bool ok = forces_from<true>(p, v12, v34, v31, kRep, out);
-            for (int a = 0; a < 4; ++a) {
-                Real* cdst = slot_ptr(n, n.slot_base[K_EXVOL] + 4 * i + a);
-                for (int q = 0; q < 3; ++q) cdst[q] = (Real)out[a][q].to_float();
+            a = dot3(v12, v12);
+            b = dot3(v34, v34);
+            c = dot3(v31, v31);
+            d = dot3(v12, v34);
+            e = dot3(v12, v31);
+            F = dot3(v34, v31);
+            x21[0] = v34[1] * v12[2] - v34[2] * v12[1];
+            x21[1] = v34[2] * v12[0] - v34[0] * v12[2];
+            x21[2] = v34[0] * v12[1] - v34[1] * v12[0];
+            const double trip = -(x21[0] * v31[0] + x21[1] * v31[1] + x21[2] * v31[2]);
+            JJ = -trip * trip;
+            kRep = (double)n.ev_k[i] * (double)n.ev_la[i] * (double)n.ev_lb[i];
+        }
+        // ---- term w: cross product, norm, numerator
+        double xu[3] = {0, 0, 0}, Y = 1, N = 0;
+        if (valid) {
+            double u[3], v[3];
+#pragma unroll
+            for (int q = 0; q < 3; ++q) {   // selects, not pointers: the vectors stay in registers
+                u[q] = w < 2 ? v12[q] : v34[q];
+                v[q] = w == 0 ? v31[q] : w == 1 ? v14[q] : w == 2 ? v31[q] : v32[q];
             }
-            if (!ok) flag_fallback(n, r, i, 0.0);
-        } else {
-            PairInv<df> p;
-            pair_inv(v12, v34, v31, v14, v32, v24, p, true);
-            const double u = energy_from(p, kRep);
-            if (u != u) {
-                flag_fallback(n, r, i, tr ? S.lambda : 0.0);
-                n.ev_energy[i] = 0.0;
-            } else {
-                n.ev_energy[i] = u;
+            xu[0] = u[1] * v[2] - u[2] * v[1];
+            xu[1] = u[2] * v[0] - u[0] * v[2];
+            xu[2] = u[0] * v[1] - u[1] * v[0];
+            Y = sqrt(dot3(xu, xu));
+            if (w < 3) {
+                N = dot3(xu, x21);   // CC = x13 . x21, GG = x14 . x21, DD = x21 . x23
+                s_N[w][l] = N;
             }
         }
+        __syncthreads();
+        if (valid) {
+            if (w == 3) N = s_N[0][l] + s_N[1][l] - s_N[2][l];   // HH = CC + GG - DD
+            double p[3], q[3];
+#pragma unroll
+            for (int j = 0; j < 3; ++j) {
+                p[j] = w == 0 ? v31[j] : w == 1 ? v14[j] : w == 2 ? v31[j] : v32[j];
+                q[j] = w == 0 ? v32[j] : w == 1 ? v24[j] : w == 2 ? v14[j] : v24[j];
+            }
+            const double arg = w < 2 ? dot3(p, q) : -dot3(p, q);
+            ExtTerm t;
+            t.N = N;
+            t.ATG = atan2(Y, arg);
+            t.rY = 1.0 / Y;
+            t.S = N * t.rY * t.ATG;
+            if (force) {
+                const double al = w == 0 ? a + e : w == 1 ? a + e - d : w == 2 ? F : d + F;
+                const double be = al - (w < 2 ? a : b);
+                const double Y2 = Y * Y;
+                const double T1 = Y2 / (Y2 + al * al), T2 = Y2 / (Y2 + be * be);
+                const double r2 = t.rY * t.rY;
+                t.tN = t.ATG * t.rY;
+                const double tX = -(t.ATG * N) * r2 + ((-T1 * al + T2 * be) * N) * (r2 * t.rY);
+                t.tXr = tX * t.rY;
+                t.tlo = ((T1 - T2) * N) * r2;
+                t.thi = (T1 * N) * r2;
+            }
+            s_t[w][l] = t;
+        }
+        __syncthreads();
+        if (!force) {
+            if (w == 0 && valid) {
+                const double Ssum = s_t[0][l].S + s_t[1][l].S + s_t[2][l].S + s_t[3][l].S;
+                const double U = 0.5 * kRep / JJ * Ssum;
+                if (!(fabs(U) < 1.0 / 0.0) || U < -1.0) {
+                    flag_fallback(n, r, i, trial != 0 ? n.st[r].lambda : 0.0);
+                    n.ev_energy[i] = 0.0;
+                } else {
+                    n.ev_energy[i] = U;
+                }
+            }
+            __syncthreads();   // shared arrays are reused by the next group
+            continue;
+        }
+        // ---- G entries, split over the warps (0: G00, G12; 1: G01, G22; 2: G02; 3: G11)
+        if (valid) {
+            const ExtTerm A = s_t[0][l], E = s_t[1][l], B = s_t[2][l], FT = s_t[3][l];
+            if (w == 0) {
+                s_G[0][l] = A.tN * (-2 * F) + A.tXr * c + A.thi * 2 + E.tN * (2 * (F - b)) + E.tXr * (b + c - 2 * F) +
+                            E.thi * 2 + FT.tN * (-2 * b) + FT.tXr * b;
+                s_G[4][l] = A.tN * (-a) + E.tN * a + E.tXr * (-a) + B.tN * (-d) + B.tXr * (-F) + B.tlo + FT.tN * d +
+                            FT.tXr * (-(d + F)) + FT.tlo;
+            } else if (w == 1) {
+                s_G[1][l] = A.tN * e + E.tN * (2 * d - e) + E.tXr * (e - d) - E.tlo + B.tN * (-F) + FT.tN * (2 * d + F) +
+                            FT.tXr * (-(d + F)) + FT.tlo;
+                s_G[5][l] = A.tXr * a + E.tXr * a + B.tXr * b + FT.tXr * b;
+            } else if (w == 2) {
+                s_G[2][l] = A.tN * d + A.tXr * (-e) + A.tlo + E.tN * (-d) + E.tXr * (-(e - d)) + E.tlo + B.tN * b +
+                            FT.tN * (-b) + FT.tXr * b;
+            } else {
+                s_G[3][l] = E.tN * (-2 * a) + E.tXr * a + B.tN * (2 * e) + B.tXr * c + B.tlo * (-2) + B.thi * 2 +
+                            FT.tN * (-2 * (a + e)) + FT.tXr * (a + c + 2 * e) + FT.tlo * (-2) + FT.thi * 2;
+            }
+        }
+        __syncthreads();
+        // ---- warp w: the force on bead w
+        if (valid) {
+            const double G[3][3] = {{s_G[0][l], s_G[1][l], s_G[2][l]},
+                                    {s_G[1][l], s_G[3][l], s_G[4][l]},
+                                    {s_G[2][l], s_G[4][l], s_G[5][l]}};
+            const double J[3][3] = {{2 * (-b * c + F * F), 2 * (c * d - e * F), 2 * (b * e - d * F)},
+                                    {2 * (c * d - e * F), 2 * (-a * c + e * e), 2 * (-d * e + a * F)},
+                                    {2 * (b * e - d * F), 2 * (-d * e + a * F), 2 * (d * d - a * b)}};
+            const double invJJ = 1.0 / JJ;
+            const double Ssum = s_t[0][l].S + s_t[1][l].S + s_t[2][l].S + s_t[3][l].S;
+            const double pref = kRep * invJJ / 2.0, m = -invJJ * Ssum;
+            double dv[3];
+#pragma unroll
+            for (int y = 0; y < 3; ++y) {
+                const double Jw = w == 0 ? J[2][y] - J[0][y] : w == 1 ? J[0][y] : w == 2 ? -J[2][y] - J[1][y] : J[1][y];
+                const double Gw = w == 0 ? G[2][y] - G[0][y] : w == 1 ? G[0][y] : w == 2 ? -G[2][y] - G[1][y] : G[1][y];
+                dv[y] = pref * (m * Jw + Gw);
+            }
+            Real* cdst = slot_ptr(n, n.slot_base[K_EXVOL] + 4 * i + w);
+            bool bad = false;
+#pragma unroll
+            for (int q = 0; q < 3; ++q) {
+                const double o = -(dv[0] * v12[q] + dv[1] * v34[q] + dv[2] * v31[q]);
+                if (!(fabs(o) < 1.0 / 0.0)) bad = true;
+                cdst[q] = (Real)o;
+            }
+            if (bad) atomicOr(&s_bad[l], 1);
+        }
+        __syncthreads();
+        if (w == 0 && valid && s_bad[l]) flag_fallback(n, r, i, 0.0);
+        __syncthreads();   // shared arrays are reused by the next group
     }
 }
 

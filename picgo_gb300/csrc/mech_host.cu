@@ -1082,9 +1082,15 @@ int32_t mech_ctx_create(int32_t precision, int32_t device, MechContext** out) {
     MechContext* c = new MechContext();
     c->device = device;
     c->precision = precision;
-    cudaError_t e = cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking);
-    if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&c->side, cudaStreamNonBlocking);
-    if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&c->side2, cudaStreamNonBlocking);
+    // The sparse lanes get the device's highest stream priority (kept by the
+    // kernel nodes captured from them): the excluded-volume chain is the
+    // longest lane, and the persistent filament kernel on the main lane would
+    // otherwise fill the register files before its blocks are placed.
+    int prio_least = 0, prio_greatest = 0;
+    cudaError_t e = cudaDeviceGetStreamPriorityRange(&prio_least, &prio_greatest);
+    if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking);
+    if (e == cudaSuccess) e = cudaStreamCreateWithPriority(&c->side, cudaStreamNonBlocking, prio_greatest);
+    if (e == cudaSuccess) e = cudaStreamCreateWithPriority(&c->side2, cudaStreamNonBlocking, prio_greatest);
     if (e == cudaSuccess) e = cudaEventCreateWithFlags(&c->fork, cudaEventDisableTiming);
     if (e == cudaSuccess) e = cudaEventCreateWithFlags(&c->join, cudaEventDisableTiming);
     if (e == cudaSuccess) e = cudaEventCreateWithFlags(&c->join2, cudaEventDisableTiming);
@@ -1306,13 +1312,33 @@ static int profile_impl(MechContext* c, int iters, MechProfile* o) {
     o->ms_fil_force = timeit([&] { launch_part<Real>(n, 1, s); });
     o->ms_bond_energy = timeit([&] { launch_part<Real>(n, 2, s); });
     o->ms_bond_force = timeit([&] { launch_part<Real>(n, 3, s); });
-    int cnt = 0;
+    // the last evaluation's extended-pass and Simpson-fallback list lengths
+    auto counts = [&](int64_t* ext, int64_t* fb) {
+        int v[2] = {0, 0};
+        if (c->ev_list_count.p) cudaMemcpy(&v[0], c->ev_list_count.p, sizeof(int), cudaMemcpyDeviceToHost);
+        cudaMemcpy(&v[1], n.ev_fb_count, sizeof(int), cudaMemcpyDeviceToHost);
+        *ext = c->precision == MECH_PREC_MIXED ? v[0] : c->nev;
+        *fb = v[1];
+    };
     o->ms_exvol_energy = timeit([&] { launch_exvol_energy<Real>(n, -1, 0, s); });
-    cudaMemcpy(&cnt, c->ev_list_count.p, sizeof(int), cudaMemcpyDeviceToHost);
-    o->n_exvol_ext_energy = c->precision == MECH_PREC_MIXED ? cnt : c->nev;
+    counts(&o->n_exvol_ext_energy, &o->n_exvol_fallback_energy);
     o->ms_exvol_force = timeit([&] { launch_exvol_forces<Real>(n, -1, s); });
-    cudaMemcpy(&cnt, c->ev_list_count.p, sizeof(int), cudaMemcpyDeviceToHost);
-    o->n_exvol_ext_force = c->precision == MECH_PREC_MIXED ? cnt : c->nev;
+    counts(&o->n_exvol_ext_force, &o->n_exvol_fallback_force);
+    // a line-search trial: positions x + lambda d formed and materialized on the fly
+    o->ms_trial_energy_eval = timeit([&] { launch_energy<Real>(n, -1, 1, c->lanes()); });
+    // every replica finished: each launch of an iteration block reads its phase and exits
+    const std::vector<CGState> saved(c->h_st, c->h_st + c->R);
+    for (int r = 0; r < c->R; ++r) c->h_st[r].phase = PH_DONE;
+    if ((rc = push_states(c))) return rc;
+    o->ms_iteration_idle = timeit([&] {
+        for (int t = 0; t < kTrialsPerBlock; ++t) launch_energy<Real>(n, PH_LS_TRIAL, 1, c->lanes());
+        launch_forces<Real>(n, PH_FORCE, c->lanes());
+        launch_direction<Real>(n, s);
+        launch_dispatch_failed<Real>(n, s);
+        launch_reset<Real>(n, s);
+    });
+    std::copy(saved.begin(), saved.end(), c->h_st);
+    if ((rc = push_states(c))) return rc;
     cudaEventDestroy(e0);
     cudaEventDestroy(e1);
     CU(gerr);
