@@ -21,6 +21,7 @@ from __future__ import annotations
 
 import argparse
 import json
+import re
 import os
 import platform
 import statistics
@@ -38,6 +39,18 @@ UNIT = "force_evals/s"
 SEED = 20261203 + 2
 CONFIG_NAME = "c2"
 
+
+def profiled_traffic(precision: str):
+    """DRAM bytes (read + write) per launch of the mixed trial filament-energy kernel on this
+    workload, from the ncu capture summarized in profiles/ (None when absent or FP64)."""
+    if precision != "mixed":
+        return None
+    path = os.path.join(ROOT, "profiles", "k_fil_energy_bulk_trial_1M_cylinders_dram.md")
+    try:
+        m = re.search(r"dram_bytes_per_launch:\s*(\d+)", open(path).read())
+    except OSError:
+        return None
+    return int(m.group(1)) if m else None
 
 def cg(**kw):
     from picgo_gb300 import cg_params
@@ -189,12 +202,15 @@ def run_ours(args, rank, world, dist):
     prof = eng.profile(20)
     rs = 4 if args.precision == "mixed" else 8
     nb = prof["n_beads"]
-    # algorithmic bytes per launch (each input read once, each output written once)
-    fil_energy_bytes = nb * (24 + 1 + 4 * rs)                 # x, flags, k_str, l0, k_bend, theta0
-    fil_force_bytes = nb * (24 + 1 + 4 * rs + 4 + rs * 3 + rs * 3) + prof["n_slots"] * (4 + 3 * rs)
+    # Algorithmic bytes per launch (each input read once, each output written once).  The
+    # dominant kernel of a minimization is the filament energy of a line-search trial: it
+    # runs once or twice per iteration and reads positions (24 B), flags (1 B), the four
+    # per-bead constants and the direction, and writes the trial positions (24 B).
     kernels = {
-        "fil_force": (prof["ms_fil_force"], fil_force_bytes),
-        "fil_energy": (prof["ms_fil_energy"], fil_energy_bytes),
+        "fil_energy_trial": (prof["ms_fil_energy_trial"], nb * (24 + 1 + 4 * rs + 3 * rs + 24)),
+        "fil_force": (prof["ms_fil_force_kernel"], nb * (24 + 1 + 4 * rs + 3 * rs)),
+        "force_gather": (prof["ms_force_gather"],
+                         nb * (3 * rs * 3 + 4) + prof["n_slots"] * 3 * rs),
     }
     peaks = {}
     try:
@@ -202,12 +218,15 @@ def run_ours(args, rank, world, dist):
     except OSError:
         pass
     peak = float(peaks.get("hbm_gbs", 6800.0))
-    name, (ms, nbytes) = max(kernels.items(), key=lambda kv: kv[1][0])
+    name = "fil_energy_trial"
+    ms, nbytes = kernels[name]
     achieved = nbytes / (ms * 1e-3) / 1e9
     roofline = {"bound": "hbm", "kernel": name, "achieved": round(achieved, 1), "peak": peak, "unit": "GB/s",
-                "frac": round(achieved / peak, 4), "traffic": None,
+                "frac": round(achieved / peak, 4), "traffic": profiled_traffic(args.precision),
                 "peak_source": "measured" if "hbm_gbs" in peaks else "fallback",
                 "bytes_per_launch": int(nbytes), "ms_per_launch": round(ms, 5),
+                "others": {k: {"ms": round(v[0], 5), "bytes": int(v[1]),
+                               "gbs": round(v[1] / (v[0] * 1e-3) / 1e9, 1)} for k, v in kernels.items() if k != name},
                 "profile_ms": {k: round(v, 5) for k, v in prof.items() if k.startswith("ms_")}}
     eng.close()
 

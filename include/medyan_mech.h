@@ -257,6 +257,9 @@ typedef struct MechProfile {
     double ms_trial_energy_eval;   /* one line-search trial: energy at x + lambda d, trial positions written */
     int64_t n_exvol_fallback_energy;   /* pairs the last energy pass sent to the Simpson fallback */
     int64_t n_exvol_fallback_force;    /* and the last force pass */
+    double ms_fil_energy_trial;    /* filament energy of a trial (x + lambda d formed and written) */
+    double ms_fil_force_kernel;    /* filament forces alone (without the gather and reduction) */
+    double ms_force_gather;        /* sparse gather with the CG partials alone */
 } MechProfile;
 int32_t mech_profile(MechContext* ctx, int32_t iters, MechProfile* out);
 

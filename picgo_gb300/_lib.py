@@ -94,7 +94,8 @@ class MechProfile(C.Structure):
                 ("n_motors", C.c_int64), ("n_slots", C.c_int64), ("n_exvol_ext_energy", C.c_int64),
                 ("n_exvol_ext_force", C.c_int64), ("ms_iteration_idle", C.c_double),
                 ("ms_trial_energy_eval", C.c_double), ("n_exvol_fallback_energy", C.c_int64),
-                ("n_exvol_fallback_force", C.c_int64)]
+                ("n_exvol_fallback_force", C.c_int64), ("ms_fil_energy_trial", C.c_double),
+                ("ms_fil_force_kernel", C.c_double), ("ms_force_gather", C.c_double)]
 
 
 class MechSolveParams(C.Structure):

@@ -1282,6 +1282,17 @@ int launch_part(const DevNet<Real>& n, int which, cudaStream_t s) {
             return 3;
         case 2: if (lm + bb_t > 0) { k_bond_bnd<Real><<<lm + bb_t, kBlock, 0, s>>>(n, -1, 0, 0, lm, ev_t); return 1; } return 0;
         case 3: if (lm + bb_t > 0) { k_bond_bnd<Real><<<lm + bb_t, kBlock, 0, s>>>(n, -1, 0, 1, lm, ev_t); return 1; } return 0;
+        case 4:   // filament energy of a line-search trial (positions x + lambda d formed and written)
+            if constexpr (sizeof(Real) == 4) k_fil_energy_bulk<<<n.pgrid[0], kBlock, 0, s>>>(n, -1, 1);
+            else k_fil_energy<Real><<<n.n_ftiles, kBlock, 0, s>>>(n, -1, 1);
+            return 1;
+        case 5:   // filament forces alone
+            if constexpr (sizeof(Real) == 4) k_fil_force_bulk<<<n.pgrid[1], kBlock, 0, s>>>(n, -1);
+            else k_fil_force<Real><<<n.n_ftiles, kBlock, 0, s>>>(n, -1);
+            return 1;
+        case 6:   // the sparse gather with the CG partials alone
+            k_force_gather<Real><<<n.n_ftiles, kBlock, 0, s>>>(n, -1);
+            return 1;
     }
     return 0;
 }

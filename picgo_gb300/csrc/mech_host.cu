@@ -1312,6 +1312,9 @@ static int profile_impl(MechContext* c, int iters, MechProfile* o) {
     o->ms_fil_force = timeit([&] { launch_part<Real>(n, 1, s); });
     o->ms_bond_energy = timeit([&] { launch_part<Real>(n, 2, s); });
     o->ms_bond_force = timeit([&] { launch_part<Real>(n, 3, s); });
+    o->ms_fil_energy_trial = timeit([&] { launch_part<Real>(n, 4, s); });
+    o->ms_fil_force_kernel = timeit([&] { launch_part<Real>(n, 5, s); });
+    o->ms_force_gather = timeit([&] { launch_part<Real>(n, 6, s); });
     // the last evaluation's extended-pass and Simpson-fallback list lengths
     auto counts = [&](int64_t* ext, int64_t* fb) {
         int v[2] = {0, 0};
