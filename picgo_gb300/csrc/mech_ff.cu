@@ -367,63 +367,87 @@ __global__ void __launch_bounds__(kBlock) k_fil_force(DevNet<Real> n, int want) 
 // Every bead adds its sparse contributions (contiguous, in the CSR order) to
 // its filament force, then the CG partials: max |F|, F.F, F.Fprev per tile,
 // reduced by k_finalize_force (a per-tile completion ticket on one address
-// per replica would serialize thousands of atomics).
+// per replica would serialize thousands of atomics).  Each block takes
+// kGatherTiles consecutive tiles and issues the loads of all of them before
+// the per-tile reductions, so a thread keeps several beads' loads in flight.
 // ---------------------------------------------------------------------------
+constexpr int kGatherTiles = 4;
+
+template <typename Real>
+__device__ __forceinline__ void gather_bead(const DevNet<Real>& n, int b, int fb, Real& mx, Real& ff, Real& ffp) {
+    Real* Fo = n.f[fb ^ 1] + 3 * (size_t)b;
+    const Real* Fp = n.f[fb] + 3 * (size_t)b;
+    Real F[3] = {Fo[0], Fo[1], Fo[2]};
+    const int c0 = n.csr_off[b], c1 = n.csr_off[b + 1];
+    for (int c = c0; c < c1; ++c) {
+        F[0] += n.contrib[3 * (size_t)c];
+        F[1] += n.contrib[3 * (size_t)c + 1];
+        F[2] += n.contrib[3 * (size_t)c + 2];
+    }
+    Fo[0] = F[0];
+    Fo[1] = F[1];
+    Fo[2] = F[2];
+    // a non-finite component makes the bead's max infinite (fmax would drop a NaN)
+    const bool fin = F[0] - F[0] == 0 && F[1] - F[1] == 0 && F[2] - F[2] == 0;
+    mx = fin ? fmax(fmax(fabs(F[0]), fabs(F[1])), fabs(F[2])) : Real(1.0 / 0.0);
+    ff = bead_dot(F[0], F[1], F[2], F[0], F[1], F[2]);
+    ffp = bead_dot(F[0], F[1], F[2], Fp[0], Fp[1], Fp[2]);
+}
+
 template <typename Real>
 __global__ void __launch_bounds__(kBlock) k_force_gather(DevNet<Real> n, int want) {
     __shared__ double sh[32 * 3];
-    __shared__ int s_go, s_fb;
-    const Tile t = n.ftile[blockIdx.x];
-    const int r = t.replica;
-    if (threadIdx.x == 0) {
-        const CGState& S = n.st[r];
-        s_go = replica_selected(S, want);
-        s_fb = S.fbuf;
+    __shared__ int s_go[kGatherTiles], s_fb[kGatherTiles];
+    const int t0 = blockIdx.x * kGatherTiles;
+    if (threadIdx.x < kGatherTiles) {
+        const int ti = t0 + threadIdx.x;
+        int go = 0, fb = 0;
+        if (ti < n.n_ftiles) {
+            const CGState& S = n.st[n.ftile[ti].replica];
+            go = replica_selected(S, want);
+            fb = S.fbuf;
+        }
+        s_go[threadIdx.x] = go;
+        s_fb[threadIdx.x] = fb;
     }
     __syncthreads();
-    if (!s_go) return;
-    Real mx = 0, ff = 0, ffp = 0;
-    const int b = t.begin + threadIdx.x;
-    if (b < t.end) {
-        Real* Fo = n.f[s_fb ^ 1] + 3 * (size_t)b;
-        const Real* Fp = n.f[s_fb] + 3 * (size_t)b;
-        Real F[3] = {Fo[0], Fo[1], Fo[2]};
-        const int c0 = n.csr_off[b], c1 = n.csr_off[b + 1];
-        for (int c = c0; c < c1; ++c) {
-            F[0] += n.contrib[3 * (size_t)c];
-            F[1] += n.contrib[3 * (size_t)c + 1];
-            F[2] += n.contrib[3 * (size_t)c + 2];
-        }
-        Fo[0] = F[0];
-        Fo[1] = F[1];
-        Fo[2] = F[2];
-        // a non-finite component makes the bead's max infinite (fmax would drop a NaN)
-        const bool fin = F[0] - F[0] == 0 && F[1] - F[1] == 0 && F[2] - F[2] == 0;
-        mx = fin ? fmax(fmax(fabs(F[0]), fabs(F[1])), fabs(F[2])) : Real(1.0 / 0.0);
-        ff = bead_dot(F[0], F[1], F[2], F[0], F[1], F[2]);
-        ffp = bead_dot(F[0], F[1], F[2], Fp[0], Fp[1], Fp[2]);
+    Real mx[kGatherTiles], ff[kGatherTiles], ffp[kGatherTiles];
+#pragma unroll
+    for (int j = 0; j < kGatherTiles; ++j) {
+        mx[j] = 0;
+        ff[j] = 0;
+        ffp[j] = 0;
+        if (!s_go[j]) continue;
+        const Tile t = n.ftile[t0 + j];
+        const int b = t.begin + threadIdx.x;
+        if (b < t.end) gather_bead(n, b, s_fb[j], mx[j], ff[j], ffp[j]);
     }
-    if constexpr (sizeof(Real) == 4) {
-        // mixed: the tile's max and compensated (hi, lo) dot sums as floats in
-        // the tile's slots 0-2: {max, F.F hi, F.F lo, F.Fprev hi, F.Fprev lo}
-        FF a[2];
-        a[0].h = ff;
-        a[1].h = ffp;
-        float m[1] = {mx};
-        block_reduce_pairs<2, 1>(a, m, reinterpret_cast<float*>(sh));
-        if (threadIdx.x == 0) {
-            float* p = reinterpret_cast<float*>(n.part_fil + 4 * (size_t)blockIdx.x);
-            *reinterpret_cast<float4*>(p) = make_float4(m[0], a[0].h, a[0].l, a[1].h);
-            p[4] = a[1].l;
-        }
-    } else {
-        double red[3] = {warp_max_r(mx), warp_sum_r(ff), warp_sum_r(ffp)};
-        const int ops[3] = {1, 0, 0};
-        block_combine<3>(red, ops, sh);
-        if (threadIdx.x == 0) {
-            n.part_fil[4 * (size_t)blockIdx.x + 0] = red[0];
-            n.part_fil[4 * (size_t)blockIdx.x + 1] = red[1];
-            n.part_fil[4 * (size_t)blockIdx.x + 2] = red[2];
+#pragma unroll
+    for (int j = 0; j < kGatherTiles; ++j) {
+        if (!s_go[j]) continue;   // block-uniform
+        const size_t slot = 4 * (size_t)(t0 + j);
+        if constexpr (sizeof(Real) == 4) {
+            // mixed: the tile's max and compensated (hi, lo) dot sums as floats in
+            // the tile's slots 0-2: {max, F.F hi, F.F lo, F.Fprev hi, F.Fprev lo}
+            FF a[2];
+            a[0].h = ff[j];
+            a[1].h = ffp[j];
+            float m[1] = {mx[j]};
+            block_reduce_pairs<2, 1>(a, m, reinterpret_cast<float*>(sh));
+            if (threadIdx.x == 0) {
+                float* p = reinterpret_cast<float*>(n.part_fil + slot);
+                *reinterpret_cast<float4*>(p) = make_float4(m[0], a[0].h, a[0].l, a[1].h);
+                p[4] = a[1].l;
+            }
+        } else {
+            double red[3] = {warp_max_r(mx[j]), warp_sum_r(ff[j]), warp_sum_r(ffp[j])};
+            const int ops[3] = {1, 0, 0};
+            block_combine<3>(red, ops, sh);
+            if (threadIdx.x == 0) {
+                n.part_fil[slot + 0] = red[0];
+                n.part_fil[slot + 1] = red[1];
+                n.part_fil[slot + 2] = red[2];
+            }
         }
     }
 }
@@ -1045,34 +1069,45 @@ __global__ void __launch_bounds__(kBlock) k_finalize_direction(DevNet<Real> n) {
     }
 }
 
-// d = F (resetCGParams, CGMethod.hpp:963-972); the new slope d.F is F.F
+// d = F (resetCGParams, CGMethod.hpp:963-972); the new slope d.F is F.F.
+// kGatherTiles tiles per block, so that the launch costs little when no
+// replica is resetting (it is in every iteration of the graph).
 template <typename Real>
 __global__ void __launch_bounds__(kBlock) k_reset(DevNet<Real> n) {
-    __shared__ int s_go, s_fb, s_flag;
-    const Tile t = n.ftile[blockIdx.x];
-    const int r = t.replica;
-    if (threadIdx.x == 0) {
-        const CGState& S = n.st[r];
-        s_go = S.phase == PH_RESET;
-        s_fb = S.fbuf;
+    __shared__ int s_go[kGatherTiles], s_fb[kGatherTiles], s_flag;
+    const int t0 = blockIdx.x * kGatherTiles;
+    if (threadIdx.x < kGatherTiles) {
+        const int ti = t0 + threadIdx.x;
+        int go = 0, fb = 0;
+        if (ti < n.n_ftiles) {
+            const CGState& S = n.st[n.ftile[ti].replica];
+            go = S.phase == PH_RESET;
+            fb = S.fbuf;
+        }
+        s_go[threadIdx.x] = go;
+        s_fb[threadIdx.x] = fb;
     }
     __syncthreads();
-    if (!s_go) return;
-    const int b = t.begin + threadIdx.x;
-    if (b < t.end) {
-        const Real* F = n.f[s_fb] + 3 * (size_t)b;
-        Real* D = n.d + 3 * (size_t)b;
-        D[0] = F[0];
-        D[1] = F[1];
-        D[2] = F[2];
-    }
-    const RepTiles rt = n.rt[r];
-    if (last_tile(n.ticket, r, rt.fil_end - rt.fil_begin, &s_flag)) {
-        if (threadIdx.x == 0) {
-            CGState& S = n.st[r];
-            S.slope = S.FdotF;
-            S.lastFdotF = S.FdotF;
-            begin_iteration(S);
+    for (int j = 0; j < kGatherTiles; ++j) {
+        if (!s_go[j]) continue;   // block-uniform
+        const Tile t = n.ftile[t0 + j];
+        const int r = t.replica;
+        const int b = t.begin + threadIdx.x;
+        if (b < t.end) {
+            const Real* F = n.f[s_fb[j]] + 3 * (size_t)b;
+            Real* D = n.d + 3 * (size_t)b;
+            D[0] = F[0];
+            D[1] = F[1];
+            D[2] = F[2];
+        }
+        const RepTiles rt = n.rt[r];
+        if (last_tile(n.ticket, r, rt.fil_end - rt.fil_begin, &s_flag)) {
+            if (threadIdx.x == 0) {
+                CGState& S = n.st[r];
+                S.slope = S.FdotF;
+                S.lastFdotF = S.FdotF;
+                begin_iteration(S);
+            }
         }
     }
 }
@@ -1222,7 +1257,7 @@ int launch_forces(const DevNet<Real>& n, int want, const Lanes& L) {
     else k_fil_force<Real><<<n.n_ftiles, kBlock, 0, L.main>>>(n, want);
     cudaStreamWaitEvent(L.main, L.join, 0);
     cudaStreamWaitEvent(L.main, L.join2, 0);
-    k_force_gather<Real><<<n.n_ftiles, kBlock, 0, L.main>>>(n, want);
+    k_force_gather<Real><<<(n.n_ftiles + kGatherTiles - 1) / kGatherTiles, kBlock, 0, L.main>>>(n, want);
     k_finalize_force<Real><<<n.R, kBlock, 0, L.main>>>(n, want);
     return launched + 3;
 }
@@ -1237,7 +1272,7 @@ int launch_direction(const DevNet<Real>& n, cudaStream_t s) {
 
 template <typename Real>
 int launch_reset(const DevNet<Real>& n, cudaStream_t s) {
-    k_reset<Real><<<n.n_ftiles, kBlock, 0, s>>>(n);
+    k_reset<Real><<<(n.n_ftiles + kGatherTiles - 1) / kGatherTiles, kBlock, 0, s>>>(n);
     return 1;
 }
 
@@ -1277,7 +1312,7 @@ int launch_part(const DevNet<Real>& n, int which, cudaStream_t s) {
         case 1:
             if constexpr (sizeof(Real) == 4) k_fil_force_bulk<<<n.pgrid[1], kBlock, 0, s>>>(n, -1);
             else k_fil_force<Real><<<n.n_ftiles, kBlock, 0, s>>>(n, -1);
-            k_force_gather<Real><<<n.n_ftiles, kBlock, 0, s>>>(n, -1);
+            k_force_gather<Real><<<(n.n_ftiles + kGatherTiles - 1) / kGatherTiles, kBlock, 0, s>>>(n, -1);
             k_finalize_force<Real><<<n.R, kBlock, 0, s>>>(n, -1);
             return 3;
         case 2: if (lm + bb_t > 0) { k_bond_bnd<Real><<<lm + bb_t, kBlock, 0, s>>>(n, -1, 0, 0, lm, ev_t); return 1; } return 0;
@@ -1291,7 +1326,7 @@ int launch_part(const DevNet<Real>& n, int which, cudaStream_t s) {
             else k_fil_force<Real><<<n.n_ftiles, kBlock, 0, s>>>(n, -1);
             return 1;
         case 6:   // the sparse gather with the CG partials alone
-            k_force_gather<Real><<<n.n_ftiles, kBlock, 0, s>>>(n, -1);
+            k_force_gather<Real><<<(n.n_ftiles + kGatherTiles - 1) / kGatherTiles, kBlock, 0, s>>>(n, -1);
             return 1;
     }
     return 0;
