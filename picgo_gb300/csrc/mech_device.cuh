@@ -299,11 +299,12 @@ __device__ __forceinline__ float warp_max_f(float v) {
     return v;
 }
 // Block reduction with no double arithmetic: N compensated pairs and M maxima
-// of non-negative floats, in a fixed order; results valid in thread 0.  The
-// FP64 pipe runs at 1/64 of the FP32 rate on this part, so a per-tile double
-// tree costs more than the tile's loads.  `sh` holds 32 * (2N + M) floats.
+// of non-negative floats (`m` may be null when M is 0), in a fixed order;
+// results valid in thread 0.  A warp's FP64 instruction holds its sub-
+// partition's FP64 pipe for ~78 cycles on this part, so a per-tile double tree
+// costs more than the tile's loads.  `sh` holds 32 * (2N + M) floats.
 template <int N, int M>
-__device__ __forceinline__ void block_reduce_pairs(FF (&a)[N], float (&m)[M], float* sh) {
+__device__ __forceinline__ void block_reduce_ff(FF (&a)[N], float* m, float* sh) {
     const int wi = threadIdx.x >> 5, l = threadIdx.x & 31, nw = blockDim.x >> 5;
 #pragma unroll
     for (int k = 0; k < N; ++k) warp_reduce_pair(a[k].h, a[k].l);
@@ -330,6 +331,21 @@ __device__ __forceinline__ void block_reduce_pairs(FF (&a)[N], float (&m)[M], fl
 #pragma unroll
         for (int k = 0; k < M; ++k) m[k] = warp_max_f(l < nw ? sh[(2 * N + k) * 32 + l] : 0.f);
     }
+}
+template <int N, int M>
+__device__ __forceinline__ void block_reduce_pairs(FF (&a)[N], float (&m)[M], float* sh) {
+    block_reduce_ff<N, M>(a, m, sh);
+}
+
+// Mixed-engine partial slots: a compensated (hi, lo) float pair stored in the
+// 8 bytes of a double slot, so partial sums never pass through FP64.
+__device__ __forceinline__ void store_pair(double* slot, float h, float l) {
+    *reinterpret_cast<float2*>(slot) = make_float2(h, l);
+}
+__device__ __forceinline__ float2 load_pair(const double* slot) { return __ldcg(reinterpret_cast<const float2*>(slot)); }
+__device__ __forceinline__ void add_pair(FF& acc, float2 v) {
+    acc.add(v.x);
+    acc.add(v.y);
 }
 __device__ __forceinline__ double warp_max_lane0(float v) {
 #pragma unroll

@@ -253,7 +253,8 @@ __global__ void __launch_bounds__(kBlock) k_exvol(DevNet<Real> n, int want, int 
     const bool tr = trial != 0;
     const int i = t.begin + threadIdx.x;
     const bool valid = i < t.end;
-    double e = 0.0;
+    double e = 0.0;   // FP64 engine
+    float ef = 0.f;   // mixed engine
     bool need64 = false;
     if (valid) {
         const int4 bs = n.ev_bead[i];
@@ -326,9 +327,9 @@ __global__ void __launch_bounds__(kBlock) k_exvol(DevNet<Real> n, int want, int 
                 PairInv<float> pi;
                 pair_inv(v12, v34, v31, v14, v32, v24, pi, true);
                 if (!force) {
-                    const double u = energy_from(pi, kRep);
+                    const float u = energy_value(pi, kRep);
                     if (u != u) need64 = true;
-                    else e = u;
+                    else ef = u;
                 } else {
                     float out[4][3];
                     if (forces_from<true>(pi, v12, v34, v31, kRep, out)) {
@@ -341,7 +342,7 @@ __global__ void __launch_bounds__(kBlock) k_exvol(DevNet<Real> n, int want, int 
                     }
                 }
             }
-            if (!force) n.ev_energy[i] = need64 ? 0.0 : e;
+            if (!force) store_pair(n.ev_energy + i, need64 ? 0.f : ef, 0.f);
         }
     }
     if constexpr (sizeof(Real) == 4) append_fp64(n, need64, r, i);
@@ -502,9 +503,10 @@ __global__ void __launch_bounds__(128) k_exvol_ext(DevNet<Real> n, int trial, in
                 const double U = 0.5 * kRep / JJ * Ssum;
                 if (!(fabs(U) < 1.0 / 0.0) || U < -1.0) {
                     flag_fallback(n, r, i, trial != 0 ? n.st[r].lambda : 0.0);
-                    n.ev_energy[i] = 0.0;
+                    store_pair(n.ev_energy + i, 0.f, 0.f);
                 } else {
-                    n.ev_energy[i] = U;
+                    const float h = (float)U;
+                    store_pair(n.ev_energy + i, h, (float)(U - (double)h));
                 }
             }
             __syncthreads();   // shared arrays are reused by the next group
@@ -582,10 +584,14 @@ __global__ void __launch_bounds__(kBlock) k_exvol_energy_tail(DevNet<Real> n, in
     const CGState& S = n.st[t.replica];
     const bool go = want < 0 ? (S.active != 0) : (S.phase == want);
     if (!go) return;
-    const int i = t.begin + threadIdx.x;
-    double e = i < t.end ? n.ev_energy[i] : 0.0;
-    e = block_sum(e, sh);
-    if (threadIdx.x == 0) n.part_sp[ti] = e;
+    if constexpr (sizeof(Real) == 4) {
+        // per-pair energies as (hi, lo) pairs, summed compensated in single precision
+        const int i = t.begin + threadIdx.x;
+        FF a[1];
+        if (i < t.end) add_pair(a[0], load_pair(n.ev_energy + i));
+        block_reduce_ff<1, 0>(a, nullptr, reinterpret_cast<float*>(sh));
+        if (threadIdx.x == 0) store_pair(n.part_sp + ti, a[0].h, a[0].l);
+    }
 }
 
 // zero the extended-pass and fallback work-list counts (one memset when they are

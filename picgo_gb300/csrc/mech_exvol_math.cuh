@@ -140,13 +140,18 @@ __device__ __forceinline__ void diffs_of(const double* c1, const double* c2, con
 template <typename T>
 __device__ __forceinline__ bool bad_value(T x) { return !(fabs(x) < (T)(1.0 / 0.0)); }
 
-// Analytic pair energy (:427-436); NaN when unusable (inf, NaN or < -1).
+// Analytic pair energy (:427-436) in the arithmetic type; NaN when unusable
+// (inf, NaN or < -1).
 template <typename T>
-__device__ __forceinline__ double energy_from(const PairInv<T>& p, T kRepScaled) {
+__device__ __forceinline__ T energy_value(const PairInv<T>& p, T kRepScaled) {
     const T U = (T)0.5 * kRepScaled / p.JJ *
                 (p.CC / p.AA * p.ATG1 + p.GG / p.EE * p.ATG2 + p.DD / p.BB * p.ATG3 + p.HH / p.FF * p.ATG4);
-    if (bad_value(U) || U < (T)-1) return __longlong_as_double(0x7ff8000000000000ULL);
-    return (double)U;
+    if (bad_value(U) || U < (T)-1) return (T)(0.0 / 0.0);
+    return U;
+}
+template <typename T>
+__device__ __forceinline__ double energy_from(const PairInv<T>& p, T kRepScaled) {
+    return (double)energy_value(p, kRepScaled);
 }
 
 // |n_hat . v3_hat| of areInPlane (MathFunctions.h:1101-1134), n = (c2-c1) x (c3-c1), v3 = c4 - c1.

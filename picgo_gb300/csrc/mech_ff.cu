@@ -90,27 +90,50 @@ __device__ void finalize_energy(const DevNet<Real>& n, int r, int trial, double*
     const RepTiles rt = n.rt[r];
     const int stride = sizeof(Real) == 4 ? n.ptiles[0] : 1;
     const int nslot = run_slots(rt.fil_begin, rt.fil_end, stride);
-    // every thread issues its loads back to back, then sums in a fixed order
-    double acc[MECH_NUM_FF] = {0, 0, 0, 0, 0, 0};
-#pragma unroll 8
-    for (int k = threadIdx.x; k < nslot; k += blockDim.x) {
-        const int i = run_slot(rt.fil_begin, stride, k);
-        const double2 v = __ldcg(reinterpret_cast<const double2*>(n.part_fil + 4 * (size_t)i));
-        acc[MECH_FF_STRETCHING] += v.x;
-        acc[MECH_FF_BENDING] += v.y;
-    }
     const int ffk[K_NUM_SPARSE] = {MECH_FF_LINKER, MECH_FF_MOTOR, MECH_FF_EXVOL, MECH_FF_BOUNDARY};
-#pragma unroll
-    for (int k = 0; k < K_NUM_SPARSE; ++k) {
-#pragma unroll 8
-        for (int i = rt.sp_begin[k] + threadIdx.x; i < rt.sp_end[k]; i += blockDim.x) acc[ffk[k]] += __ldcg(n.part_sp + i);
-    }
     double e[MECH_NUM_FF];
+    if constexpr (sizeof(Real) == 4) {
+        // mixed: (hi, lo) pair slots summed compensated in single precision;
+        // the doubles are formed in thread 0 only
+        FF acc[MECH_NUM_FF];
+#pragma unroll 4
+        for (int k = threadIdx.x; k < nslot; k += blockDim.x) {
+            const double* slot = n.part_fil + 4 * (size_t)run_slot(rt.fil_begin, stride, k);
+            add_pair(acc[MECH_FF_STRETCHING], load_pair(slot));
+            add_pair(acc[MECH_FF_BENDING], load_pair(slot + 1));
+        }
 #pragma unroll
-    for (int k = 0; k < MECH_NUM_FF; ++k) e[k] = warp_sum(acc[k]);
-    const int ops[MECH_NUM_FF] = {0, 0, 0, 0, 0, 0};
-    block_combine<MECH_NUM_FF>(e, ops, sh);
-    if (threadIdx.x != 0) return;
+        for (int k = 0; k < K_NUM_SPARSE; ++k) {
+#pragma unroll 4
+            for (int i = rt.sp_begin[k] + threadIdx.x; i < rt.sp_end[k]; i += blockDim.x)
+                add_pair(acc[ffk[k]], load_pair(n.part_sp + i));
+        }
+        block_reduce_ff<MECH_NUM_FF, 0>(acc, nullptr, reinterpret_cast<float*>(sh));
+        if (threadIdx.x != 0) return;
+#pragma unroll
+        for (int k = 0; k < MECH_NUM_FF; ++k) e[k] = (double)acc[k].h + (double)acc[k].l;
+    } else {
+        // every thread issues its loads back to back, then sums in a fixed order
+        double acc[MECH_NUM_FF] = {0, 0, 0, 0, 0, 0};
+#pragma unroll 8
+        for (int k = threadIdx.x; k < nslot; k += blockDim.x) {
+            const int i = run_slot(rt.fil_begin, stride, k);
+            const double2 v = __ldcg(reinterpret_cast<const double2*>(n.part_fil + 4 * (size_t)i));
+            acc[MECH_FF_STRETCHING] += v.x;
+            acc[MECH_FF_BENDING] += v.y;
+        }
+#pragma unroll
+        for (int k = 0; k < K_NUM_SPARSE; ++k) {
+#pragma unroll 8
+            for (int i = rt.sp_begin[k] + threadIdx.x; i < rt.sp_end[k]; i += blockDim.x)
+                acc[ffk[k]] += __ldcg(n.part_sp + i);
+        }
+#pragma unroll
+        for (int k = 0; k < MECH_NUM_FF; ++k) e[k] = warp_sum(acc[k]);
+        const int ops[MECH_NUM_FF] = {0, 0, 0, 0, 0, 0};
+        block_combine<MECH_NUM_FF>(e, ops, sh);
+        if (threadIdx.x != 0) return;
+    }
     // Pairs whose analytic energy was not usable were evaluated numerically;
     // add them in pair order.  A failed pair makes the force field report -1
     // (CylinderExclVolRepulsion.cpp:442-481).
@@ -481,15 +504,14 @@ __global__ void __launch_bounds__(kBlock) k_finalize_energy(DevNet<Real> n, int 
 // ---------------------------------------------------------------------------
 
 
-// Store a run's partial sums (lane-0 warp results) in the slot of its first
-// tile; the reduction kernel that follows the evaluation reads them.
+// Store a run's compensated partial sums as (hi, lo) pairs in the slot of its
+// first tile; the reduction kernel that follows the evaluation reads them.
 template <int N>
-__device__ __forceinline__ void write_run(const DevNet<float>& n, int first, double (&w)[N], const int (&ops)[N],
-                                          double* sh) {
-    block_combine<N>(w, ops, sh);
+__device__ __forceinline__ void write_run(const DevNet<float>& n, int first, FF (&a)[N], double* sh) {
+    block_reduce_ff<N, 0>(a, nullptr, reinterpret_cast<float*>(sh));
     if (threadIdx.x == 0) {
 #pragma unroll
-        for (int k = 0; k < N; ++k) n.part_fil[4 * (size_t)first + k] = w[k];
+        for (int k = 0; k < N; ++k) store_pair(n.part_fil + 4 * (size_t)first + k, a[k].h, a[k].l);
     }
 }
 
@@ -621,13 +643,12 @@ __global__ void __launch_bounds__(kBlock) k_fil_energy_bulk(DevNet<float> n, int
     bool go = false;
     float lf = 0.f;
     FF es, eb;
-    const int ops[2] = {0, 0};
     for (int k = 0; k < nt; ++k) {
         const int4 t = s_desc[k];
         if (t.z != cur) {
             if (cnt) {
-                double w[2] = {warp_sum_pair(es), warp_sum_pair(eb)};
-                write_run<2>(n, first, w, ops, sh);
+                FF a[2] = {es, eb};
+                write_run<2>(n, first, a, sh);
             }
             cur = t.z;
             first = t0 + k;
@@ -692,8 +713,8 @@ __global__ void __launch_bounds__(kBlock) k_fil_energy_bulk(DevNet<float> n, int
         return;
     }
     if (cnt) {
-        double w[2] = {warp_sum_pair(es), warp_sum_pair(eb)};
-        write_run<2>(n, first, w, ops, sh);
+        FF a[2] = {es, eb};
+        write_run<2>(n, first, a, sh);
     }
 }
 
@@ -874,12 +895,11 @@ __global__ void __launch_bounds__(kBlock) k_direction_mx(DevNet<float> n) {
     bool go = false;
     float beta = 0.f;
     FF dF;
-    const int ops[1] = {0};
-    // the run's partial goes to slot 3 of its first tile
+    // the run's partial goes to slot 3 of its first tile, as a (hi, lo) pair
     auto finish = [&](int) {
-        double w[1] = {warp_sum_pair(dF)};
-        block_combine<1>(w, ops, sh);
-        if (threadIdx.x == 0) n.part_fil[4 * (size_t)first + 3] = w[0];
+        FF a[1] = {dF};
+        block_reduce_ff<1, 0>(a, nullptr, reinterpret_cast<float*>(sh));
+        if (threadIdx.x == 0) store_pair(n.part_fil + 4 * (size_t)first + 3, a[0].h, a[0].l);
     };
     for (int ti = t0; ti < t1; ++ti) {
         const Tile t = n.ftile[ti];
@@ -922,6 +942,7 @@ __global__ void __launch_bounds__(kBlock) k_bond_bnd(DevNet<Real> n, int want, i
     __shared__ double sh[32];
     __shared__ int s_go, s_xb;
     __shared__ double s_lam;
+    __shared__ float s_lf;   // the step rounded once (mixed engine)
     const int ti = blockIdx.x < n_lm_tiles ? blockIdx.x : blockIdx.x + ev_tiles;
     const Tile t = n.stile[ti];
     const int kind = n.stile_kind[ti];
@@ -931,18 +952,27 @@ __global__ void __launch_bounds__(kBlock) k_bond_bnd(DevNet<Real> n, int want, i
         s_go = replica_selected(S, want);
         s_xb = S.xbuf;
         s_lam = S.lambda;
+        s_lf = (float)S.lambda;
     }
     __syncthreads();
     if (!s_go) return;
     const Real* X = n.x[s_xb];
     const bool tr = trial != 0;
+    auto pos = [&](int b) -> Pos<Real> {
+        if constexpr (sizeof(Real) == 4) {
+            const Pos<float> p = load_pos(X, b);
+            return tr ? moved_f(p, n.d, b, s_lf) : p;
+        } else {
+            return bead_at(X, n.d, b, tr, s_lam);
+        }
+    };
     const int i = t.begin + threadIdx.x;
     Real e = 0;
     if (i < t.end) {
         if (kind == K_BOUNDARY) {
             const int b = n.bb_bead[i];
             const double* pl = n.planes + 4 * n.bb_plane[i];
-            const Pos<Real> p = bead_at(X, n.d, b, tr, s_lam);
+            const Pos<Real> p = pos(b);
             const Real rr = plane_dist_p(pl, p);
             const Real K = n.bb_k[i], sl = n.bb_slen[i];
             const Real R = -rr / sl;
@@ -963,8 +993,7 @@ __global__ void __launch_bounds__(kBlock) k_bond_bnd(DevNet<Real> n, int want, i
             const Real l0 = lk ? n.lk_l0[i] : n.mt_l0[i];
             const Real s1 = lk ? n.lk_s1[i] : n.mt_s1[i];
             const Real s2 = lk ? n.lk_s2[i] : n.mt_s2[i];
-            const Pos<Real> c1 = bead_at(X, n.d, bs.x, tr, s_lam), c2 = bead_at(X, n.d, bs.y, tr, s_lam);
-            const Pos<Real> c3 = bead_at(X, n.d, bs.z, tr, s_lam), c4 = bead_at(X, n.d, bs.w, tr, s_lam);
+            const Pos<Real> c1 = pos(bs.x), c2 = pos(bs.y), c3 = pos(bs.z), c4 = pos(bs.w);
             Real v[3];
             bond_vector(c1, c2, c3, c4, s1, s2, v);
             const Real lx = v[0], ly = v[1], lz = v[2];
@@ -993,8 +1022,15 @@ __global__ void __launch_bounds__(kBlock) k_bond_bnd(DevNet<Real> n, int want, i
         }
     }
     if (!force) {
-        const double se = block_sum_r(e, sh);
-        if (threadIdx.x == 0) n.part_sp[ti] = se;
+        if constexpr (sizeof(Real) == 4) {
+            FF a[1];
+            a[0].h = e;
+            block_reduce_ff<1, 0>(a, nullptr, reinterpret_cast<float*>(sh));
+            if (threadIdx.x == 0) store_pair(n.part_sp + ti, a[0].h, a[0].l);
+        } else {
+            const double se = block_sum_r(e, sh);
+            if (threadIdx.x == 0) n.part_sp[ti] = se;
+        }
     }
 }
 
@@ -1047,11 +1083,12 @@ __global__ void __launch_bounds__(kBlock) k_finalize_direction(DevNet<Real> n) {
     if constexpr (sizeof(Real) == 8) {
         slope = sum_slots(n.part_fil, 4, 3, rt.fil_begin, rt.fil_end, sh);
     } else {
-        double a = 0.0;
+        FF a[1];
         const int nslot = run_slots(rt.fil_begin, rt.fil_end, n.ptiles[2]);
         for (int k = threadIdx.x; k < nslot; k += blockDim.x)
-            a += __ldcg(n.part_fil + 4 * (size_t)run_slot(rt.fil_begin, n.ptiles[2], k) + 3);
-        slope = block_sum(a, sh);
+            add_pair(a[0], load_pair(n.part_fil + 4 * (size_t)run_slot(rt.fil_begin, n.ptiles[2], k) + 3));
+        block_reduce_ff<1, 0>(a, nullptr, reinterpret_cast<float*>(sh));
+        slope = threadIdx.x == 0 ? (double)a[0].h + (double)a[0].l : 0.0;
     }
     if (threadIdx.x == 0) {
         CGState& S = n.st[r];
