@@ -33,7 +33,7 @@ EXPORTS = [
     "mech_set_coords", "mech_get_coords", "mech_rebuild_neighbors", "mech_get_pairs", "mech_energy",
     "mech_forces", "mech_minimize", "mech_get_forces", "mech_get_stretch_forces", "mech_get_timing",
     "mech_reset_coords", "mech_profile", "mech_filament_energy_device", "mech_hvp", "mech_set_linker_params",
-    "mech_adjoint", "mech_newton_refine", "mech_autotune", "mech_set_tuning",
+    "mech_adjoint", "mech_newton_refine", "mech_autotune", "mech_set_tuning", "mech_set_graph_mode",
 ]
 
 
@@ -161,6 +161,7 @@ def load(build_if_missing: bool = False):
         L.mech_hvp.argtypes = [vp, C.c_int32, C.c_int32, _dp, _dp]
         L.mech_autotune.argtypes = [vp, C.c_int32, C.POINTER(MechTuning)]
         L.mech_set_tuning.argtypes = [vp, C.POINTER(MechTuning)]
+        L.mech_set_graph_mode.argtypes = [vp, C.c_int32]
         L.mech_set_linker_params.argtypes = [vp, C.c_int32, _dp, _dp]
         L.mech_adjoint.argtypes = [vp, C.c_int32, _dp, C.c_double, C.POINTER(MechSolveParams), _dp, _dp,
                                    C.POINTER(MechSolveInfo)]

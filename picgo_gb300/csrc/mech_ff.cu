@@ -258,6 +258,60 @@ __device__ void finalize_force(const DevNet<Real>& n, int r, double* sh) {
 }
 
 // ---------------------------------------------------------------------------
+// Conditions of the minimizer's conditional graph (GraphConds).
+// ---------------------------------------------------------------------------
+constexpr int kCondTrial = 2, kCondForce = 3, kCondDir = 4, kCondMisc = 5;   // counter slots
+
+// Which phases the replicas are in, read past L1 (other blocks wrote the
+// states); every thread of one block calls it, thread 0 sets the handles.
+// `head`: the kernel at the head of a loop body, which also counts bodies and
+// decides whether the loop runs another one after this body.
+template <typename Real>
+__device__ void set_conditions(const DevNet<Real>& n, bool head, int phase_slot) {
+    int tr = 0, fo = 0, di = 0, mi = 0, host = 0;
+    for (int r = threadIdx.x; r < n.R; r += blockDim.x) {
+        const int ph = __ldcg(&n.st[r].phase);
+        tr |= ph == PH_LS_TRIAL;
+        fo |= ph == PH_FORCE;
+        di |= ph == PH_DIR;
+        mi |= ph == PH_RESET || ph == PH_FAILED;
+        host |= ph >= PH_RECOVER;   // the recovery move is sequenced by the host
+    }
+    tr = __syncthreads_or(tr);
+    fo = __syncthreads_or(fo);
+    di = __syncthreads_or(di);
+    mi = __syncthreads_or(mi);
+    host = __syncthreads_or(host);
+    if (threadIdx.x != 0) return;
+    cudaGraphSetConditional(n.cond.trial, tr ? 1u : 0u);
+    cudaGraphSetConditional(n.cond.force, fo ? 1u : 0u);
+    cudaGraphSetConditional(n.cond.dir, di ? 1u : 0u);
+    cudaGraphSetConditional(n.cond.misc, mi ? 1u : 0u);
+    if (phase_slot >= 0) n.cond.counter[phase_slot]++;
+    if (head) {
+        // the loop ends after this body when nothing is left to do on the
+        // device, an error is latched or the body budget of the launch is spent
+        const int bodies = ++n.cond.counter[0];
+        const bool more = (tr | fo | di | mi) && !host && __ldcg(n.err) == 0 && bodies < n.cond.cap;
+        cudaGraphSetConditional(n.cond.loop, more ? 1u : 0u);
+    }
+}
+
+// After a phase's per-replica reduction (one block per replica): the last
+// block to finish sets the conditions of the phases that follow in the body.
+template <typename Real>
+__device__ void after_phase(const DevNet<Real>& n, int phase_slot, int* s_flag) {
+    if (!n.cond.on) return;
+    if (last_tile(n.cond.counter + 1, 0, gridDim.x, s_flag)) set_conditions(n, false, phase_slot);
+}
+
+// The kernel at the head of every body of the minimizer's while loop.
+template <typename Real>
+__global__ void __launch_bounds__(kBlock) k_body_head(DevNet<Real> n) {
+    set_conditions(n, true, -1);
+}
+
+// ---------------------------------------------------------------------------
 // filament energy: stretching + bending of the tile's own cylinders/triples
 // ---------------------------------------------------------------------------
 template <typename Real>
@@ -479,9 +533,10 @@ __global__ void __launch_bounds__(kBlock) k_force_gather(DevNet<Real> n, int wan
 template <typename Real>
 __global__ void __launch_bounds__(kBlock) k_finalize_force(DevNet<Real> n, int want) {
     __shared__ double sh[32 * 3];
+    __shared__ int s_flag;
     const int r = blockIdx.x;
-    if (!replica_selected(n.st[r], want)) return;
-    finalize_force(n, r, sh);
+    if (replica_selected(n.st[r], want)) finalize_force(n, r, sh);
+    after_phase(n, kCondForce, &s_flag);
 }
 
 // One block per replica: the energy reduction and the line-search step, after
@@ -489,9 +544,10 @@ __global__ void __launch_bounds__(kBlock) k_finalize_force(DevNet<Real> n, int w
 template <typename Real>
 __global__ void __launch_bounds__(kBlock) k_finalize_energy(DevNet<Real> n, int want, int trial) {
     __shared__ double sh[32 * MECH_NUM_FF];
+    __shared__ int s_flag;
     const int r = blockIdx.x;
-    if (!replica_selected(n.st[r], want)) return;
-    finalize_energy(n, r, trial, sh);
+    if (replica_selected(n.st[r], want)) finalize_energy(n, r, trial, sh);
+    after_phase(n, kCondTrial, &s_flag);
 }
 
 // ---------------------------------------------------------------------------
@@ -1074,10 +1130,7 @@ __global__ void __launch_bounds__(kBlock) k_direction(DevNet<Real> n) {
 // One block per replica after the direction update: the slope d.F, the
 // conjugacy test and the next iteration's start (CGMethod.hpp:1553-1560).
 template <typename Real>
-__global__ void __launch_bounds__(kBlock) k_finalize_direction(DevNet<Real> n) {
-    __shared__ double sh[32];
-    const int r = blockIdx.x;
-    if (n.st[r].phase != PH_DIR) return;
+__device__ void finalize_direction(const DevNet<Real>& n, int r, double* sh) {
     const RepTiles rt = n.rt[r];
     double slope;
     if constexpr (sizeof(Real) == 8) {
@@ -1104,6 +1157,15 @@ __global__ void __launch_bounds__(kBlock) k_finalize_direction(DevNet<Real> n) {
             begin_iteration(S);
         }
     }
+}
+
+template <typename Real>
+__global__ void __launch_bounds__(kBlock) k_finalize_direction(DevNet<Real> n) {
+    __shared__ double sh[32];
+    __shared__ int s_flag;
+    const int r = blockIdx.x;
+    if (n.st[r].phase == PH_DIR) finalize_direction(n, r, sh);
+    after_phase(n, kCondDir, &s_flag);
 }
 
 // d = F (resetCGParams, CGMethod.hpp:963-972); the new slope d.F is F.F.
@@ -1150,8 +1212,9 @@ __global__ void __launch_bounds__(kBlock) k_reset(DevNet<Real> n) {
 }
 
 // lambda = 0 after a line search (CGMethod.hpp:1337-1367)
-__global__ void k_dispatch_failed(CGState* st, int R) {
+__global__ void k_dispatch_failed(CGState* st, int R, int* misc_count) {
     const int r = blockIdx.x * blockDim.x + threadIdx.x;
+    if (misc_count && r == 0) ++*misc_count;   // failure-dispatch bodies of the conditional graph
     if (r >= R) return;
     CGState& S = st[r];
     if (S.phase != PH_FAILED) return;
@@ -1314,8 +1377,14 @@ int launch_reset(const DevNet<Real>& n, cudaStream_t s) {
 }
 
 template <typename Real>
+int launch_body_head(const DevNet<Real>& n, cudaStream_t s) {
+    k_body_head<Real><<<1, kBlock, 0, s>>>(n);
+    return 1;
+}
+
+template <typename Real>
 int launch_dispatch_failed(const DevNet<Real>& n, cudaStream_t s) {
-    k_dispatch_failed<<<(n.R + 127) / 128, 128, 0, s>>>(n.st, n.R);
+    k_dispatch_failed<<<(n.R + 127) / 128, 128, 0, s>>>(n.st, n.R, n.cond.on ? n.cond.counter + kCondMisc : nullptr);
     return 1;
 }
 
@@ -1391,6 +1460,7 @@ int persistent_blocks(int device, int which) {
     template int launch_direction<R>(const DevNet<R>&, cudaStream_t);                   \
     template int launch_reset<R>(const DevNet<R>&, cudaStream_t);                       \
     template int launch_dispatch_failed<R>(const DevNet<R>&, cudaStream_t);             \
+    template int launch_body_head<R>(const DevNet<R>&, cudaStream_t);                   \
     template int launch_recover<R>(const DevNet<R>&, const Lanes&);                     \
     template int launch_backup_restore<R>(const DevNet<R>&, cudaStream_t);
 MECH_INSTANTIATE(double)

@@ -80,7 +80,8 @@ struct MechContext {
     // excluded volume
     DeviceBuffer ev_bead, ev_k, ev_la, ev_lb, ev_list, ev_list_count, ev_energy;
     // tiles, partials, state
-    DeviceBuffer ftile, stile, stile_kind, rt, part_fil, part_sp, st, ticket, gticket, err;
+    DeviceBuffer ftile, stile, stile_kind, rt, part_fil, part_sp, st, ticket, gticket, err, cond_counter;
+    int graph_mode = MECH_GRAPH_CONDITIONAL;
     DeviceBuffer contrib, ev_fb_count, ev_fb_list, ev_fb_energy, fb_moments, fb_tickets;
     // rebuild scratch
     PairBuild pb;
@@ -529,6 +530,8 @@ static int set_networks(MechContext* c, int R, const MechNetwork* nets) {
     CU(cudaMemsetAsync(c->ticket.p, 0, sizeof(int) * R, s));
     CU(c->gticket.ensure(sizeof(int) * 4));
     CU(cudaMemsetAsync(c->gticket.p, 0, sizeof(int) * 4, s));
+    CU(c->cond_counter.ensure(sizeof(int) * 8));
+    CU(cudaMemsetAsync(c->cond_counter.p, 0, sizeof(int) * 8, s));
     CU(c->err.ensure(sizeof(unsigned) * 4));
     CU(cudaMemsetAsync(c->err.p, 0, sizeof(unsigned) * 4, s));
     CU(c->ev_fb_count.ensure(sizeof(int) * 4));
@@ -866,6 +869,98 @@ static int capture_iteration_graph(MechContext* c, cudaGraphExec_t* exec, int* n
     return MECH_OK;
 }
 
+// Kernels per body part of the conditional graph (for the launch count).
+struct CondGraphCounts {
+    int head, trial, force, dir, misc;
+};
+static constexpr int kBodiesPerLaunch = 512;
+
+// The minimizer as one conditional graph: a while loop whose body is
+//   head -> if (trial) energy at x + lambda d -> if (force) forces
+//        -> if (direction) d = F + beta d -> if (misc) failure dispatch, reset.
+// The head sets the four conditions from the replicas' phases and whether the
+// loop runs another body; each phase's reduction sets them again for the
+// phases after it in the same body.  Only phases some replica is in run, and
+// control returns to the host when no replica has device work left, a
+// recovery move or an error needs the host, or kBodiesPerLaunch bodies ran.
+// The active kernels and their order are those of the unrolled graph.
+template <typename Real>
+static int capture_conditional_graph(MechContext* c, cudaGraphExec_t* exec, CondGraphCounts* counts) {
+    cudaGraph_t g = nullptr;
+    cudaError_t e = cudaGraphCreate(&g, 0);
+    auto fail = [&](cudaError_t err, const char* what) {
+        if (g) cudaGraphDestroy(g);
+        return set_err(MECH_ERR_CUDA, std::string("conditional graph, ") + what + ": " + cudaGetErrorString(err));
+    };
+    if (e != cudaSuccess) return fail(e, "create");
+    cudaMemsetParams mp{};
+    mp.dst = c->cond_counter.p;
+    mp.value = 0;
+    mp.elementSize = 4;
+    mp.width = 8;
+    mp.height = 1;
+    cudaGraphNode_t reset_node = nullptr;
+    if ((e = cudaGraphAddMemsetNode(&reset_node, g, nullptr, 0, &mp)) != cudaSuccess) return fail(e, "counter reset");
+    cudaGraphConditionalHandle h_loop = 0;
+    if ((e = cudaGraphConditionalHandleCreate(&h_loop, g, 1, cudaGraphCondAssignDefault)) != cudaSuccess)
+        return fail(e, "loop handle");
+    cudaGraphNodeParams wp{};
+    wp.type = cudaGraphNodeTypeConditional;
+    wp.conditional.handle = h_loop;
+    wp.conditional.type = cudaGraphCondTypeWhile;
+    wp.conditional.size = 1;
+    cudaGraphNode_t loop_node = nullptr;
+    if ((e = cudaGraphAddNode(&loop_node, g, &reset_node, nullptr, 1, &wp)) != cudaSuccess) return fail(e, "loop node");
+    cudaGraph_t body = wp.conditional.phGraph_out[0];
+    cudaGraphConditionalHandle h[4] = {0, 0, 0, 0};
+    for (int k = 0; k < 4; ++k)
+        if ((e = cudaGraphConditionalHandleCreate(&h[k], body, 0, 0)) != cudaSuccess) return fail(e, "phase handle");
+    DevNet<Real> n = make_devnet<Real>(c);
+    n.cond = GraphConds{h[0], h[1], h[2], h[3], h_loop, c->cond_counter.as<int>(), kBodiesPerLaunch, 1};
+    // capture `fn` into `graph` after `dep` (none when null)
+    auto capture_into = [&](cudaGraph_t graph, const cudaGraphNode_t* dep, auto&& fn) -> cudaError_t {
+        cudaError_t err = cudaStreamBeginCaptureToGraph(c->stream, graph, dep, nullptr, dep ? 1 : 0,
+                                                        cudaStreamCaptureModeThreadLocal);
+        if (err != cudaSuccess) return err;
+        fn();
+        cudaGraph_t out = nullptr;
+        return cudaStreamEndCapture(c->stream, &out);
+    };
+    if ((e = capture_into(body, nullptr, [&] { counts->head = launch_body_head<Real>(n, c->stream); })) != cudaSuccess)
+        return fail(e, "head capture");
+    cudaGraphNode_t prev = nullptr;
+    size_t nn = 1;
+    if ((e = cudaGraphGetNodes(body, &prev, &nn)) != cudaSuccess || nn != 1) return fail(e, "head node");
+    auto add_if = [&](cudaGraphConditionalHandle hc, auto&& fn) -> cudaError_t {
+        cudaGraphNodeParams ip{};
+        ip.type = cudaGraphNodeTypeConditional;
+        ip.conditional.handle = hc;
+        ip.conditional.type = cudaGraphCondTypeIf;
+        ip.conditional.size = 1;
+        cudaGraphNode_t node = nullptr;
+        cudaError_t err = cudaGraphAddNode(&node, body, &prev, nullptr, 1, &ip);
+        if (err != cudaSuccess) return err;
+        prev = node;
+        return capture_into(ip.conditional.phGraph_out[0], nullptr, fn);
+    };
+    if ((e = add_if(h[0], [&] { counts->trial = launch_energy<Real>(n, PH_LS_TRIAL, 1, c->lanes()); })) != cudaSuccess)
+        return fail(e, "trial body");
+    if ((e = add_if(h[1], [&] { counts->force = launch_forces<Real>(n, PH_FORCE, c->lanes()); })) != cudaSuccess)
+        return fail(e, "force body");
+    if ((e = add_if(h[2], [&] { counts->dir = launch_direction<Real>(n, c->stream); })) != cudaSuccess)
+        return fail(e, "direction body");
+    if ((e = add_if(h[3], [&] {
+             counts->misc = launch_dispatch_failed<Real>(n, c->stream);
+             counts->misc += launch_reset<Real>(n, c->stream);
+         })) != cudaSuccess)
+        return fail(e, "dispatch body");
+    e = cudaGraphInstantiate(exec, g, 0);
+    cudaGraphDestroy(g);
+    g = nullptr;
+    if (e != cudaSuccess) return set_err(MECH_ERR_CUDA, std::string("conditional graph, instantiate: ") + cudaGetErrorString(e));
+    return MECH_OK;
+}
+
 // Tile lists of the replicas still minimizing (in the same order, with the
 // same per-replica tile counts, so tickets and partial slots work unchanged);
 // finished replicas get empty ranges.  The kernels' grids then cover only the
@@ -957,17 +1052,29 @@ static int minimize_impl(MechContext* c, const MechCGParams* p, MechResult* res)
     for (int r = 0; r < c->R; ++r) before[r].assign(c->h_st[r].eval, c->h_st[r].eval + MECH_NUM_FF + 1);
     cudaGraphExec_t exec = nullptr;
     int per_graph = 0;
-    if ((rc = capture_iteration_graph<Real>(c, &exec, &per_graph))) return rc;
+    CondGraphCounts cc{};
+    const bool conditional = c->graph_mode == MECH_GRAPH_CONDITIONAL;
+    auto build_graph = [&]() {
+        return conditional ? capture_conditional_graph<Real>(c, &exec, &cc)
+                           : capture_iteration_graph<Real>(c, &exec, &per_graph);
+    };
+    if ((rc = build_graph())) return rc;
     long long graphs = 0;
     long long max_graphs = 0;
     for (int r = 0; r < c->R; ++r)
         max_graphs = std::max<long long>(max_graphs, 4LL * c->h_st[r].forceCallLimit / kBlocksPerGraph + 1000);
     int status = MECH_OK;
+    int body_counts[8] = {0, 0, 0, 0, 0, 0, 0, 0};
     for (;;) {
         CU(cudaGraphLaunch(exec, s));
         ++graphs;
-        launches += per_graph;
+        if (conditional)   // bodies and phases this launch ran (read after the sync in pull_states)
+            CU(cudaMemcpyAsync(body_counts, c->cond_counter.p, sizeof(body_counts), cudaMemcpyDeviceToHost, s));
         if ((rc = pull_states(c))) { cudaGraphExecDestroy(exec); return rc; }
+        launches += conditional ? (long long)body_counts[0] * cc.head + (long long)body_counts[2] * cc.trial +
+                                      (long long)body_counts[3] * cc.force + (long long)body_counts[4] * cc.dir +
+                                      (long long)body_counts[5] * cc.misc
+                                : per_graph;
         if (*c->h_err) {
             status = err_status(*c->h_err);
             break;
@@ -998,7 +1105,7 @@ static int minimize_impl(MechContext* c, const MechCGParams* p, MechResult* res)
                 exec = nullptr;
                 if ((rc = compact_tiles(c, act))) { c->compact = false; return rc; }
                 n = make_devnet<Real>(c);
-                if ((rc = capture_iteration_graph<Real>(c, &exec, &per_graph))) { c->compact = false; return rc; }
+                if ((rc = build_graph())) { c->compact = false; return rc; }
             }
         }
         if (graphs > max_graphs) {
@@ -1249,6 +1356,13 @@ int32_t mech_get_stretch_forces(MechContext* ctx, int32_t r, double* linker_f, d
         CU(cudaMemcpy(linker_f, ctx->lk_sf.as<double>() + h.lk_begin, sizeof(double) * h.nlk, cudaMemcpyDeviceToHost));
     if (motor_f && h.nmt > 0)
         CU(cudaMemcpy(motor_f, ctx->mt_sf.as<double>() + h.mt_begin, sizeof(double) * h.nmt, cudaMemcpyDeviceToHost));
+    return MECH_OK;
+}
+
+int32_t mech_set_graph_mode(MechContext* ctx, int32_t mode) {
+    if (!ctx) return set_err(MECH_ERR_ARG, "null context");
+    if (mode != MECH_GRAPH_CONDITIONAL && mode != MECH_GRAPH_UNROLLED) return set_err(MECH_ERR_ARG, "bad graph mode");
+    ctx->graph_mode = mode;
     return MECH_OK;
 }
 

@@ -100,6 +100,19 @@ struct RepTiles {
     int sp_begin[K_NUM_SPARSE], sp_end[K_NUM_SPARSE];
 };
 
+// Conditions of the minimizer's conditional graph: a while loop whose body
+// runs one guarded phase after another (line-search trial, forces, direction,
+// failure dispatch + reset).  The kernel at the head of a body and the last
+// block of each phase's reduction set them from the replicas' phases; outside
+// that graph `on` is 0 and no kernel touches them.
+struct GraphConds {
+    unsigned long long trial, force, dir, misc, loop;   // cudaGraphConditionalHandle values
+    int* counter;   // [0] bodies run in this graph launch, [1] reduction ticket,
+                    // [2..5] trial, force, direction, failure-dispatch bodies run (for the launch count)
+    int cap;        // bodies per graph launch before control returns to the host
+    int on;
+};
+
 // Everything the kernels read, passed by value.
 template <typename Real>
 struct DevNet {
@@ -152,6 +165,7 @@ struct DevNet {
     int* ticket;            // [R] last-tile tickets
     int* gticket;           // whole-grid ticket
     unsigned* err;          // device error word
+    GraphConds cond;
 };
 
 #ifdef __CUDACC__
@@ -181,6 +195,9 @@ template <typename Real> int launch_forces(const DevNet<Real>& n, int want, cons
 template <typename Real> int launch_direction(const DevNet<Real>& n, cudaStream_t s);
 template <typename Real> int launch_reset(const DevNet<Real>& n, cudaStream_t s);
 template <typename Real> int launch_dispatch_failed(const DevNet<Real>& n, cudaStream_t s);
+// head of a body of the minimizer's conditional graph: sets the phase
+// conditions, counts the body and decides whether the loop continues
+template <typename Real> int launch_body_head(const DevNet<Real>& n, cudaStream_t s);
 template <typename Real> int launch_recover(const DevNet<Real>& n, const Lanes& L);
 template <typename Real> int launch_backup_restore(const DevNet<Real>& n, cudaStream_t s);
 // single kernel families in plain-evaluation mode, for profiling:

@@ -181,6 +181,11 @@ class Engine:
     def reset_coords(self) -> None:
         check(self._L.mech_reset_coords(self._ctx))
 
+    def set_graph_mode(self, mode: str) -> None:
+        """'conditional' (default): one graph whose while loop runs only the phases in use;
+        'unrolled': relaunched graphs of 8 unrolled iteration blocks.  Same results."""
+        check(self._L.mech_set_graph_mode(self._ctx, {"conditional": 0, "unrolled": 1}[mode]))
+
     # -- second order (FP64 contexts) -----------------------------------------
     def hvp(self, v: np.ndarray, replica: int = 0, jacobian: bool = False) -> np.ndarray:
         """H v at the current coordinates (caller bead order): the energy's Hessian,
