@@ -85,8 +85,14 @@ __device__ __forceinline__ int run_slot(int b, int stride, int k) {
     return k == 0 ? b : (b / stride + 1) * stride + (k - 1) * stride;
 }
 
+// The CG step logic of the finalizers runs in thread 0 on a register copy of
+// its replica's state, loaded at the start so that the loads overlap the
+// block's reduction, and stored back once: done field by field on global
+// memory, the branchy logic waits on one dependent load after another.
 template <typename Real>
 __device__ void finalize_energy(const DevNet<Real>& n, int r, int trial, double* sh) {
+    CGState S;
+    if (threadIdx.x == 0) S = n.st[r];
     const RepTiles rt = n.rt[r];
     const int stride = sizeof(Real) == 4 ? n.ptiles[0] : 1;
     const int nslot = run_slots(rt.fil_begin, rt.fil_end, stride);
@@ -153,7 +159,6 @@ __device__ void finalize_energy(const DevNet<Real>& n, int r, int trial, double*
         last = bestPair;
     }
     if (ev_failed) e[MECH_FF_EXVOL] = -1.0;
-    CGState& S = n.st[r];
     double tot = 0.0;
     bool failed = false;
     for (int k = 0; k < MECH_NUM_FF; ++k) {
@@ -174,10 +179,49 @@ __device__ void finalize_energy(const DevNet<Real>& n, int r, int trial, double*
     } else {
         S.E0 = E;
     }
+    n.st[r] = S;
+}
+
+// CG bookkeeping after the forces (CGMethod.hpp:1540-1580): max |F|, beta.
+__device__ __forceinline__ void force_step(CGState& S, double mx, double ff, double ffp) {
+    const int ph = S.phase;
+    if (ph == PH_FORCE || ph == PH_RECOVER_FORCE) S.numForceCall++;
+    S.maxF = mx;
+    S.FdotF = ff;
+    S.fbuf ^= 1;
+    if (!isfinite(mx)) {   // CGMethod::maxF throws (CGMethod.hpp:207-210)
+        S.status = MECH_ERR_NONFINITE;
+        S.phase = PH_ERROR;
+        return;
+    }
+    if (ph == PH_FORCE) {
+        S.energyRelChange = fabs(S.newEnergy - S.prevEnergy) / fabs(S.prevEnergy);
+        S.prevEnergy = S.newEnergy;
+        double beta = 0.0;
+        if (S.method == 1) {
+            S.newGrad = ff;
+            beta = S.newGrad / S.lastFdotF;
+        } else if (S.method == 2) {
+            S.newGrad = ff;
+            S.prevGrad = ffp;
+            beta = fmax(0.0, (S.newGrad - S.prevGrad) / S.lastFdotF);
+        }
+        S.beta = beta;
+        // minimum-energy backup once past half the call limit (CGMethod.hpp:1564-1566)
+        if (mx <= 10 * S.gradTol && S.numIter > S.forceCallLimit / 2 && S.totalEnergy <= S.minimumE) {
+            S.minimumE = S.totalEnergy;
+            S.backupPending = 1;
+        }
+        S.phase = PH_DIR;
+    } else if (ph == PH_RECOVER_FORCE) {
+        S.phase = PH_RECOVER_ENERGY;
+    }
 }
 
 template <typename Real>
 __device__ void finalize_force(const DevNet<Real>& n, int r, double* sh) {
+    CGState S;
+    if (threadIdx.x == 0) S = n.st[r];
     const RepTiles rt = n.rt[r];
     const int stride = 1;   // k_force_gather writes one slot per tile
     const int nslot = run_slots(rt.fil_begin, rt.fil_end, stride);
@@ -222,39 +266,8 @@ __device__ void finalize_force(const DevNet<Real>& n, int r, double* sh) {
         ffp = red[2];
         if (threadIdx.x != 0) return;
     }
-    CGState& S = n.st[r];
-    const int ph = S.phase;
-    if (ph == PH_FORCE || ph == PH_RECOVER_FORCE) S.numForceCall++;
-    S.maxF = mx;
-    S.FdotF = ff;
-    S.fbuf ^= 1;
-    if (!isfinite(mx)) {   // CGMethod::maxF throws (CGMethod.hpp:207-210)
-        S.status = MECH_ERR_NONFINITE;
-        S.phase = PH_ERROR;
-        return;
-    }
-    if (ph == PH_FORCE) {
-        S.energyRelChange = fabs(S.newEnergy - S.prevEnergy) / fabs(S.prevEnergy);
-        S.prevEnergy = S.newEnergy;
-        double beta = 0.0;
-        if (S.method == 1) {
-            S.newGrad = ff;
-            beta = S.newGrad / S.lastFdotF;
-        } else if (S.method == 2) {
-            S.newGrad = ff;
-            S.prevGrad = ffp;
-            beta = fmax(0.0, (S.newGrad - S.prevGrad) / S.lastFdotF);
-        }
-        S.beta = beta;
-        // minimum-energy backup once past half the call limit (CGMethod.hpp:1564-1566)
-        if (mx <= 10 * S.gradTol && S.numIter > S.forceCallLimit / 2 && S.totalEnergy <= S.minimumE) {
-            S.minimumE = S.totalEnergy;
-            S.backupPending = 1;
-        }
-        S.phase = PH_DIR;
-    } else if (ph == PH_RECOVER_FORCE) {
-        S.phase = PH_RECOVER_ENERGY;
-    }
+    force_step(S, mx, ff, ffp);
+    n.st[r] = S;
 }
 
 // ---------------------------------------------------------------------------
@@ -1131,6 +1144,8 @@ __global__ void __launch_bounds__(kBlock) k_direction(DevNet<Real> n) {
 // conjugacy test and the next iteration's start (CGMethod.hpp:1553-1560).
 template <typename Real>
 __device__ void finalize_direction(const DevNet<Real>& n, int r, double* sh) {
+    CGState S;
+    if (threadIdx.x == 0) S = n.st[r];
     const RepTiles rt = n.rt[r];
     double slope;
     if constexpr (sizeof(Real) == 8) {
@@ -1144,7 +1159,6 @@ __device__ void finalize_direction(const DevNet<Real>& n, int r, double* sh) {
         slope = threadIdx.x == 0 ? (double)a[0].h + (double)a[0].l : 0.0;
     }
     if (threadIdx.x == 0) {
-        CGState& S = n.st[r];
         if (S.backupPending) {
             S.backupValid = 1;
             S.backupPending = 0;
@@ -1156,6 +1170,7 @@ __device__ void finalize_direction(const DevNet<Real>& n, int r, double* sh) {
             if (S.method >= 1) S.lastFdotF = S.newGrad;
             begin_iteration(S);
         }
+        n.st[r] = S;
     }
 }
 

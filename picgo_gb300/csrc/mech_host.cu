@@ -81,7 +81,7 @@ struct MechContext {
     DeviceBuffer ev_bead, ev_k, ev_la, ev_lb, ev_list, ev_list_count, ev_energy;
     // tiles, partials, state
     DeviceBuffer ftile, stile, stile_kind, rt, part_fil, part_sp, st, ticket, gticket, err, cond_counter;
-    int graph_mode = MECH_GRAPH_CONDITIONAL;
+    int graph_mode = MECH_GRAPH_UNROLLED;
     DeviceBuffer contrib, ev_fb_count, ev_fb_list, ev_fb_energy, fb_moments, fb_tickets;
     // rebuild scratch
     PairBuild pb;

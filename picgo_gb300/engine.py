@@ -182,8 +182,8 @@ class Engine:
         check(self._L.mech_reset_coords(self._ctx))
 
     def set_graph_mode(self, mode: str) -> None:
-        """'conditional' (default): one graph whose while loop runs only the phases in use;
-        'unrolled': relaunched graphs of 8 unrolled iteration blocks.  Same results."""
+        """'unrolled' (default): relaunched graphs of 8 unrolled iteration blocks;
+        'conditional': one graph whose device while loop runs only the phases in use.  Same results."""
         check(self._L.mech_set_graph_mode(self._ctx, {"conditional": 0, "unrolled": 1}[mode]))
 
     # -- second order (FP64 contexts) -----------------------------------------
