@@ -612,12 +612,16 @@ static inline int ev_tiles_of(const DevNet<Real>& n, int* off) {
     return n.sp_tiles[K_EXVOL];
 }
 
+// Inside an evaluation (standalone = false) the work-list counts are zero on
+// entry: the evaluation's reduction kernel zeroes them for the next one, which
+// keeps a memset off the head of the excluded-volume lane.  A standalone
+// launch zeroes them first and leaves them as they end.
 template <typename Real>
-int launch_exvol_energy(const DevNet<Real>& n, int want, int trial, cudaStream_t s) {
+int launch_exvol_energy(const DevNet<Real>& n, int want, int trial, cudaStream_t s, bool standalone) {
     int off = 0;
     const int nt = ev_tiles_of(n, &off);
     if (nt == 0) return 0;
-    reset_counts(n, s);
+    if (standalone) reset_counts(n, s);
     k_exvol<Real><<<nt, kBlock, 0, s>>>(n, want, trial, 0, off);
     int k = 1;
     if constexpr (sizeof(Real) == 4) {
@@ -629,11 +633,11 @@ int launch_exvol_energy(const DevNet<Real>& n, int want, int trial, cudaStream_t
 }
 
 template <typename Real>
-int launch_exvol_forces(const DevNet<Real>& n, int want, cudaStream_t s) {
+int launch_exvol_forces(const DevNet<Real>& n, int want, cudaStream_t s, bool standalone) {
     int off = 0;
     const int nt = ev_tiles_of(n, &off);
     if (nt == 0) return 0;
-    reset_counts(n, s);
+    if (standalone) reset_counts(n, s);
     k_exvol<Real><<<nt, kBlock, 0, s>>>(n, want, 0, 1, off);
     int k = 1;
     if constexpr (sizeof(Real) == 4) {
@@ -644,7 +648,7 @@ int launch_exvol_forces(const DevNet<Real>& n, int want, cudaStream_t s) {
     return k + 1;
 }
 
-template int launch_exvol_energy<MECH_EXVOL_REAL>(const DevNet<MECH_EXVOL_REAL>&, int, int, cudaStream_t);
-template int launch_exvol_forces<MECH_EXVOL_REAL>(const DevNet<MECH_EXVOL_REAL>&, int, cudaStream_t);
+template int launch_exvol_energy<MECH_EXVOL_REAL>(const DevNet<MECH_EXVOL_REAL>&, int, int, cudaStream_t, bool);
+template int launch_exvol_forces<MECH_EXVOL_REAL>(const DevNet<MECH_EXVOL_REAL>&, int, cudaStream_t, bool);
 
 }  // namespace mech

@@ -318,6 +318,19 @@ __device__ void after_phase(const DevNet<Real>& n, int phase_slot, int* s_flag) 
     if (last_tile(n.cond.counter + 1, 0, gridDim.x, s_flag)) set_conditions(n, false, phase_slot);
 }
 
+// After an evaluation's per-replica reduction: the last block zeroes the
+// excluded-volume work-list counts for the next evaluation (every block has
+// read them by then), then sets the graph conditions when there are any.
+template <typename Real>
+__device__ void after_evaluation(const DevNet<Real>& n, int phase_slot, int* s_flag) {
+    if (!last_tile(n.gticket, 0, gridDim.x, s_flag)) return;
+    if (threadIdx.x == 0) {
+        if (n.ev_list_count) *n.ev_list_count = 0;
+        if (n.ev_fb_count) *n.ev_fb_count = 0;
+    }
+    if (n.cond.on) set_conditions(n, false, phase_slot);
+}
+
 // The kernel at the head of every body of the minimizer's while loop.
 template <typename Real>
 __global__ void __launch_bounds__(kBlock) k_body_head(DevNet<Real> n) {
@@ -549,7 +562,7 @@ __global__ void __launch_bounds__(kBlock) k_finalize_force(DevNet<Real> n, int w
     __shared__ int s_flag;
     const int r = blockIdx.x;
     if (replica_selected(n.st[r], want)) finalize_force(n, r, sh);
-    after_phase(n, kCondForce, &s_flag);
+    after_evaluation(n, kCondForce, &s_flag);
 }
 
 // One block per replica: the energy reduction and the line-search step, after
@@ -560,7 +573,7 @@ __global__ void __launch_bounds__(kBlock) k_finalize_energy(DevNet<Real> n, int 
     __shared__ int s_flag;
     const int r = blockIdx.x;
     if (replica_selected(n.st[r], want)) finalize_energy(n, r, trial, sh);
-    after_phase(n, kCondTrial, &s_flag);
+    after_evaluation(n, kCondTrial, &s_flag);
 }
 
 // ---------------------------------------------------------------------------
@@ -678,6 +691,23 @@ __device__ void issue_energy_stage(const DevNet<float>& n, int4 t, bool tr, Ener
         if (bytes[k]) bulk_copy_g2s(dst[k], src[k], bytes[k], bar);
 }
 
+// True in every thread when a launch selects no replica of the block's tile
+// range [t0, t1): tiles are ordered by replica, so a range whose first and
+// last tiles share a replica belongs to it alone.  The block then exits before
+// any barrier or descriptor setup.
+__device__ __forceinline__ bool idle_range(const DevNet<float>& n, int t0, int t1, int want, int* s_flag) {
+    if (threadIdx.x == 0) {
+        int idle = t1 <= t0;
+        if (!idle) {
+            const int ra = n.ftile[t0].replica, rb = n.ftile[t1 - 1].replica;
+            idle = ra == rb && !replica_selected(n.st[ra], want);
+        }
+        *s_flag = idle;
+    }
+    __syncthreads();
+    return *s_flag != 0;
+}
+
 __global__ void __launch_bounds__(kBlock) k_fil_energy_bulk(DevNet<float> n, int want, int trial) {
     __shared__ EnergyStage stage[kBulkStages];
     __shared__ __align__(8) uint64_t bar[kBulkStages];
@@ -688,6 +718,7 @@ __global__ void __launch_bounds__(kBlock) k_fil_energy_bulk(DevNet<float> n, int
     const int t0 = blockIdx.x * n.ptiles[0], t1 = min(t0 + n.ptiles[0], n.n_ftiles);
     const int nt = t1 - t0;
     const bool tr = trial != 0;
+    if (idle_range(n, t0, t1, want, &s_abort)) return;
     if (threadIdx.x == 0) {
         for (int k = 0; k < kBulkStages; ++k) mbar_init(&bar[k], 1);
         mbar_init_fence();
@@ -857,6 +888,7 @@ __global__ void __launch_bounds__(kBlock) k_fil_force_bulk(DevNet<float> n, int 
     __shared__ int s_abort;
     const int t0 = blockIdx.x * n.ptiles[1], t1 = min(t0 + n.ptiles[1], n.n_ftiles);
     const int nt = t1 - t0;
+    if (idle_range(n, t0, t1, want, &s_abort)) return;
     if (threadIdx.x == 0) {
         for (int k = 0; k < kBulkStages; ++k) mbar_init(&bar[k], 1);
         mbar_init_fence();
@@ -1338,7 +1370,7 @@ int launch_energy(const DevNet<Real>& n, int want, int trial, const Lanes& L) {
     cudaEventRecord(L.fork, L.main);
     cudaStreamWaitEvent(L.side, L.fork, 0);
     cudaStreamWaitEvent(L.side2, L.fork, 0);
-    launched += launch_exvol_energy<Real>(n, want, trial, L.side);
+    launched += launch_exvol_energy<Real>(n, want, trial, L.side, false);
     cudaEventRecord(L.join, L.side);
     if (lm + bb_t > 0) {
         k_bond_bnd<Real><<<lm + bb_t, kBlock, 0, L.side2>>>(n, want, trial, 0, lm, ev_t);
@@ -1361,7 +1393,7 @@ int launch_forces(const DevNet<Real>& n, int want, const Lanes& L) {
     cudaEventRecord(L.fork, L.main);
     cudaStreamWaitEvent(L.side, L.fork, 0);
     cudaStreamWaitEvent(L.side2, L.fork, 0);
-    launched += launch_exvol_forces<Real>(n, want, L.side);
+    launched += launch_exvol_forces<Real>(n, want, L.side, false);
     cudaEventRecord(L.join, L.side);
     if (lm + bb_t > 0) {
         k_bond_bnd<Real><<<lm + bb_t, kBlock, 0, L.side2>>>(n, want, 0, 1, lm, ev_t);

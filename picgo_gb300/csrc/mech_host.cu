@@ -1437,10 +1437,13 @@ static int profile_impl(MechContext* c, int iters, MechProfile* o) {
         *ext = c->precision == MECH_PREC_MIXED ? v[0] : c->nev;
         *fb = v[1];
     };
-    o->ms_exvol_energy = timeit([&] { launch_exvol_energy<Real>(n, -1, 0, s); });
+    o->ms_exvol_energy = timeit([&] { launch_exvol_energy<Real>(n, -1, 0, s, true); });
     counts(&o->n_exvol_ext_energy, &o->n_exvol_fallback_energy);
-    o->ms_exvol_force = timeit([&] { launch_exvol_forces<Real>(n, -1, s); });
+    o->ms_exvol_force = timeit([&] { launch_exvol_forces<Real>(n, -1, s, true); });
     counts(&o->n_exvol_ext_force, &o->n_exvol_fallback_force);
+    // evaluations expect zero counts on entry
+    if (c->ev_list_count.p) CU(cudaMemsetAsync(c->ev_list_count.p, 0, 4 * sizeof(int), s));
+    CU(cudaMemsetAsync(n.ev_fb_count, 0, sizeof(int), s));
     // a line-search trial: positions x + lambda d formed and materialized on the fly
     o->ms_trial_energy_eval = timeit([&] { launch_energy<Real>(n, -1, 1, c->lanes()); });
     // every replica finished: each launch of an iteration block reads its phase and exits

@@ -210,8 +210,11 @@ int persistent_blocks(int device, int which);
 // Records the text mech_last_error returns on this thread; returns `code`.
 int set_error_text(int code, const std::string& msg);
 // excluded-volume kernels (mech_exvol.cu, one object per precision)
-template <typename Real> int launch_exvol_energy(const DevNet<Real>& n, int want, int trial, cudaStream_t s);
-template <typename Real> int launch_exvol_forces(const DevNet<Real>& n, int want, cudaStream_t s);
+// (standalone: zero the work-list counts first; inside an evaluation they are
+// zero on entry, reset by the evaluation's reduction kernel)
+template <typename Real> int launch_exvol_energy(const DevNet<Real>& n, int want, int trial, cudaStream_t s,
+                                                 bool standalone);
+template <typename Real> int launch_exvol_forces(const DevNet<Real>& n, int want, cudaStream_t s, bool standalone);
 
 // ---- Hessian-vector products and solves (mech_hvp.cu, FP64 engine) --------
 // hv = (H + shift I) v at the positions in x[0], v and hv in internal bead
