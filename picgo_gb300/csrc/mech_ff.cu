@@ -555,6 +555,110 @@ __global__ void __launch_bounds__(kBlock) k_force_gather(DevNet<Real> n, int wan
     }
 }
 
+// Mixed engine gather: 64 threads per tile, each taking 4 consecutive beads
+// whose force records (4 x 12 B) move as three 16-byte vectors, when the tile
+// starts on a multiple of 4 beads (always, unless a replica before it has a
+// bead count that is not; a partial group at the tile's end goes bead by
+// bead); otherwise 4 beads strided by 64.  The tile's partials combine the
+// two warps of its 64 threads.
+__global__ void __launch_bounds__(kBlock) k_force_gather_mx(DevNet<float> n, int want) {
+    static_assert(kFilTile == 256 && kBlock == 64 * kGatherTiles, "64 threads x 4 beads per tile");
+    __shared__ float sh[8][5];   // per warp: F.F (hi, lo), F.Fprev (hi, lo), max
+    __shared__ int s_go[kGatherTiles], s_fb[kGatherTiles];
+    const int t0 = blockIdx.x * kGatherTiles;
+    if (threadIdx.x < kGatherTiles) {
+        const int ti = t0 + threadIdx.x;
+        int go = 0, fb = 0;
+        if (ti < n.n_ftiles) {
+            const CGState& S = n.st[n.ftile[ti].replica];
+            go = replica_selected(S, want);
+            fb = S.fbuf;
+        }
+        s_go[threadIdx.x] = go;
+        s_fb[threadIdx.x] = fb;
+    }
+    __syncthreads();
+    const int j = threadIdx.x >> 6, tt = threadIdx.x & 63;
+    FF aff, affp;
+    float mx = 0.f;
+    if (s_go[j]) {   // uniform over the tile's two warps
+        const Tile t = n.ftile[t0 + j];
+        const int fb = s_fb[j];
+        const int b0 = t.begin + 4 * tt;
+        const bool vec_tile = (t.begin & 3) == 0;   // uniform over the tile
+        if (vec_tile && b0 + 4 <= t.end) {
+            float* Fo = n.f[fb ^ 1] + 3 * (size_t)b0;
+            const float* Fp = n.f[fb] + 3 * (size_t)b0;
+            const float4 u0 = reinterpret_cast<const float4*>(Fo)[0], u1 = reinterpret_cast<const float4*>(Fo)[1],
+                         u2 = reinterpret_cast<const float4*>(Fo)[2];
+            const float4 p0 = reinterpret_cast<const float4*>(Fp)[0], p1 = reinterpret_cast<const float4*>(Fp)[1],
+                         p2 = reinterpret_cast<const float4*>(Fp)[2];
+            float F[12] = {u0.x, u0.y, u0.z, u0.w, u1.x, u1.y, u1.z, u1.w, u2.x, u2.y, u2.z, u2.w};
+            const float P[12] = {p0.x, p0.y, p0.z, p0.w, p1.x, p1.y, p1.z, p1.w, p2.x, p2.y, p2.z, p2.w};
+            int off[5];
+#pragma unroll
+            for (int q = 0; q < 5; ++q) off[q] = n.csr_off[b0 + q];
+#pragma unroll
+            for (int k = 0; k < 4; ++k)
+                for (int c = off[k]; c < off[k + 1]; ++c) {
+                    F[3 * k] += n.contrib[3 * (size_t)c];
+                    F[3 * k + 1] += n.contrib[3 * (size_t)c + 1];
+                    F[3 * k + 2] += n.contrib[3 * (size_t)c + 2];
+                }
+            reinterpret_cast<float4*>(Fo)[0] = make_float4(F[0], F[1], F[2], F[3]);
+            reinterpret_cast<float4*>(Fo)[1] = make_float4(F[4], F[5], F[6], F[7]);
+            reinterpret_cast<float4*>(Fo)[2] = make_float4(F[8], F[9], F[10], F[11]);
+#pragma unroll
+            for (int k = 0; k < 4; ++k) {
+                const float* f = F + 3 * k;
+                const bool fin = f[0] - f[0] == 0 && f[1] - f[1] == 0 && f[2] - f[2] == 0;
+                mx = fmaxf(mx, fin ? fmaxf(fmaxf(fabsf(f[0]), fabsf(f[1])), fabsf(f[2])) : INFINITY);
+                aff.add(bead_dot(f[0], f[1], f[2], f[0], f[1], f[2]));
+                affp.add(bead_dot(f[0], f[1], f[2], P[3 * k], P[3 * k + 1], P[3 * k + 2]));
+            }
+        } else {
+            // the partial group at the end of a vector tile, or a tile that
+            // starts off the 4-bead grid: 4 beads strided by 64
+#pragma unroll
+            for (int q = 0; q < 4; ++q) {
+                const int b = vec_tile ? b0 + q : t.begin + tt + 64 * q;
+                if (b < t.end) {
+                    float m1, f1, f2;
+                    gather_bead(n, b, fb, m1, f1, f2);
+                    mx = fmaxf(mx, m1);
+                    aff.add(f1);
+                    affp.add(f2);
+                }
+            }
+        }
+    }
+    warp_reduce_pair(aff.h, aff.l);
+    warp_reduce_pair(affp.h, affp.l);
+    mx = warp_max_f(mx);
+    const int w = threadIdx.x >> 5;
+    if ((threadIdx.x & 31) == 0) {
+        sh[w][0] = aff.h;
+        sh[w][1] = aff.l;
+        sh[w][2] = affp.h;
+        sh[w][3] = affp.l;
+        sh[w][4] = mx;
+    }
+    __syncthreads();
+    if (threadIdx.x < kGatherTiles && s_go[threadIdx.x]) {
+        // the tile's two warps, combined with an error-free sum
+        const int a = 2 * threadIdx.x, b = a + 1;
+        float s1, e1, s2, e2, h, l;
+        two_sum(sh[a][0], sh[b][0], s1, e1);
+        fast_two_sum(s1, __fadd_rn(e1, __fadd_rn(sh[a][1], sh[b][1])), h, l);
+        const float ffh = h, ffl = l;
+        two_sum(sh[a][2], sh[b][2], s2, e2);
+        fast_two_sum(s2, __fadd_rn(e2, __fadd_rn(sh[a][3], sh[b][3])), h, l);
+        float* p = reinterpret_cast<float*>(n.part_fil + 4 * (size_t)(t0 + threadIdx.x));
+        *reinterpret_cast<float4*>(p) = make_float4(fmaxf(sh[a][4], sh[b][4]), ffh, ffl, h);
+        p[4] = l;
+    }
+}
+
 // One block per replica: max |F|, the dots and the CG step logic after the gather.
 template <typename Real>
 __global__ void __launch_bounds__(kBlock) k_finalize_force(DevNet<Real> n, int want) {
@@ -1404,7 +1508,8 @@ int launch_forces(const DevNet<Real>& n, int want, const Lanes& L) {
     else k_fil_force<Real><<<n.n_ftiles, kBlock, 0, L.main>>>(n, want);
     cudaStreamWaitEvent(L.main, L.join, 0);
     cudaStreamWaitEvent(L.main, L.join2, 0);
-    k_force_gather<Real><<<(n.n_ftiles + kGatherTiles - 1) / kGatherTiles, kBlock, 0, L.main>>>(n, want);
+    if constexpr (sizeof(Real) == 4) k_force_gather_mx<<<(n.n_ftiles + kGatherTiles - 1) / kGatherTiles, kBlock, 0, L.main>>>(n, want);
+    else k_force_gather<Real><<<(n.n_ftiles + kGatherTiles - 1) / kGatherTiles, kBlock, 0, L.main>>>(n, want);
     k_finalize_force<Real><<<n.R, kBlock, 0, L.main>>>(n, want);
     return launched + 3;
 }
@@ -1465,7 +1570,8 @@ int launch_part(const DevNet<Real>& n, int which, cudaStream_t s) {
         case 1:
             if constexpr (sizeof(Real) == 4) k_fil_force_bulk<<<n.pgrid[1], kBlock, 0, s>>>(n, -1);
             else k_fil_force<Real><<<n.n_ftiles, kBlock, 0, s>>>(n, -1);
-            k_force_gather<Real><<<(n.n_ftiles + kGatherTiles - 1) / kGatherTiles, kBlock, 0, s>>>(n, -1);
+            if constexpr (sizeof(Real) == 4) k_force_gather_mx<<<(n.n_ftiles + kGatherTiles - 1) / kGatherTiles, kBlock, 0, s>>>(n, -1);
+            else k_force_gather<Real><<<(n.n_ftiles + kGatherTiles - 1) / kGatherTiles, kBlock, 0, s>>>(n, -1);
             k_finalize_force<Real><<<n.R, kBlock, 0, s>>>(n, -1);
             return 3;
         case 2: if (lm + bb_t > 0) { k_bond_bnd<Real><<<lm + bb_t, kBlock, 0, s>>>(n, -1, 0, 0, lm, ev_t); return 1; } return 0;
@@ -1479,7 +1585,8 @@ int launch_part(const DevNet<Real>& n, int which, cudaStream_t s) {
             else k_fil_force<Real><<<n.n_ftiles, kBlock, 0, s>>>(n, -1);
             return 1;
         case 6:   // the sparse gather with the CG partials alone
-            k_force_gather<Real><<<(n.n_ftiles + kGatherTiles - 1) / kGatherTiles, kBlock, 0, s>>>(n, -1);
+            if constexpr (sizeof(Real) == 4) k_force_gather_mx<<<(n.n_ftiles + kGatherTiles - 1) / kGatherTiles, kBlock, 0, s>>>(n, -1);
+            else k_force_gather<Real><<<(n.n_ftiles + kGatherTiles - 1) / kGatherTiles, kBlock, 0, s>>>(n, -1);
             return 1;
     }
     return 0;
