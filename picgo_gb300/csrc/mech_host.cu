@@ -110,12 +110,24 @@ struct MechContext {
     std::vector<RepTiles> h_rt;
     CGState* h_st = nullptr;   // pinned mirror of the states
     unsigned* h_err = nullptr;
+    // pinned snapshots taken after each minimizer graph launch: states, error
+    // word and the conditional graph's body counters, double-buffered
+    struct Snapshot {
+        CGState* st = nullptr;
+        unsigned* err = nullptr;   // [0] error word, [1..8] body counters
+        cudaEvent_t done = nullptr;
+    } snap[2];
     MechTiming timing{};
     std::vector<int32_t> cyl_local_first;   // replica-local cylinder -> internal global first bead
 
     ~MechContext() {
         if (h_st) cudaFreeHost(h_st);
         if (h_err) cudaFreeHost(h_err);
+        for (auto& k : snap) {
+            if (k.st) cudaFreeHost(k.st);
+            if (k.err) cudaFreeHost(k.err);
+            if (k.done) cudaEventDestroy(k.done);
+        }
         if (fork) cudaEventDestroy(fork);
         if (join) cudaEventDestroy(join);
         if (join2) cudaEventDestroy(join2);
@@ -544,6 +556,13 @@ static int set_networks(MechContext* c, int R, const MechNetwork* nets) {
     if (c->h_st) cudaFreeHost(c->h_st);
     CU(cudaMallocHost(&c->h_st, sizeof(CGState) * R));
     if (!c->h_err) CU(cudaMallocHost(&c->h_err, sizeof(unsigned) * 4));
+    for (auto& k : c->snap) {
+        if (k.st) cudaFreeHost(k.st);
+        k.st = nullptr;
+        CU(cudaMallocHost(&k.st, sizeof(CGState) * R));
+        if (!k.err) CU(cudaMallocHost(&k.err, sizeof(unsigned) * 9));
+        if (!k.done) CU(cudaEventCreateWithFlags(&k.done, cudaEventDisableTiming));
+    }
     CU(cudaStreamSynchronize(s));
     c->have_net = true;
     c->have_lists = false;
@@ -1064,55 +1083,101 @@ static int minimize_impl(MechContext* c, const MechCGParams* p, MechResult* res)
     for (int r = 0; r < c->R; ++r)
         max_graphs = std::max<long long>(max_graphs, 4LL * c->h_st[r].forceCallLimit / kBlocksPerGraph + 1000);
     int status = MECH_OK;
-    int body_counts[8] = {0, 0, 0, 0, 0, 0, 0, 0};
-    for (;;) {
+    // The next graph is launched before the host reads the snapshot of the
+    // previous one, so the device does not idle while the host checks the
+    // states.  A launch after every replica has finished, or while one waits
+    // for the host, only runs kernels that find nothing to do; before acting
+    // on a finished, failed or compactable state the host drains the launch
+    // in flight and acts on the newest snapshot.
+    auto launch = [&](int k) -> int {
         CU(cudaGraphLaunch(exec, s));
         ++graphs;
-        if (conditional)   // bodies and phases this launch ran (read after the sync in pull_states)
-            CU(cudaMemcpyAsync(body_counts, c->cond_counter.p, sizeof(body_counts), cudaMemcpyDeviceToHost, s));
-        if ((rc = pull_states(c))) { cudaGraphExecDestroy(exec); return rc; }
-        launches += conditional ? (long long)body_counts[0] * cc.head + (long long)body_counts[2] * cc.trial +
-                                      (long long)body_counts[3] * cc.force + (long long)body_counts[4] * cc.dir +
-                                      (long long)body_counts[5] * cc.misc
+        auto& sn = c->snap[k];
+        CU(cudaMemcpyAsync(sn.st, c->st.p, sizeof(CGState) * c->R, cudaMemcpyDeviceToHost, s));
+        CU(cudaMemcpyAsync(sn.err, c->err.p, sizeof(unsigned), cudaMemcpyDeviceToHost, s));
+        if (conditional)   // bodies and phases this launch ran
+            CU(cudaMemcpyAsync(sn.err + 1, c->cond_counter.p, 8 * sizeof(int), cudaMemcpyDeviceToHost, s));
+        CU(cudaEventRecord(sn.done, s));
+        return MECH_OK;
+    };
+    // launches of snapshot k's graph (the conditional graph counts what its bodies ran)
+    auto account = [&](int k) {
+        const int* bc = reinterpret_cast<const int*>(c->snap[k].err + 1);
+        launches += conditional ? (long long)bc[0] * cc.head + (long long)bc[2] * cc.trial +
+                                      (long long)bc[3] * cc.force + (long long)bc[4] * cc.dir + (long long)bc[5] * cc.misc
                                 : per_graph;
+    };
+    auto wants_host = [&](const CGState* st, unsigned err, bool* all_done) {
+        bool done = true, host = false;
+        long long live = 0;
+        for (int r = 0; r < c->R; ++r) {
+            const int ph = st[r].phase;
+            const bool act = ph != PH_DONE && ph != PH_ERROR;
+            if (act) {
+                done = false;
+                live += c->h_rt[r].fil_end - c->h_rt[r].fil_begin;
+            }
+            if (ph == PH_RECOVER) host = true;
+        }
+        *all_done = done;
+        // batched runs: relaunch over the live replicas once they hold at most half of the tiles
+        const bool compactable = c->R > 1 && !done && 2 * live <= (long long)n.n_ftiles;
+        return err != 0 || done || host || compactable || graphs > max_graphs;
+    };
+    int cur = 0;
+    if ((rc = launch(cur))) { cudaGraphExecDestroy(exec); return rc; }
+    for (;;) {
+        const int nxt = cur ^ 1;
+        if ((rc = launch(nxt))) { cudaGraphExecDestroy(exec); return rc; }
+        CU(cudaEventSynchronize(c->snap[cur].done));
+        account(cur);
+        bool all_done = false;
+        if (!wants_host(c->snap[cur].st, *c->snap[cur].err, &all_done)) {
+            cur = nxt;
+            continue;
+        }
+        // drain the launch in flight and act on its (newest) snapshot
+        CU(cudaEventSynchronize(c->snap[nxt].done));
+        account(nxt);
+        std::memcpy(c->h_st, c->snap[nxt].st, sizeof(CGState) * c->R);
+        *c->h_err = *c->snap[nxt].err;
         if (*c->h_err) {
             status = err_status(*c->h_err);
             break;
         }
-        bool all_done = true, recover = false;
+        bool recover = false;
+        std::vector<char> act(c->R, 0);
+        long long live = 0;
+        all_done = true;
         for (int r = 0; r < c->R; ++r) {
             const int ph = c->h_st[r].phase;
-            if (ph != PH_DONE && ph != PH_ERROR) all_done = false;
+            act[r] = ph != PH_DONE && ph != PH_ERROR;
+            if (act[r]) {
+                all_done = false;
+                live += c->h_rt[r].fil_end - c->h_rt[r].fil_begin;
+            }
             if (ph == PH_RECOVER) recover = true;
         }
         if (all_done) break;
-        if (recover) {
-            launches += launch_recover<Real>(n, c->lanes());
-            CU(cudaGetLastError());
-        }
-        // batched runs: once the replicas still minimizing hold at most half
-        // of the tiles in the current lists, relaunch over theirs only
-        if (c->R > 1) {
-            std::vector<char> act(c->R, 0);
-            long long live = 0;
-            for (int r = 0; r < c->R; ++r) {
-                const int ph = c->h_st[r].phase;
-                act[r] = ph != PH_DONE && ph != PH_ERROR;
-                if (act[r]) live += c->h_rt[r].fil_end - c->h_rt[r].fil_begin;
-            }
-            if (2 * live <= (long long)n.n_ftiles) {
-                cudaGraphExecDestroy(exec);
-                exec = nullptr;
-                if ((rc = compact_tiles(c, act))) { c->compact = false; return rc; }
-                n = make_devnet<Real>(c);
-                if ((rc = build_graph())) { c->compact = false; return rc; }
-            }
-        }
         if (graphs > max_graphs) {
             status = set_err(MECH_ERR_ITER_LIMIT, "minimizer loop exceeded its iteration cap");
             break;
         }
+        if (recover) {
+            launches += launch_recover<Real>(n, c->lanes());
+            CU(cudaGetLastError());
+        }
+        if (c->R > 1 && 2 * live <= (long long)n.n_ftiles) {
+            cudaGraphExecDestroy(exec);
+            exec = nullptr;
+            if ((rc = compact_tiles(c, act))) { c->compact = false; return rc; }
+            n = make_devnet<Real>(c);
+            if ((rc = build_graph())) { c->compact = false; return rc; }
+        }
+        cur = nxt ^ 1;
+        if ((rc = launch(cur))) { cudaGraphExecDestroy(exec); return rc; }
     }
+    CU(cudaStreamSynchronize(s));
     if (exec) cudaGraphExecDestroy(exec);
     c->compact = false;   // the full lists again for energiesAfter and later calls
     n = make_devnet<Real>(c);
