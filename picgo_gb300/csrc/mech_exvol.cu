@@ -121,7 +121,6 @@ template <typename Real>
 __global__ void __launch_bounds__(kBlock) k_exvol_fb_force(DevNet<Real> n, double* moments, int* tickets) {
     __shared__ double sh[32];
     __shared__ int s_last;
-    pdl_wait();   // the pair passes filled the fallback list
     const int cnt = min(*n.ev_fb_count, kExvolFallbackCap);
     const int N = kFbNodesForce;
     for (int wi = blockIdx.x; wi < cnt * kFbChunks; wi += gridDim.x) {
@@ -234,7 +233,6 @@ __device__ __forceinline__ void append_fp64(const DevNet<Real>& n, bool need, in
 
 template <typename Real>
 __global__ void __launch_bounds__(kBlock) k_exvol(DevNet<Real> n, int want, int trial, int force, int tile_off) {
-    pdl_trigger();  // let the extended pass / fallback kernel be scheduled
     __shared__ double sh[32];
     __shared__ int s_go, s_xb;
     __shared__ double s_lam;
@@ -379,8 +377,6 @@ struct ExtTerm {
 
 template <typename Real>
 __global__ void __launch_bounds__(128) k_exvol_ext(DevNet<Real> n, int trial, int force) {
-    pdl_wait();     // the FP32 pass filled the list
-    pdl_trigger();
     __shared__ double s_c[4][32][3];       // bead positions
     __shared__ double s_N[3][32];          // CC, GG, DD for the F term's HH
     __shared__ ExtTerm s_t[4][32];
@@ -578,7 +574,6 @@ __global__ void __launch_bounds__(128) k_exvol_ext(DevNet<Real> n, int trial, in
 constexpr int kFbEnergyBlocks = 64;
 template <typename Real>
 __global__ void __launch_bounds__(kBlock) k_exvol_energy_tail(DevNet<Real> n, int want, int tile_off) {
-    pdl_wait();
     __shared__ double sh[32];
     if ((int)blockIdx.x < kFbEnergyBlocks) {
         fb_energy_blocks(n, blockIdx.x, kFbEnergyBlocks, sh);
@@ -630,10 +625,10 @@ int launch_exvol_energy(const DevNet<Real>& n, int want, int trial, cudaStream_t
     k_exvol<Real><<<nt, kBlock, 0, s>>>(n, want, trial, 0, off);
     int k = 1;
     if constexpr (sizeof(Real) == 4) {
-        launch_pdl(k_exvol_ext<Real>, kExtBlocks, 128, s, n, trial, 0);
+        k_exvol_ext<Real><<<kExtBlocks, 128, 0, s>>>(n, trial, 0);
         ++k;
     }
-    launch_pdl(k_exvol_energy_tail<Real>, kFbEnergyBlocks + (sizeof(Real) == 4 ? nt : 0), kBlock, s, n, want, off);
+    k_exvol_energy_tail<Real><<<kFbEnergyBlocks + (sizeof(Real) == 4 ? nt : 0), kBlock, 0, s>>>(n, want, off);
     return k + 1;
 }
 
@@ -646,10 +641,10 @@ int launch_exvol_forces(const DevNet<Real>& n, int want, cudaStream_t s, bool st
     k_exvol<Real><<<nt, kBlock, 0, s>>>(n, want, 0, 1, off);
     int k = 1;
     if constexpr (sizeof(Real) == 4) {
-        launch_pdl(k_exvol_ext<Real>, kExtBlocks, 128, s, n, 0, 1);
+        k_exvol_ext<Real><<<kExtBlocks, 128, 0, s>>>(n, 0, 1);
         ++k;
     }
-    launch_pdl(k_exvol_fb_force<Real>, 4 * 152, kBlock, s, n, n.fb_moments, n.fb_tickets);
+    k_exvol_fb_force<Real><<<4 * 152, kBlock, 0, s>>>(n, n.fb_moments, n.fb_tickets);
     return k + 1;
 }
 

@@ -342,7 +342,6 @@ __global__ void __launch_bounds__(kBlock) k_body_head(DevNet<Real> n) {
 // ---------------------------------------------------------------------------
 template <typename Real>
 __global__ void __launch_bounds__(kBlock) k_fil_energy(DevNet<Real> n, int want, int trial) {
-    pdl_wait();
     __shared__ Pos<Real> xs[kFilTile + 4];
     __shared__ double sh[32 * MECH_NUM_FF];
     __shared__ int s_go, s_xb;
@@ -400,7 +399,6 @@ __global__ void __launch_bounds__(kBlock) k_fil_energy(DevNet<Real> n, int want,
 // ---------------------------------------------------------------------------
 template <typename Real>
 __global__ void __launch_bounds__(kBlock) k_fil_force(DevNet<Real> n, int want) {
-    pdl_wait();
     __shared__ Pos<Real> xs[kFilTile + 4];
     __shared__ Real fs[(kFilTile + 2) * 3];    // stretch force on the second bead
     __shared__ Real f1[(kFilTile + 2) * 3];    // bending Fr1
@@ -501,7 +499,6 @@ __device__ __forceinline__ void gather_bead(const DevNet<Real>& n, int b, int fb
 
 template <typename Real>
 __global__ void __launch_bounds__(kBlock) k_force_gather(DevNet<Real> n, int want) {
-    pdl_trigger();  // let the reduction be scheduled
     __shared__ double sh[32 * 3];
     __shared__ int s_go[kGatherTiles], s_fb[kGatherTiles];
     const int t0 = blockIdx.x * kGatherTiles;
@@ -565,7 +562,6 @@ __global__ void __launch_bounds__(kBlock) k_force_gather(DevNet<Real> n, int wan
 // bead); otherwise 4 beads strided by 64.  The tile's partials combine the
 // two warps of its 64 threads.
 __global__ void __launch_bounds__(kBlock) k_force_gather_mx(DevNet<float> n, int want) {
-    pdl_trigger();  // let the reduction be scheduled
     static_assert(kFilTile == 256 && kBlock == 64 * kGatherTiles, "64 threads x 4 beads per tile");
     __shared__ float sh[8][5];   // per warp: F.F (hi, lo), F.Fprev (hi, lo), max
     __shared__ int s_go[kGatherTiles], s_fb[kGatherTiles];
@@ -666,8 +662,6 @@ __global__ void __launch_bounds__(kBlock) k_force_gather_mx(DevNet<float> n, int
 // One block per replica: max |F|, the dots and the CG step logic after the gather.
 template <typename Real>
 __global__ void __launch_bounds__(kBlock) k_finalize_force(DevNet<Real> n, int want) {
-    pdl_wait();     // after the gather
-    pdl_trigger();  // let the direction update be scheduled
     __shared__ double sh[32 * 3];
     __shared__ int s_flag;
     const int r = blockIdx.x;
@@ -679,7 +673,6 @@ __global__ void __launch_bounds__(kBlock) k_finalize_force(DevNet<Real> n, int w
 // every kernel of the evaluation has written its partial sums.
 template <typename Real>
 __global__ void __launch_bounds__(kBlock) k_finalize_energy(DevNet<Real> n, int want, int trial) {
-    pdl_trigger();  // let the next filament kernel be scheduled
     __shared__ double sh[32 * MECH_NUM_FF];
     __shared__ int s_flag;
     const int r = blockIdx.x;
@@ -820,7 +813,6 @@ __device__ __forceinline__ bool idle_range(const DevNet<float>& n, int t0, int t
 }
 
 __global__ void __launch_bounds__(kBlock) k_fil_energy_bulk(DevNet<float> n, int want, int trial) {
-    pdl_wait();   // the previous kernel of the main lane wrote states and positions
     __shared__ EnergyStage stage[kBulkStages];
     __shared__ __align__(8) uint64_t bar[kBulkStages];
     __shared__ int4 s_desc[kBulkMaxTiles];
@@ -993,7 +985,6 @@ __device__ void issue_force_stage(const DevNet<float>& n, int4 t, ForceStage* st
 // is written to the force buffer, where k_force_gather adds the bead's sparse
 // contributions and forms the CG partials.
 __global__ void __launch_bounds__(kBlock) k_fil_force_bulk(DevNet<float> n, int want) {
-    pdl_wait();
     __shared__ ForceStage stage[kBulkStages];
     __shared__ __align__(8) uint64_t bar[kBulkStages];
     __shared__ int4 s_desc[kBulkMaxTiles];
@@ -1103,8 +1094,6 @@ __global__ void __launch_bounds__(kBlock) k_fil_force_bulk(DevNet<float> n, int 
 
 // Mixed engine: persistent direction update d = F + beta d with the d.F partials.
 __global__ void __launch_bounds__(kBlock) k_direction_mx(DevNet<float> n) {
-    pdl_wait();
-    pdl_trigger();
     __shared__ double sh[32];
     const int t0 = blockIdx.x * n.ptiles[2], t1 = min(t0 + n.ptiles[2], n.n_ftiles);
     int cur = -1, first = 0, cnt = 0, fb = 0, xb = 0, bk = 0;
@@ -1255,8 +1244,6 @@ __global__ void __launch_bounds__(kBlock) k_bond_bnd(DevNet<Real> n, int want, i
 // ---------------------------------------------------------------------------
 template <typename Real>
 __global__ void __launch_bounds__(kBlock) k_direction(DevNet<Real> n) {
-    pdl_wait();
-    pdl_trigger();
     __shared__ double sh[32];
     __shared__ int s_go, s_fb, s_xb, s_bk;
     __shared__ double s_beta;
@@ -1325,8 +1312,6 @@ __device__ void finalize_direction(const DevNet<Real>& n, int r, double* sh) {
 
 template <typename Real>
 __global__ void __launch_bounds__(kBlock) k_finalize_direction(DevNet<Real> n) {
-    pdl_wait();
-    pdl_trigger();
     __shared__ double sh[32];
     __shared__ int s_flag;
     const int r = blockIdx.x;
@@ -1339,8 +1324,6 @@ __global__ void __launch_bounds__(kBlock) k_finalize_direction(DevNet<Real> n) {
 // replica is resetting (it is in every iteration of the graph).
 template <typename Real>
 __global__ void __launch_bounds__(kBlock) k_reset(DevNet<Real> n) {
-    pdl_wait();
-    pdl_trigger();
     __shared__ int s_go[kGatherTiles], s_fb[kGatherTiles], s_flag;
     const int t0 = blockIdx.x * kGatherTiles;
     if (threadIdx.x < kGatherTiles) {
@@ -1381,8 +1364,6 @@ __global__ void __launch_bounds__(kBlock) k_reset(DevNet<Real> n) {
 
 // lambda = 0 after a line search (CGMethod.hpp:1337-1367)
 __global__ void k_dispatch_failed(CGState* st, int R, int* misc_count) {
-    pdl_wait();
-    pdl_trigger();
     const int r = blockIdx.x * blockDim.x + threadIdx.x;
     if (misc_count && r == 0) ++*misc_count;   // failure-dispatch bodies of the conditional graph
     if (r >= R) return;
@@ -1500,8 +1481,8 @@ int launch_energy(const DevNet<Real>& n, int want, int trial, const Lanes& L) {
         ++launched;
     }
     cudaEventRecord(L.join2, L.side2);
-    if constexpr (sizeof(Real) == 4) launch_pdl(k_fil_energy_bulk, n.pgrid[0], kBlock, L.main, n, want, trial);
-    else launch_pdl(k_fil_energy<Real>, n.n_ftiles, kBlock, L.main, n, want, trial);
+    if constexpr (sizeof(Real) == 4) k_fil_energy_bulk<<<n.pgrid[0], kBlock, 0, L.main>>>(n, want, trial);
+    else k_fil_energy<Real><<<n.n_ftiles, kBlock, 0, L.main>>>(n, want, trial);
     cudaStreamWaitEvent(L.main, L.join, 0);
     cudaStreamWaitEvent(L.main, L.join2, 0);
     k_finalize_energy<Real><<<n.R, kBlock, 0, L.main>>>(n, want, trial);
@@ -1523,27 +1504,27 @@ int launch_forces(const DevNet<Real>& n, int want, const Lanes& L) {
         ++launched;
     }
     cudaEventRecord(L.join2, L.side2);
-    if constexpr (sizeof(Real) == 4) launch_pdl(k_fil_force_bulk, n.pgrid[1], kBlock, L.main, n, want);
-    else launch_pdl(k_fil_force<Real>, n.n_ftiles, kBlock, L.main, n, want);
+    if constexpr (sizeof(Real) == 4) k_fil_force_bulk<<<n.pgrid[1], kBlock, 0, L.main>>>(n, want);
+    else k_fil_force<Real><<<n.n_ftiles, kBlock, 0, L.main>>>(n, want);
     cudaStreamWaitEvent(L.main, L.join, 0);
     cudaStreamWaitEvent(L.main, L.join2, 0);
     if constexpr (sizeof(Real) == 4) k_force_gather_mx<<<(n.n_ftiles + kGatherTiles - 1) / kGatherTiles, kBlock, 0, L.main>>>(n, want);
     else k_force_gather<Real><<<(n.n_ftiles + kGatherTiles - 1) / kGatherTiles, kBlock, 0, L.main>>>(n, want);
-    launch_pdl(k_finalize_force<Real>, n.R, kBlock, L.main, n, want);
+    k_finalize_force<Real><<<n.R, kBlock, 0, L.main>>>(n, want);
     return launched + 3;
 }
 
 template <typename Real>
 int launch_direction(const DevNet<Real>& n, cudaStream_t s) {
-    if constexpr (sizeof(Real) == 4) launch_pdl(k_direction_mx, n.pgrid[2], kBlock, s, n);
-    else launch_pdl(k_direction<Real>, n.n_ftiles, kBlock, s, n);
-    launch_pdl(k_finalize_direction<Real>, n.R, kBlock, s, n);
+    if constexpr (sizeof(Real) == 4) k_direction_mx<<<n.pgrid[2], kBlock, 0, s>>>(n);
+    else k_direction<Real><<<n.n_ftiles, kBlock, 0, s>>>(n);
+    k_finalize_direction<Real><<<n.R, kBlock, 0, s>>>(n);
     return 2;
 }
 
 template <typename Real>
 int launch_reset(const DevNet<Real>& n, cudaStream_t s) {
-    launch_pdl(k_reset<Real>, (n.n_ftiles + kGatherTiles - 1) / kGatherTiles, kBlock, s, n);
+    k_reset<Real><<<(n.n_ftiles + kGatherTiles - 1) / kGatherTiles, kBlock, 0, s>>>(n);
     return 1;
 }
 
@@ -1555,8 +1536,7 @@ int launch_body_head(const DevNet<Real>& n, cudaStream_t s) {
 
 template <typename Real>
 int launch_dispatch_failed(const DevNet<Real>& n, cudaStream_t s) {
-    launch_pdl(k_dispatch_failed, (n.R + 127) / 128, 128, s, n.st, n.R,
-               n.cond.on ? n.cond.counter + kCondMisc : (int*)nullptr);
+    k_dispatch_failed<<<(n.R + 127) / 128, 128, 0, s>>>(n.st, n.R, n.cond.on ? n.cond.counter + kCondMisc : nullptr);
     return 1;
 }
 

@@ -14,12 +14,10 @@
 //             contributions go to a slot buffer and every bead gathers its own
 //             slots through a CSR index, in a fixed order (no float atomics).
 //   tiles     every kernel works on tiles that never straddle replicas; each
-//             tile (or run of tiles) writes its partial sums to a fixed slot
-//             and a reduction kernel (one block per replica) reduces the slots
-//             in order, so every sum is deterministic.
+//             tile writes its partial sums to a fixed slot and the last tile of
+//             a replica (atomic ticket) reduces the slots in order, so every
+//             sum is deterministic.
 #pragma once
-
-#include <utility>
 
 #include <cuda_runtime.h>
 #include <stdint.h>
@@ -176,30 +174,6 @@ template <typename Real>
 __device__ __forceinline__ Real* slot_ptr(const DevNet<Real>& n, int slot) {
     return n.contrib + 3 * (size_t)__ldg(n.slot_pos + slot);
 }
-#endif
-
-// Programmatic dependent launch: the kernel may be scheduled while the
-// previous kernel of the stream is still running (that kernel lets it go by
-// pdl_trigger() at its start); the kernel calls pdl_wait() before it reads
-// anything the previous kernel wrote.  Both are no-ops for a plain launch.
-template <typename... KArgs, typename... Args>
-inline cudaError_t launch_pdl(void (*kernel)(KArgs...), unsigned grid, unsigned block, cudaStream_t s,
-                              Args&&... args) {
-    cudaLaunchConfig_t cfg{};
-    cfg.gridDim = dim3(grid);
-    cfg.blockDim = dim3(block);
-    cfg.dynamicSmemBytes = 0;
-    cfg.stream = s;
-    cudaLaunchAttribute attr[1];
-    attr[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
-    attr[0].val.programmaticStreamSerializationAllowed = 1;
-    cfg.attrs = attr;
-    cfg.numAttrs = 1;
-    return cudaLaunchKernelEx(&cfg, kernel, std::forward<Args>(args)...);
-}
-#ifdef __CUDACC__
-__device__ __forceinline__ void pdl_wait() { asm volatile("griddepcontrol.wait;" ::: "memory"); }
-__device__ __forceinline__ void pdl_trigger() { asm volatile("griddepcontrol.launch_dependents;" :::); }
 #endif
 
 // ---- kernels (mech_ff.cu) -------------------------------------------------
