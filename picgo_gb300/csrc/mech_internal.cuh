@@ -14,9 +14,9 @@
 //             contributions go to a slot buffer and every bead gathers its own
 //             slots through a CSR index, in a fixed order (no float atomics).
 //   tiles     every kernel works on tiles that never straddle replicas; each
-//             tile writes its partial sums to a fixed slot and the last tile of
-//             a replica (atomic ticket) reduces the slots in order, so every
-//             sum is deterministic.
+//             tile (or run of tiles) writes its partial sums to a fixed slot
+//             and a reduction kernel (one block per replica) reduces the slots
+//             in order, so every sum is deterministic.
 #pragma once
 
 #include <cuda_runtime.h>
