@@ -296,7 +296,7 @@ typedef struct MechTuning {
     int32_t energy_tiles_per_block;
     int32_t force_tiles_per_block;
     double cell_scale;              /* multiplier on the default bin edge */
-    double ms_energy, ms_force;     /* best times found (ms): a trial energy evaluation, a force evaluation */
+    double ms_energy, ms_force;     /* best filament-kernel times found (ms) */
     double ms_rebuild;              /* best rebuild wall time found (ms) */
 } MechTuning;
 int32_t mech_autotune(MechContext* ctx, int32_t flags, MechTuning* out);

@@ -1446,35 +1446,6 @@ int32_t mech_reset_coords(MechContext* ctx) {
 
 }  // extern "C"
 
-// Average device time (ms) of `fn`'s launches captured once as a CUDA graph
-// and replayed `iters` times, the way the minimizer runs them: direct launches
-// of a three-lane evaluation are bound by the host's launch rate, not by the
-// device.  The first CUDA error is kept in *err.
-template <typename Fn>
-static double graph_time(cudaStream_t s, cudaEvent_t e0, cudaEvent_t e1, int iters, Fn&& fn, cudaError_t* err) {
-    cudaGraph_t g = nullptr;
-    cudaGraphExec_t ge = nullptr;
-    cudaError_t e = cudaStreamBeginCapture(s, cudaStreamCaptureModeThreadLocal);
-    if (e == cudaSuccess) {
-        fn();
-        e = cudaStreamEndCapture(s, &g);
-    }
-    if (e == cudaSuccess) e = cudaGraphInstantiate(&ge, g, 0);
-    float ms = 0.f;
-    if (e == cudaSuccess) e = cudaGraphLaunch(ge, s);   // warm
-    if (e == cudaSuccess) {
-        cudaEventRecord(e0, s);
-        for (int i = 0; i < iters && e == cudaSuccess; ++i) e = cudaGraphLaunch(ge, s);
-        cudaEventRecord(e1, s);
-        if (e == cudaSuccess) e = cudaEventSynchronize(e1);
-        if (e == cudaSuccess) cudaEventElapsedTime(&ms, e0, e1);
-    }
-    if (ge) cudaGraphExecDestroy(ge);
-    if (g) cudaGraphDestroy(g);
-    if (e != cudaSuccess && *err == cudaSuccess) *err = e;
-    return ms / iters;
-}
-
 template <typename Real>
 static int profile_impl(MechContext* c, int iters, MechProfile* o) {
     int rc;
@@ -1487,8 +1458,33 @@ static int profile_impl(MechContext* c, int iters, MechProfile* o) {
     cudaEvent_t e0, e1;
     CU(cudaEventCreate(&e0));
     CU(cudaEventCreate(&e1));
+    // Each evaluation is captured once as a CUDA graph and replayed, the way
+    // the minimizer runs it: direct launches of a three-lane evaluation are
+    // bound by the host's launch rate, not by the device.
     cudaError_t gerr = cudaSuccess;
-    auto timeit = [&](auto&& fn) -> double { return graph_time(s, e0, e1, iters, fn, &gerr); };
+    auto timeit = [&](auto&& fn) -> double {
+        cudaGraph_t g = nullptr;
+        cudaGraphExec_t ge = nullptr;
+        cudaError_t e = cudaStreamBeginCapture(s, cudaStreamCaptureModeThreadLocal);
+        if (e == cudaSuccess) {
+            fn();
+            e = cudaStreamEndCapture(s, &g);
+        }
+        if (e == cudaSuccess) e = cudaGraphInstantiate(&ge, g, 0);
+        float ms = 0.f;
+        if (e == cudaSuccess) e = cudaGraphLaunch(ge, s);   // warm
+        if (e == cudaSuccess) {
+            cudaEventRecord(e0, s);
+            for (int i = 0; i < iters && e == cudaSuccess; ++i) e = cudaGraphLaunch(ge, s);
+            cudaEventRecord(e1, s);
+            if (e == cudaSuccess) e = cudaEventSynchronize(e1);
+            if (e == cudaSuccess) cudaEventElapsedTime(&ms, e0, e1);
+        }
+        if (ge) cudaGraphExecDestroy(ge);
+        if (g) cudaGraphDestroy(g);
+        if (e != cudaSuccess && gerr == cudaSuccess) gerr = e;
+        return ms / iters;
+    };
     o->ms_energy_eval = timeit([&] { launch_energy<Real>(n, -1, 0, c->lanes()); });
     o->ms_force_eval = timeit([&] { launch_forces<Real>(n, -1, c->lanes()); });
     o->ms_fil_energy = timeit([&] { launch_part<Real>(n, 0, s); });
@@ -1598,18 +1594,15 @@ static int autotune_impl(MechContext* c, int flags, MechTuning* out) {
                 if (cap > kFilBulkMaxTiles) continue;
                 c->tile_cap[which] = cap;
                 const DevNet<Real> n = make_devnet<Real>(c);
-                // the whole evaluation the kernel belongs to, lanes included: a
-                // line-search trial's energy, a force evaluation (the filament
-                // kernel runs beside the excluded-volume lane, so its best shape
-                // alone is not its best shape there)
-                cudaError_t gerr = cudaSuccess;
-                const double ms = graph_time(s, e0, e1, 20, [&] {
-                    if (which == 0) launch_energy<Real>(n, -1, 1, c->lanes());
-                    else launch_forces<Real>(n, -1, c->lanes());
-                }, &gerr);
-                CU(gerr);
-                if (ms < best) {
-                    best = ms;
+                launch_part<Real>(n, which, s);   // warm
+                cudaEventRecord(e0, s);
+                for (int i = 0; i < 10; ++i) launch_part<Real>(n, which, s);
+                cudaEventRecord(e1, s);
+                CU(cudaEventSynchronize(e1));
+                float ms = 0.f;
+                cudaEventElapsedTime(&ms, e0, e1);
+                if (ms / 10 < best) {
+                    best = ms / 10;
                     best_cap = cap;
                 }
             }
