@@ -285,14 +285,6 @@ __device__ __forceinline__ void warp_reduce_pair(float& s, float& e) {
         fast_two_sum(t, te, s, e);
     }
 }
-// warp sum of (h, l) pairs; the double value is formed in lane 0 only
-__device__ __forceinline__ double warp_sum_pair(FF a) {
-    float s = a.h, e = a.l;
-    warp_reduce_pair(s, e);
-    double r = 0.0;
-    if ((threadIdx.x & 31) == 0) r = (double)s + (double)e;
-    return r;
-}
 __device__ __forceinline__ float warp_max_f(float v) {
 #pragma unroll
     for (int o = 16; o > 0; o >>= 1) v = fmaxf(v, __shfl_down_sync(0xffffffffu, v, o));
@@ -346,13 +338,6 @@ __device__ __forceinline__ float2 load_pair(const double* slot) { return __ldcg(
 __device__ __forceinline__ void add_pair(FF& acc, float2 v) {
     acc.add(v.x);
     acc.add(v.y);
-}
-__device__ __forceinline__ double warp_max_lane0(float v) {
-#pragma unroll
-    for (int o = 16; o > 0; o >>= 1) v = fmaxf(v, __shfl_down_sync(0xffffffffu, v, o));
-    double r = 0.0;
-    if ((threadIdx.x & 31) == 0) r = (double)v;
-    return r;
 }
 
 // a - b as Real

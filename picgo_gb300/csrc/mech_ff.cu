@@ -470,9 +470,10 @@ __global__ void __launch_bounds__(kBlock) k_fil_force(DevNet<Real> n, int want) 
 // Every bead adds its sparse contributions (contiguous, in the CSR order) to
 // its filament force, then the CG partials: max |F|, F.F, F.Fprev per tile,
 // reduced by k_finalize_force (a per-tile completion ticket on one address
-// per replica would serialize thousands of atomics).  Each block takes
-// kGatherTiles consecutive tiles and issues the loads of all of them before
-// the per-tile reductions, so a thread keeps several beads' loads in flight.
+// per replica would serialize thousands of atomics).  FP64 engine: each block
+// takes kGatherTiles consecutive tiles and issues the loads of all of them
+// before the per-tile reductions, so a thread keeps several beads' loads in
+// flight; the mixed engine's version is k_force_gather_mx below.
 // ---------------------------------------------------------------------------
 constexpr int kGatherTiles = 4;
 
@@ -529,28 +530,13 @@ __global__ void __launch_bounds__(kBlock) k_force_gather(DevNet<Real> n, int wan
     for (int j = 0; j < kGatherTiles; ++j) {
         if (!s_go[j]) continue;   // block-uniform
         const size_t slot = 4 * (size_t)(t0 + j);
-        if constexpr (sizeof(Real) == 4) {
-            // mixed: the tile's max and compensated (hi, lo) dot sums as floats in
-            // the tile's slots 0-2: {max, F.F hi, F.F lo, F.Fprev hi, F.Fprev lo}
-            FF a[2];
-            a[0].h = ff[j];
-            a[1].h = ffp[j];
-            float m[1] = {mx[j]};
-            block_reduce_pairs<2, 1>(a, m, reinterpret_cast<float*>(sh));
-            if (threadIdx.x == 0) {
-                float* p = reinterpret_cast<float*>(n.part_fil + slot);
-                *reinterpret_cast<float4*>(p) = make_float4(m[0], a[0].h, a[0].l, a[1].h);
-                p[4] = a[1].l;
-            }
-        } else {
-            double red[3] = {warp_max_r(mx[j]), warp_sum_r(ff[j]), warp_sum_r(ffp[j])};
-            const int ops[3] = {1, 0, 0};
-            block_combine<3>(red, ops, sh);
-            if (threadIdx.x == 0) {
-                n.part_fil[slot + 0] = red[0];
-                n.part_fil[slot + 1] = red[1];
-                n.part_fil[slot + 2] = red[2];
-            }
+        double red[3] = {warp_max_r(mx[j]), warp_sum_r(ff[j]), warp_sum_r(ffp[j])};
+        const int ops[3] = {1, 0, 0};
+        block_combine<3>(red, ops, sh);
+        if (threadIdx.x == 0) {
+            n.part_fil[slot + 0] = red[0];
+            n.part_fil[slot + 1] = red[1];
+            n.part_fil[slot + 2] = red[2];
         }
     }
 }
