@@ -117,6 +117,21 @@ class Clocks:
                 "samples": len(sm)}
 
 
+def combine_ranks(dist, total_ms: float, force_calls: int, device="cpu"):
+    """Whole-job figures over the ranks of a replicas-only run: the slowest
+    rank's timed milliseconds and the force evaluations of every rank (one
+    replica per rank, no data-path collective).  Identity without a process
+    group."""
+    if dist is None:
+        return total_ms, force_calls
+    import torch
+    t = torch.tensor([total_ms], dtype=torch.float64, device=device)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    c = torch.tensor([float(force_calls)], dtype=torch.float64, device=device)
+    dist.all_reduce(c)
+    return float(t.item()), int(round(c.item()))
+
+
 def flush_l2(torch, dev):
     buf = torch.empty(64 * 1024 * 1024, dtype=torch.float32, device=dev)   # 256 MB > 129 MB L2
     buf.zero_()
@@ -168,12 +183,8 @@ def run_ours(args, rank, world, dist):
             launches += eng.timing()["launches"]
         barrier()
     clocks = clk.summary()
-    total_ms = sum(step_ms)
-    if dist is not None:
-        t = torch.tensor([total_ms], device=dev)
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        total_ms = float(t.item())
     force_calls = sum(r["num_force_call"] for r in results)
+    total_ms, force_calls_all = combine_ranks(dist, sum(step_ms), force_calls, dev)
     value_local = force_calls / (total_ms / 1e3)
     ms_per_step = total_ms / args.steps
 
@@ -252,9 +263,7 @@ def run_ours(args, rank, world, dist):
         "roofline": roofline,
     }
     if dist is not None:
-        t = torch.tensor([force_calls], dtype=torch.float64, device=dev)
-        dist.all_reduce(t)
-        out["value"] = float(t.item()) / (total_ms / 1e3)
+        out["value"] = force_calls_all / (total_ms / 1e3)
     out["value"] = round(out["value"], 2)
     return out, net
 
