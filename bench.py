@@ -496,6 +496,41 @@ def run_reference(args, rank, world):
             "e2e": {"value": round(v, 4), "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
 
 
+def probe(args):
+    """A bounded piece of the minimization for profiler captures and quick timings.
+
+    Default: neighbor-list rebuild + Polak-Ribiere CG from the seeded start until
+    `--energy-calls` energy calls (every kernel of real CG iterations);
+    `--evals N`: each evaluation kernel launched N times through mech_profile;
+    `--forces N` / `--energies N`: only that many mech_forces / mech_energy calls,
+    so that a profiler's first matching launches are those of one evaluation kind.
+    Prints one JSON line.
+    """
+    from picgo_gb300 import Engine, make_network
+    net = make_network(args.workload, seed=args.seed)
+    out = {"probe": args.workload, "precision": args.precision, "n_beads": net.n_beads}
+    with Engine(args.precision) as eng:
+        eng.set_network(net)
+        if args.autotune:
+            out["tuning"] = eng.autotune()
+        out["lists"] = eng.rebuild()
+        if args.forces > 0 or args.energies > 0:
+            for _ in range(args.forces):
+                eng.forces()
+            for _ in range(args.energies):
+                eng.energies()
+            out["calls"] = {"forces": args.forces, "energies": args.energies}
+        elif args.evals > 0:
+            out["profile"] = eng.profile(args.evals)
+        else:
+            t0 = time.perf_counter()
+            r = eng.minimize(cg(energy_call_limit=args.energy_calls))[0]
+            out["seconds"] = round(time.perf_counter() - t0, 4)
+            out.update({k: r[k] for k in ("num_iter", "num_force_call", "num_energy_eval", "grad_inf_norm",
+                                          "status")})
+    print(json.dumps(out))
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -511,7 +546,19 @@ def main():
                     help="only run the implicit-adjoint check on P parameters of the 2,000 x 30 network")
     ap.add_argument("--c4", type=int, default=0, metavar="R",
                     help="only run the batched-ensemble comparison on R replicas and print its JSON line")
+    ap.add_argument("--probe", action="store_true",
+                    help="profiler probe: a bounded minimization (or single evaluations) of --workload, one JSON line")
+    ap.add_argument("--workload", default="c2", help="probe: network config name (c1, c2, c5)")
+    ap.add_argument("--seed", type=int, default=None, help="probe: network seed (default: the config's)")
+    ap.add_argument("--energy-calls", type=int, default=40, help="probe: energy calls of the bounded minimization")
+    ap.add_argument("--evals", type=int, default=0, help="probe: launches per evaluation kernel (mech_profile)")
+    ap.add_argument("--forces", type=int, default=0, help="probe: only this many mech_forces calls")
+    ap.add_argument("--energies", type=int, default=0, help="probe: only this many mech_energy calls")
+    ap.add_argument("--autotune", action="store_true", help="probe: run the autotuner first")
     args = ap.parse_args()
+    if args.probe:
+        probe(args)
+        return
     world = int(os.environ.get("WORLD_SIZE", "1"))
     rank = int(os.environ.get("RANK", "0"))
     dist = None

@@ -373,8 +373,10 @@ int32_t mech_newton_refine(MechContext* ctx, int32_t max_steps, double force_tol
  * scratch is a fixed 131,328-byte device array inside the library.
  *
  * Inputs (device pointers, current device): fil_cyl_start[n_filaments+1]
- * ascending cylinder ranges from 0 to n_cylinders (not checked: the arrays
- * are on the device); coord[3 * (n_cylinders + n_filaments)] with the
+ * strictly ascending cylinder ranges from 0 to n_cylinders: every filament
+ * holds at least one cylinder, as every MEDYAN filament does (not checked:
+ * the arrays are on the device; an empty filament shifts the beads of every
+ * later filament and gives wrong energies); coord[3 * (n_cylinders + n_filaments)] with the
  * beads filament by filament, minus end first (cylinder c of filament f joins
  * beads c + f and c + f + 1); per-cylinder k_stretch, eq_length, k_bend,
  * eq_theta (the bending triple ending in cylinder c uses c's constants).
@@ -382,8 +384,10 @@ int32_t mech_newton_refine(MechContext* ctx, int32_t max_steps, double force_tol
  * cudaStream_t; NULL = legacy default stream); synchronize before reading.
  *
  * Limits: n_cylinders <= 2,097,152, else MECH_ERR_CAPACITY and nothing runs.
- * The first call on each device looks up the scratch address: make it before
- * any stream capture on that device.  The scratch's completion ticket must be
+ * The first call in each CUDA context of a device looks up the scratch
+ * address (again after a cudaDeviceReset or any other re-creation of the
+ * context, since the array can move): make that call before any stream
+ * capture on that device.  The scratch's completion ticket must be
  * zero at launch: the call clears it on `stream` and the kernel leaves it
  * zero.  Calls that overlap in time on one device share the scratch and
  * race: issue them on one stream or order them.

@@ -98,20 +98,50 @@ k_fil_energy_static(const double* __restrict__ x, const int32_t* __restrict__ fc
     }
 }
 
+// The scratch address belongs to the module loaded into one CUDA context: a
+// context that is destroyed and re-created (cudaDeviceReset, a primary
+// context released by every user) reloads the module and the array can move.
+// So the address is cached per (device, current context) and looked up again
+// whenever the current context of that device changes.  The context handle
+// comes from the driver's cuCtxGetCurrent, reached through the runtime's
+// entry-point query so that the library needs no link against libcuda.
+using CtxGetCurrentFn = int (*)(void**);   // CUresult cuCtxGetCurrent(CUcontext*)
+
 static std::mutex g_static_mu;
 static void* g_static_ptr[kStaticMaxDevices];
+static void* g_static_ctx[kStaticMaxDevices];
+static CtxGetCurrentFn g_ctx_get_current = nullptr;
+static bool g_ctx_query_done = false;
 
-// Device address of the scratch array on the current device, looked up once
-// per device.
+static void* current_context() {
+    if (!g_ctx_query_done) {
+        g_ctx_query_done = true;
+        void* fn = nullptr;
+        cudaDriverEntryPointQueryResult q = cudaDriverEntryPointSymbolNotFound;
+        if (cudaGetDriverEntryPointByVersion("cuCtxGetCurrent", &fn, 12000, cudaEnableDefault, &q) == cudaSuccess &&
+            q == cudaDriverEntryPointSuccess)
+            g_ctx_get_current = reinterpret_cast<CtxGetCurrentFn>(fn);
+        else
+            cudaGetLastError();
+    }
+    void* ctx = nullptr;
+    if (!g_ctx_get_current || g_ctx_get_current(&ctx) != 0) return nullptr;
+    return ctx;
+}
+
+// Device address of the scratch array in the current context of device
+// `dev` (which must be current), looked up at the first call in that context.
 static int static_scratch(int dev, unsigned char** out) {
     if (dev < 0 || dev >= kStaticMaxDevices) return set_error_text(MECH_ERR_ARG, "device ordinal out of range");
     std::lock_guard<std::mutex> lk(g_static_mu);
-    if (!g_static_ptr[dev]) {
+    void* ctx = current_context();
+    if (!g_static_ptr[dev] || !ctx || ctx != g_static_ctx[dev]) {
         void* p = nullptr;
         const cudaError_t e = cudaGetSymbolAddress(&p, g_static_scratch);
         if (e != cudaSuccess || !p)
             return set_error_text(MECH_ERR_CUDA, std::string("cudaGetSymbolAddress(scratch): ") + cudaGetErrorString(e));
         g_static_ptr[dev] = p;
+        g_static_ctx[dev] = current_context();   // the lookup itself makes the primary context current
     }
     *out = static_cast<unsigned char*>(g_static_ptr[dev]);
     return MECH_OK;

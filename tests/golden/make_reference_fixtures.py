@@ -3,8 +3,10 @@
 The reference (MEDYAN 5.4.0 inside whwh13/picgo) cannot be compiled here, so
 its Catch2 cases that pin this path are re-run against the oracle and the GPU
 path from the inputs they hold.  This script reads those test sources as text
-and writes the numbers (coordinates, bead sets, constants, CG problem) to a
-small JSON fixture, so the tests need no access to the reference tree:
+and returns the numbers (coordinates, bead sets, constants, CG problem).  The
+tests call extract() at run time and skip where the reference tree is absent:
+the reference's licence bars redistributing its material, so the values are
+not committed.  The cases:
 
 * Mechanics/ForceField/Volume/TestCylinderExclVolume.cpp:13-47   (split-segment scaling)
 * Mechanics/ForceField/Volume/TestCylinderExclVolume.cpp:49-101  (integral vs monomer energy)
@@ -12,7 +14,7 @@ small JSON fixture, so the tests need no access to the reference tree:
 * Mechanics/ForceField/Boundary/TestBoundaryBeadRepulsion.cpp:13-96
 * Mechanics/Minimizer/TestCGMethod.cpp:9-93
 
-Usage:  python tests/golden/make_reference_fixtures.py [reference_root]
+Usage:  python tests/golden/make_reference_fixtures.py [reference_root [out.json]]  (a local copy for inspection)
 """
 from __future__ import annotations
 
@@ -142,13 +144,21 @@ def cg_case(root):
                 methods=["steepest", "fletcherRieves", "polakRibiere"])
 
 
+def extract(root: str = DEFAULT_ROOT) -> dict:
+    """The inputs of the reference's unit cases, read from its test sources under ``root``."""
+    return dict(source="whwh13/picgo medyan-5.4.0 Catch2 cases", exvol=exvol_cases(root),
+                boundary=boundary_case(root), cg=cg_case(root))
+
+
+def available(root: str = DEFAULT_ROOT) -> bool:
+    return os.path.isdir(os.path.join(root, TESTS))
+
+
 def main(argv):
     root = argv[1] if len(argv) > 1 else DEFAULT_ROOT
-    out = dict(source="whwh13/picgo medyan-5.4.0 Catch2 cases", exvol=exvol_cases(root),
-               boundary=boundary_case(root), cg=cg_case(root))
-    path = os.path.join(HERE, "reference_cases.json")
+    path = argv[2] if len(argv) > 2 else os.path.join(HERE, "reference_cases.json")
     with open(path, "w") as fh:
-        json.dump(out, fh, indent=1)
+        json.dump(extract(root), fh, indent=1)
     print("wrote", path)
 
 

@@ -1,8 +1,8 @@
 """The oracle pinned against the reference's own unit cases and known answers.
 
 The reference (MEDYAN 5.4.0) cannot be built here; its Catch2 cases for this
-path are re-run on the oracle from the inputs in tests/golden/reference_cases.json
-(extracted by tests/golden/make_reference_fixtures.py):
+path are re-run on the oracle from the inputs in the reference's test sources,
+read at test time by tests/golden/make_reference_fixtures.py:
 
 * TestCylinderExclVolume.cpp:13-47, :49-101, :103-244
 * TestBoundaryBeadRepulsion.cpp:13-96
@@ -221,15 +221,55 @@ def test_forcefield_gradients_match_finite_differences(ff):
         assert abs(de - ex) <= 1e-6 * abs(ex) + 1e-12, (ff, de, ex)
 
 
+def _fd_force(coord, bs, k, ln, h=1e-6):
+    """-dE/dx by central differences of the oracle's pair energy."""
+    g = np.zeros_like(coord)
+    for i in range(coord.size):
+        cp, cm = coord.copy(), coord.copy()
+        cp[i] += h
+        cm[i] -= h
+        g[i] = -(_exvol_E(cp, bs, k, ln) - _exvol_E(cm, bs, k, ln)) / (2 * h)
+    return g
+
+
+def _moved_c2(c):
+    """c with bead 2 moved 0.01 nm along unit((c2 - c1) x (c3 - c1)): the reference's
+    movePointOutOfPlane for a pair judged coplanar (MathFunctions.h:1221-1273,
+    CylinderExclVolRepulsion.cpp:610-626)."""
+    p = c.reshape(4, 3)
+    n = np.cross(p[1] - p[0], p[2] - p[0])
+    q = p.copy()
+    q[1] = p[1] + n / np.linalg.norm(n) * 0.01
+    return q.reshape(-1)
+
+
 def test_exvol_force_nudge_only_in_force_path():
-    """Near-coplanar pairs: forces are taken with c2 moved 0.01 nm off the plane, energies are not."""
-    c = np.array([0, 0, 0, 10, 0, 0, 3, 5, 0.1, 4, -5, 0.1], dtype=np.float64)
-    e = _exvol_E(c, [0, 3, 6, 9], [1.0], [10.0, 10.0])
-    f = _exvol_F(c, [0, 3, 6, 9], [1.0], [10.0, 10.0])
-    assert np.isfinite(e) and np.all(np.isfinite(f))
-    c2 = c.copy()
-    c2[[2, 5, 8, 11]] += 1.0  # far from coplanar along z? no: translate; still coplanar-ish
-    assert math.isclose(_exvol_E(c2, [0, 3, 6, 9], [1.0], [10.0, 10.0]), e, rel_tol=1e-9)
+    """A pair judged coplanar (|cos| < 0.1): its forces are those of the pair with c2
+    moved 0.01 nm off the plane, its energy is that of the pair as given; a pair far
+    from coplanar gets the plain gradient."""
+    bs, k, ln = [0, 3, 6, 9], [1.0], [10.0, 10.0]
+    # a 10 nm segment and a 2.8 nm one 1-3 nm from it, tilted by ~0.1 deg out of a common plane
+    c = np.array([0, 0, 0, 10, 0, 0, 3, 3, 0.002, 5, 1, -0.002], dtype=np.float64)
+    f = _exvol_F(c, bs, k, ln)
+    # h = 3e-4 nm balances the truncation error against the round-off of the
+    # energy, which is ill-conditioned this close to coplanar (FD error ~3e-7)
+    g_here = _fd_force(c, bs, k, ln, 3e-4)
+    g_moved = _fd_force(_moved_c2(c), bs, k, ln, 3e-4)
+    scale = np.abs(f).max()
+    assert np.abs(f - g_moved).max() <= 2e-6 * scale, (f, g_moved)
+    assert np.abs(f - g_here).max() >= 1e-3 * scale, (f, g_here)    # the move is visible in the forces
+    # the energy path does not move: E(c) differs from E(moved) and is smooth through c
+    e = _exvol_E(c, bs, k, ln)
+    assert abs(e - _exvol_E(_moved_c2(c), bs, k, ln)) >= 1e-6 * abs(e)
+    dz = np.zeros_like(c)
+    dz[5] = 1e-4
+    mid = 0.5 * (_exvol_E(c + dz, bs, k, ln) + _exvol_E(c - dz, bs, k, ln))
+    assert abs(mid - e) <= 1e-7 * abs(e)
+    # far from coplanar (|cos| ~ 0.7): forces are the plain gradient
+    c3 = np.array([0, 0, 0, 10, 0, 0, 3, 3, 2.0, 5, -3, -3.0], dtype=np.float64)
+    f3 = _exvol_F(c3, bs, k, ln)
+    g3 = _fd_force(c3, bs, k, ln, 3e-4)
+    assert np.abs(f3 - g3).max() <= 1e-6 * np.abs(f3).max(), (f3, g3)
 
 
 # --------------------------------------------------------------------------- neighbor lists
