@@ -187,6 +187,45 @@ int32_t mech_rebuild_neighbors(MechContext* ctx, double cell_size, MechListInfo*
 int32_t mech_get_pairs(MechContext* ctx, int32_t replica, int32_t* pairs, int64_t cap, int64_t* count);
 
 /*
+ * The BoundaryCylinderNL of replica r built by the last rebuild
+ * (Structure/NeighborListImpl.cpp:801-809): for each plane in order, the
+ * cylinders whose midpoint lies closer than BoundaryCutoff, ascending, as
+ * (plane, cylinder) pairs.  Writes min(cap, count) pairs; *count receives the
+ * total.
+ */
+int32_t mech_get_boundary_list(MechContext* ctx, int32_t replica, int32_t* entries, int64_t cap, int64_t* count);
+
+/*
+ * Boundary load forces on the filament ends of replica r at its current
+ * coordinates, with the boundary list of the last rebuild: what
+ * ForceFieldManager::computeLoadForces (ForceFieldManager.cpp:292-311) leaves
+ * in Bead::loadForcesP / loadForcesM after a minimization
+ * (MController::afterMinimization_, Controller/MController.h:240-268) for the
+ * chemistry's polymerization rate changers.  For each plane in order and each
+ * listed cylinder, a plus-end cylinder loads its second bead and a minus-end
+ * cylinder its first (BoundaryCylinderRepulsion.cpp:122-192): monomer i at
+ * bd + i * mon_size * dir, dir the unit vector from the other bead, gets
+ * max(-n . dir, 0) * K exp(-dist / lambda) / lambda
+ * (BoundaryCylinderRepulsionExp.cpp:113-118).  mon_size[t] and n_mon[t]
+ * (SysParams::Geometry().monomerSize, cylinderNumMon) are given per filament
+ * type t < n_types.  plus / minus: [n_filaments * stride] doubles, filament f's
+ * monomers at f * stride; entries with i >= n_mon of the filament's type are 0.
+ */
+int32_t mech_load_forces(MechContext* ctx, int32_t replica, int32_t n_types, const double* mon_size,
+                         const int32_t* n_mon, int32_t stride, double* plus, double* minus);
+
+/*
+ * Diagnostic: the filament energy terms of replica r at its current
+ * coordinates as the engine computes them before summing (FP32 terms in a
+ * mixed context, FP64 in an FP64 one), per cylinder in the caller's order:
+ * stretch[c] its stretching energy, bend[c] the bending energy of the triple
+ * ending in it (0 for a filament's first cylinder).  Summing these exactly
+ * and comparing with mech_energy separates the engine's accumulation error
+ * from the error of its terms.  No reference counterpart.
+ */
+int32_t mech_energy_terms(MechContext* ctx, int32_t replica, double* stretch, double* bend);
+
+/*
  * ForceFieldManager::computeIndividualEnergies and ::computeEnergy
  * (ForceFieldManager.cpp:96-227) at `coord` (NULL: current coordinates).
  * per_ff receives MECH_NUM_FF energies; *total the plain sum and *energy the
@@ -298,6 +337,9 @@ typedef struct MechTuning {
     double cell_scale;              /* multiplier on the default bin edge */
     double ms_energy, ms_force;     /* best filament-kernel times found (ms) */
     double ms_rebuild;              /* best rebuild wall time found (ms) */
+    int32_t energy_blocks_per_sm;   /* resident blocks per SM of the persistent filament energy kernel */
+    int32_t force_blocks_per_sm;    /* and of the filament force kernel (0: as many as fit); fewer leave SM
+                                       room for the excluded-volume and linker lanes running beside them */
 } MechTuning;
 int32_t mech_autotune(MechContext* ctx, int32_t flags, MechTuning* out);
 int32_t mech_set_tuning(MechContext* ctx, const MechTuning* t);

@@ -7,5 +7,5 @@ and by ``bench.py``'s CPU-baseline leg, as the checker.  The product library
 from .oracle import (  # noqa: F401
     FF_NAMES, CGParams, CGResult, System, Vectorized, build, lib, vectorize, energy, energies, forces,
     cyl_pairs, cyl_pairs_fast, boundary_list, minimize, minimize_quadratic, cg_params, force_scale,
-    series_atan_mode, threads,
+    series_atan_mode, threads, stretch_forces, load_forces,
 )

@@ -722,6 +722,71 @@ int64_t orc_boundary_list(int ncyl, const double* coord, const int* b1, const in
 }
 
 // ---------------------------------------------------------------------------
+// Boundary load forces on filament ends after a minimization
+// (ForceFieldManager::computeLoadForces, ForceFieldManager.cpp:292-311;
+// BoundaryCylinderRepulsion<Exp>::computeLoadForces and its helper,
+// BoundaryCylinderRepulsion.cpp:122-192; the Exp load force,
+// BoundaryCylinderRepulsionExp.cpp:113-118).  Every filament end bead starts
+// at zero; then for each plane in order and each cylinder of its boundary
+// list in order: a plus-end cylinder loads its second bead (polymerizing away
+// from its first), a minus-end cylinder its first bead (away from its second).
+// For monomer i of the end, at x_i = bd + (i * monSize) * dir with
+// dir = (bd - bo) / |bd - bo|:
+//   load[i] += max(-(n . dir), 0) * K exp(-dist(x_i) / lambda) / lambda
+// with n = (a, b, c) of the plane as stored (PlaneBoundaryElement::normal,
+// BoundaryElementImpl.h:99-105) and dist its signed distance.  Output per
+// filament f: plus[f * stride + i], minus[f * stride + i], i < n_mon of the
+// filament's type (entries beyond stay zero).
+// ---------------------------------------------------------------------------
+static void load_force_end(const double* bo, const double* bd, const double* pl, double K, double lam, double mon,
+                           int nmon, double* load) {
+    double dir[3] = {bd[0] - bo[0], bd[1] - bo[1], bd[2] - bo[2]};
+    double m2 = 0.0;
+    for (int k = 0; k < 3; ++k) m2 += dir[k] * dir[k];
+    const double norm = std::sqrt(m2);
+    for (int k = 0; k < 3; ++k) dir[k] /= norm;
+    double dn = 0.0;
+    for (int k = 0; k < 3; ++k) dn += pl[k] * dir[k];
+    const double proj = std::max(-dn, 0.0);
+    for (int i = 0; i < nmon; ++i) {
+        const double step = i * mon;
+        const double x[3] = {bd[0] + step * dir[0], bd[1] + step * dir[1], bd[2] + step * dir[2]};
+        const double R = -plane_distance(pl, x) / lam;
+        const double f = K * std::exp(R) / lam;
+        load[i] += proj * f;
+    }
+}
+
+int orc_boundary_load_forces(int nfil, const int* fil_cyl_start, const int* b1, const int* b2, const int* cyl_type,
+                             const double* coord, int nplanes, const double* planes, const double* plane_k,
+                             const double* plane_slen, const int* nn, const int32_t* list, const double* mon_size,
+                             const int* n_mon, int stride, double* plus, double* minus) {
+    const int ncyl = fil_cyl_start[nfil];
+    std::vector<int> fil(ncyl);
+    for (int f = 0; f < nfil; ++f)
+        for (int c = fil_cyl_start[f]; c < fil_cyl_start[f + 1]; ++c) fil[c] = f;
+    std::fill(plus, plus + (size_t)nfil * stride, 0.0);
+    std::fill(minus, minus + (size_t)nfil * stride, 0.0);
+    int off = 0;
+    for (int p = 0; p < nplanes; ++p) {
+        for (int j = 0; j < nn[p]; ++j) {
+            const int c = list[off + j];
+            const int f = fil[c];
+            const int t = cyl_type[c];
+            const int nm = std::min(n_mon[t], stride);
+            if (c == fil_cyl_start[f + 1] - 1)
+                load_force_end(coord + 3 * b1[c], coord + 3 * b2[c], planes + 4 * p, plane_k[p], plane_slen[p],
+                               mon_size[t], nm, plus + (size_t)f * stride);
+            if (c == fil_cyl_start[f])
+                load_force_end(coord + 3 * b2[c], coord + 3 * b1[c], planes + 4 * p, plane_k[p], plane_slen[p],
+                               mon_size[t], nm, minus + (size_t)f * stride);
+        }
+        off += nn[p];
+    }
+    return 0;
+}
+
+// ---------------------------------------------------------------------------
 // Force-field manager (ForceFieldManager.cpp:96-290) over the six configured
 // force fields in MController's order (MController.cpp:65-196).
 // ---------------------------------------------------------------------------

@@ -120,6 +120,9 @@ def lib():
             L.orc_series_atan.argtypes = [C.c_double]
             L.orc_system_force_scale.argtypes = [C.POINTER(System), _dp, _dp, C.c_int]
             L.orc_set_threads.argtypes = [C.c_int]
+            L.orc_boundary_load_forces.restype = C.c_int
+            L.orc_boundary_load_forces.argtypes = [C.c_int, _ip, _ip, _ip, _ip, _dp, C.c_int, _dp, _dp, _dp, _ip,
+                                                   _i32p, _dp, _ip, C.c_int, _dp, _dp]
             L.orc_get_threads.restype = C.c_int
             _lib = L
     return _lib
@@ -324,6 +327,45 @@ def forces(vec: Vectorized, coord: np.ndarray) -> np.ndarray:
     f = np.zeros_like(x)
     lib().orc_system_forces(C.byref(vec.system), _p(x), _p(f), x.size, None, None)
     return f.reshape(-1, 3)
+
+
+def stretch_forces(vec: Vectorized, coord: np.ndarray):
+    """Per-linker and per-motor stretch force of the force routine
+    (LinkerStretching::assignforcemags, LinkerStretching.cpp:117-123; motors alike)."""
+    x = np.ascontiguousarray(coord, dtype=np.float64).reshape(-1)
+    f = np.zeros_like(x)
+    lk = np.zeros(max(1, vec.system.n_linker))
+    mt = np.zeros(max(1, vec.system.n_motor))
+    lib().orc_system_forces(C.byref(vec.system), _p(x), _p(f), x.size, _p(lk), _p(mt))
+    return lk[:vec.system.n_linker], mt[:vec.system.n_motor]
+
+
+def load_forces(net, coord=None, bnd=None, mon_size=(2.7,), n_mon=(40,)):
+    """Boundary load forces on filament ends, (plus, minus) each [n_filaments, max n_mon]
+    (ForceFieldManager.cpp:292-311, BoundaryCylinderRepulsion.cpp:122-192)."""
+    coord = np.ascontiguousarray(net.coord if coord is None else coord, dtype=np.float64)
+    if bnd is None:
+        bnd = boundary_list(net, coord)
+    bcyl, bnn = bnd
+    ms = np.ascontiguousarray(mon_size, dtype=np.float64)
+    nm = np.ascontiguousarray(n_mon, dtype=np.int32)
+    stride = int(nm.max())
+    nfil = int(net.n_filaments)
+    plus = np.zeros((nfil, stride))
+    minus = np.zeros((nfil, stride))
+    fcs = np.ascontiguousarray(net.fil_cyl_start, dtype=np.int32)
+    b1 = np.ascontiguousarray(net.cyl_b1, dtype=np.int32)
+    b2 = np.ascontiguousarray(net.cyl_b2, dtype=np.int32)
+    ty = np.ascontiguousarray(net.cyl_type, dtype=np.int32)
+    planes = np.ascontiguousarray(net.planes, dtype=np.float64)
+    pk = np.ascontiguousarray(net.plane_k, dtype=np.float64)
+    ps = np.ascontiguousarray(net.plane_slen, dtype=np.float64)
+    nn = np.ascontiguousarray(bnn, dtype=np.int32)
+    lst = np.ascontiguousarray(bcyl, dtype=np.int32)
+    lib().orc_boundary_load_forces(nfil, _p(fcs, _ip), _p(b1, _ip), _p(b2, _ip), _p(ty, _ip), _p(coord),
+                                   planes.shape[0], _p(planes), _p(pk), _p(ps), _p(nn, _ip), _p(lst, _i32p),
+                                   _p(ms), _p(nm, _ip), stride, _p(plus), _p(minus))
+    return plus, minus
 
 
 def force_scale(vec: Vectorized, coord: np.ndarray) -> np.ndarray:

@@ -33,7 +33,8 @@ EXPORTS = [
     "mech_set_coords", "mech_get_coords", "mech_rebuild_neighbors", "mech_get_pairs", "mech_energy",
     "mech_forces", "mech_minimize", "mech_get_forces", "mech_get_stretch_forces", "mech_get_timing",
     "mech_reset_coords", "mech_profile", "mech_filament_energy_device", "mech_hvp", "mech_set_linker_params",
-    "mech_adjoint", "mech_newton_refine", "mech_autotune", "mech_set_tuning", "mech_set_graph_mode",
+    "mech_adjoint", "mech_newton_refine", "mech_autotune", "mech_set_tuning", "mech_set_graph_mode", "mech_get_boundary_list",
+    "mech_load_forces", "mech_energy_terms",
 ]
 
 
@@ -114,7 +115,8 @@ class MechSolveInfo(C.Structure):
 class MechTuning(C.Structure):
     _fields_ = [("energy_tiles_per_block", C.c_int32), ("force_tiles_per_block", C.c_int32),
                 ("cell_scale", C.c_double), ("ms_energy", C.c_double), ("ms_force", C.c_double),
-                ("ms_rebuild", C.c_double)]
+                ("ms_rebuild", C.c_double), ("energy_blocks_per_sm", C.c_int32),
+                ("force_blocks_per_sm", C.c_int32)]
 
 
 _lock = threading.Lock()
@@ -149,6 +151,9 @@ def load(build_if_missing: bool = False):
         L.mech_get_coords.argtypes = [vp, C.c_int32, _dp]
         L.mech_rebuild_neighbors.argtypes = [vp, C.c_double, C.POINTER(MechListInfo)]
         L.mech_get_pairs.argtypes = [vp, C.c_int32, _i32p, C.c_int64, _i64p]
+        L.mech_get_boundary_list.argtypes = [vp, C.c_int32, _i32p, C.c_int64, _i64p]
+        L.mech_energy_terms.argtypes = [vp, C.c_int32, _dp, _dp]
+        L.mech_load_forces.argtypes = [vp, C.c_int32, C.c_int32, _dp, _i32p, C.c_int32, _dp, _dp]
         L.mech_energy.argtypes = [vp, C.c_int32, _dp, _dp, _dp, _dp]
         L.mech_forces.argtypes = [vp, C.c_int32, _dp, _dp]
         L.mech_minimize.argtypes = [vp, C.POINTER(MechCGParams), C.POINTER(MechResult)]

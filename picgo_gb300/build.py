@@ -2,6 +2,11 @@
 
 Translation units are compiled in parallel; the FP64 excluded-volume object
 is compiled without FMA contraction (see mech_exvol.cu).
+
+With MECH_TRACE=1 in the environment, a diagnostic variant is built into (and
+loaded from) _lib_trace/ instead: every kernel block appends a (start, end,
+kernel, block) record to a timeline that mech_minimize writes to the file
+named by MECH_TRACE_FILE.
 """
 from __future__ import annotations
 
@@ -12,7 +17,8 @@ import subprocess
 
 HERE = os.path.dirname(os.path.abspath(__file__))
 CSRC = os.path.join(HERE, "csrc")
-OUTDIR = os.path.join(HERE, "_lib")
+TRACE = bool(os.environ.get("MECH_TRACE"))
+OUTDIR = os.path.join(HERE, "_lib_trace" if TRACE else "_lib")
 LIBNAME = "libmedyan_mech.so"
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 COMMON = ["-O3", "-std=c++17", "-lineinfo", "-Xcompiler", "-fPIC", "-Xcompiler", "-O2",
@@ -58,7 +64,7 @@ def build(verbose: bool = False, force: bool = False, ptxas_info: bool = False) 
         s = os.path.join(CSRC, src)
         o = os.path.join(OUTDIR, obj)
         if force or ptxas_info or _stale(o, [s] + headers):
-            cmd = [nv, *ARCH, *COMMON, *extra, "-c", s, "-o", o]
+            cmd = [nv, *ARCH, *COMMON, *extra, *(["-DMECH_TRACE"] if TRACE else []), "-c", s, "-o", o]
             if ptxas_info:
                 cmd += ["-Xptxas", "-v"]
             jobs.append(cmd)

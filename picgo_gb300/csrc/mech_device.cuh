@@ -143,8 +143,9 @@ __device__ __forceinline__ void begin_iteration(CGState& S) {
     S.phase = PH_LS_TRIAL;
 }
 
-// One backtracking step after the trial energy E (CGMethod.hpp:296-361).
-__device__ __forceinline__ void line_search_step(CGState& S, double E) {
+// One backtracking step after the trial energy E (CGMethod.hpp:296-361);
+// `trial_buf` is the position buffer holding that trial's coordinates.
+__device__ __forceinline__ void line_search_step(CGState& S, double E, int trial_buf) {
     S.numEnergyCall++;
     S.numTrials++;
     double lambda = S.lambda;
@@ -172,7 +173,7 @@ __device__ __forceinline__ void line_search_step(CGState& S, double E) {
     }
     S.newEnergy = Elam;
     S.E0 = Elam;                       // energy at the moved coordinates
-    S.xbuf ^= 1;                       // the trial buffer becomes current
+    S.xbuf = trial_buf;                // the trial buffer becomes current
     S.phase = PH_FORCE;
 }
 

@@ -119,6 +119,7 @@ __device__ void fb_energy_blocks(const DevNet<Real>& n, int blk, int nblk, doubl
 // numeric forces: partial moments of (entry, chunk), combined by the last chunk
 template <typename Real>
 __global__ void __launch_bounds__(kBlock) k_exvol_fb_force(DevNet<Real> n, double* moments, int* tickets) {
+    MECH_TRACE_KERNEL(n, TK_EXVOL_FB_FORCE);
     __shared__ double sh[32];
     __shared__ int s_last;
     const int cnt = min(*n.ev_fb_count, kExvolFallbackCap);
@@ -222,7 +223,7 @@ __device__ __forceinline__ void append_fp64(const DevNet<Real>& n, bool need, in
     base = __shfl_sync(0xffffffffu, base, leader);
     if (need) {
         const int k = base + __popc(m & ((1u << lane) - 1u));
-        if (k < n.n_ev) {
+        if (k < 2 * n.n_ev) {   // room for both trials of a two-trial pass
             n.ev_list[2 * k] = r;
             n.ev_list[2 * k + 1] = pr;
         } else {
@@ -231,8 +232,37 @@ __device__ __forceinline__ void append_fp64(const DevNet<Real>& n, bool need, in
     }
 }
 
+// Mixed engine: the energy of one pair in single precision, or need64 when the
+// pair is ill-conditioned (normalized triple product under kMixedTauEnergy) or
+// the formula gives no number; such pairs go to the extended pass.
+__device__ __forceinline__ float mixed_pair_energy(const Pos<float>& p1, const Pos<float>& p2, const Pos<float>& p3,
+                                                   const Pos<float>& p4, float kRep, bool& need64) {
+    float v12[3], v34[3], v31[3], v14[3], v32[3], v24[3];
+    pdiff(p2, p1, v12);
+    pdiff(p4, p3, v34);
+    pdiff(p1, p3, v31);
+    pdiff(p4, p1, v14);
+    pdiff(p2, p3, v32);
+    pdiff(p4, p2, v24);
+    const float cx = v12[1] * v34[2] - v12[2] * v34[1], cy = v12[2] * v34[0] - v12[0] * v34[2],
+                cz = v12[0] * v34[1] - v12[1] * v34[0];
+    const float trip = fabsf(cx * v31[0] + cy * v31[1] + cz * v31[2]);
+    const float q = trip / (sqrtf(dot3(v12, v12)) * sqrtf(dot3(v34, v34)) * sqrtf(dot3(v31, v31)));
+    need64 = !(q >= kMixedTauEnergy);
+    if (need64) return 0.f;
+    PairInv<float> pi;
+    pair_inv(v12, v34, v31, v14, v32, v24, pi, true);
+    const float u = energy_value(pi, kRep);
+    if (u != u) {
+        need64 = true;
+        return 0.f;
+    }
+    return u;
+}
+
 template <typename Real>
 __global__ void __launch_bounds__(kBlock) k_exvol(DevNet<Real> n, int want, int trial, int force, int tile_off) {
+    MECH_TRACE_KERNEL(n, TK_EXVOL);
     __shared__ double sh[32];
     __shared__ int s_go, s_xb;
     __shared__ double s_lam;
@@ -255,7 +285,9 @@ __global__ void __launch_bounds__(kBlock) k_exvol(DevNet<Real> n, int want, int 
     const bool valid = i < t.end;
     double e = 0.0;   // FP64 engine
     float ef = 0.f;   // mixed engine
-    bool need64 = false;
+    bool need64 = false, need64b = false;
+    // a two-trial pass also evaluates the energy at lambda / 2 (mixed engine)
+    const bool dual = sizeof(Real) == 4 && trial == kTrialDual && !force;
     if (valid) {
         const int4 bs = n.ev_bead[i];
         auto pos = [&](int b) -> Pos<Real> {
@@ -288,8 +320,21 @@ __global__ void __launch_bounds__(kBlock) k_exvol(DevNet<Real> n, int want, int 
                 }
                 if (!ok) flag_fallback(n, r, i, 0.0);
             }
-        } else {
+        } else if (!force) {
             // mixed engine: single precision unless the pair is ill-conditioned
+            const float kRep = n.ev_k[i] * n.ev_la[i] * n.ev_lb[i];
+            ef = mixed_pair_energy(p1, p2, p3, p4, kRep, need64);
+            store_pair(n.ev_energy + i, ef, 0.f);
+            if (dual) {
+                const float lh = 0.5f * s_lf;
+                const float ef2 = mixed_pair_energy(moved_f(load_pos(X, bs.x), n.d, bs.x, lh),
+                                                    moved_f(load_pos(X, bs.y), n.d, bs.y, lh),
+                                                    moved_f(load_pos(X, bs.z), n.d, bs.z, lh),
+                                                    moved_f(load_pos(X, bs.w), n.d, bs.w, lh), kRep, need64b);
+                store_pair(n.ev_energy2 + i, ef2, 0.f);
+            }
+        } else {
+            // mixed engine, forces: single precision unless the pair is ill-conditioned
             const float kRep = n.ev_k[i] * n.ev_la[i] * n.ev_lb[i];
             float v12[3], v34[3], v31[3], v14[3], v32[3], v24[3];
             pdiff(p2, p1, v12);
@@ -326,26 +371,22 @@ __global__ void __launch_bounds__(kBlock) k_exvol(DevNet<Real> n, int want, int 
             if (!need64) {
                 PairInv<float> pi;
                 pair_inv(v12, v34, v31, v14, v32, v24, pi, true);
-                if (!force) {
-                    const float u = energy_value(pi, kRep);
-                    if (u != u) need64 = true;
-                    else ef = u;
-                } else {
-                    float out[4][3];
-                    if (forces_from<true>(pi, v12, v34, v31, kRep, out)) {
-                        for (int a = 0; a < 4; ++a) {
-                            Real* cdst = slot_ptr(n, n.slot_base[K_EXVOL] + 4 * i + a);
-                            for (int k = 0; k < 3; ++k) cdst[k] = (Real)out[a][k];
-                        }
-                    } else {
-                        need64 = true;
+                float out[4][3];
+                if (forces_from<true>(pi, v12, v34, v31, kRep, out)) {
+                    for (int a = 0; a < 4; ++a) {
+                        Real* cdst = slot_ptr(n, n.slot_base[K_EXVOL] + 4 * i + a);
+                        for (int k = 0; k < 3; ++k) cdst[k] = (Real)out[a][k];
                     }
+                } else {
+                    need64 = true;
                 }
             }
-            if (!force) store_pair(n.ev_energy + i, need64 ? 0.f : ef, 0.f);
         }
     }
-    if constexpr (sizeof(Real) == 4) append_fp64(n, need64, r, i);
+    if constexpr (sizeof(Real) == 4) {
+        append_fp64(n, need64, r, i);
+        if (dual) append_fp64(n, need64b, r, i | kExtSecond);   // block-uniform
+    }
     if (!force && sizeof(Real) == 8) {
         e = block_sum(e, sh);
         if (threadIdx.x == 0) n.part_sp[ti] = e;
@@ -377,21 +418,28 @@ struct ExtTerm {
 
 template <typename Real>
 __global__ void __launch_bounds__(128) k_exvol_ext(DevNet<Real> n, int trial, int force) {
+    MECH_TRACE_KERNEL(n, TK_EXVOL_EXT);
     __shared__ double s_c[4][32][3];       // bead positions
     __shared__ double s_N[3][32];          // CC, GG, DD for the F term's HH
     __shared__ ExtTerm s_t[4][32];
     __shared__ double s_G[6][32];
     __shared__ int s_bad[32];
-    const int cnt = min(*n.ev_list_count, n.n_ev);
+    const int cnt = min(*n.ev_list_count, 2 * n.n_ev);
     const int w = threadIdx.x >> 5, l = threadIdx.x & 31;
     const int ngroups = (cnt + 31) >> 5;
     for (int g = blockIdx.x; g < ngroups; g += gridDim.x) {
         const int k = 32 * g + l;
         const bool valid = k < cnt;
         int r = 0, i = 0;
+        bool second = false;   // the lambda / 2 trial of a two-trial pass
+        double lam = 0.0;
         if (valid) {
             r = n.ev_list[2 * k];
             i = n.ev_list[2 * k + 1];
+            second = (i & kExtSecond) != 0;
+            i &= ~kExtSecond;
+            lam = n.st[r].lambda;
+            if (second) lam *= 0.5;
         }
         // ---- positions: warp w converts bead w of every pair
         if (valid) {
@@ -399,7 +447,7 @@ __global__ void __launch_bounds__(128) k_exvol_ext(DevNet<Real> n, int trial, in
             const int4 bs = n.ev_bead[i];
             const int bead = w == 0 ? bs.x : w == 1 ? bs.y : w == 2 ? bs.z : bs.w;
             double c[3];
-            to_double(bead_at(n.x[S.xbuf], n.d, bead, trial != 0, S.lambda), c);
+            to_double(bead_at(n.x[S.xbuf], n.d, bead, trial != 0, lam), c);
             s_c[w][l][0] = c[0];
             s_c[w][l][1] = c[1];
             s_c[w][l][2] = c[2];
@@ -501,12 +549,13 @@ __global__ void __launch_bounds__(128) k_exvol_ext(DevNet<Real> n, int trial, in
             if (w == 0 && valid) {
                 const double Ssum = s_t[0][l].S + s_t[1][l].S + s_t[2][l].S + s_t[3][l].S;
                 const double U = 0.5 * kRep / JJ * Ssum;
+                double* dst = (second ? n.ev_energy2 : n.ev_energy) + i;
                 if (!(fabs(U) < 1.0 / 0.0) || U < -1.0) {
-                    flag_fallback(n, r, i, trial != 0 ? n.st[r].lambda : 0.0);
-                    store_pair(n.ev_energy + i, 0.f, 0.f);
+                    flag_fallback(n, r, i, trial != 0 ? lam : 0.0);
+                    store_pair(dst, 0.f, 0.f);
                 } else {
                     const float h = (float)U;
-                    store_pair(n.ev_energy + i, h, (float)(U - (double)h));
+                    store_pair(dst, h, (float)(U - (double)h));
                 }
             }
             __syncthreads();   // shared arrays are reused by the next group
@@ -573,24 +622,39 @@ __global__ void __launch_bounds__(128) k_exvol_ext(DevNet<Real> n, int trial, in
 // sums of the per-pair energies (one block per exvol tile).
 constexpr int kFbEnergyBlocks = 64;
 template <typename Real>
-__global__ void __launch_bounds__(kBlock) k_exvol_energy_tail(DevNet<Real> n, int want, int tile_off) {
-    __shared__ double sh[32];
+__global__ void __launch_bounds__(kBlock) k_exvol_energy_tail(DevNet<Real> n, int want, int trial, int tile_off) {
+    MECH_TRACE_KERNEL(n, TK_EXVOL_TAIL);
+    __shared__ double sh[64];   // block_reduce_ff<2>: 32 * 4 floats
     if ((int)blockIdx.x < kFbEnergyBlocks) {
         fb_energy_blocks(n, blockIdx.x, kFbEnergyBlocks, sh);
-        return;
-    }
-    const int ti = tile_off + (int)blockIdx.x - kFbEnergyBlocks;
-    const Tile t = n.stile[ti];
-    const CGState& S = n.st[t.replica];
-    const bool go = want < 0 ? (S.active != 0) : (S.phase == want);
-    if (!go) return;
-    if constexpr (sizeof(Real) == 4) {
-        // per-pair energies as (hi, lo) pairs, summed compensated in single precision
-        const int i = t.begin + threadIdx.x;
-        FF a[1];
-        if (i < t.end) add_pair(a[0], load_pair(n.ev_energy + i));
-        block_reduce_ff<1, 0>(a, nullptr, reinterpret_cast<float*>(sh));
-        if (threadIdx.x == 0) store_pair(n.part_sp + ti, a[0].h, a[0].l);
+    } else {
+        const int ti = tile_off + (int)blockIdx.x - kFbEnergyBlocks;
+        const Tile t = n.stile[ti];
+        const CGState& S = n.st[t.replica];
+        const bool go = want < 0 ? (S.active != 0) : (S.phase == want);
+        if constexpr (sizeof(Real) == 4) {
+            if (go) {   // block-uniform
+                // per-pair energies as (hi, lo) pairs, summed compensated in single precision
+                const int i = t.begin + threadIdx.x;
+                if (trial == kTrialDual) {   // both trials of a two-trial pass
+                    FF a[2];
+                    if (i < t.end) {
+                        add_pair(a[0], load_pair(n.ev_energy + i));
+                        add_pair(a[1], load_pair(n.ev_energy2 + i));
+                    }
+                    block_reduce_ff<2, 0>(a, nullptr, reinterpret_cast<float*>(sh));
+                    if (threadIdx.x == 0) {
+                        store_pair(n.part_sp + ti, a[0].h, a[0].l);
+                        store_pair(n.part_sp2 + ti, a[1].h, a[1].l);
+                    }
+                } else {
+                    FF a[1];
+                    if (i < t.end) add_pair(a[0], load_pair(n.ev_energy + i));
+                    block_reduce_ff<1, 0>(a, nullptr, reinterpret_cast<float*>(sh));
+                    if (threadIdx.x == 0) store_pair(n.part_sp + ti, a[0].h, a[0].l);
+                }
+            }
+        }
     }
 }
 
@@ -628,7 +692,7 @@ int launch_exvol_energy(const DevNet<Real>& n, int want, int trial, cudaStream_t
         k_exvol_ext<Real><<<kExtBlocks, 128, 0, s>>>(n, trial, 0);
         ++k;
     }
-    k_exvol_energy_tail<Real><<<kFbEnergyBlocks + (sizeof(Real) == 4 ? nt : 0), kBlock, 0, s>>>(n, want, off);
+    k_exvol_energy_tail<Real><<<kFbEnergyBlocks + (sizeof(Real) == 4 ? nt : 0), kBlock, 0, s>>>(n, want, trial, off);
     return k + 1;
 }
 

@@ -19,6 +19,7 @@
 #include <algorithm>
 
 #include "mech_bulk.cuh"
+#include "mech_cg.cuh"
 #include "mech_device.cuh"
 
 namespace mech {
@@ -65,209 +66,6 @@ __device__ __forceinline__ void bond_vector(const Pos<float>& c1, const Pos<floa
     pdiff(c2, c1, d21);
 #pragma unroll
     for (int k = 0; k < 3; ++k) v[k] = fmaf(s2, d43[k], fmaf(-s1, d21[k], d31[k]));
-}
-
-__device__ __forceinline__ bool replica_selected(const CGState& S, int want) {
-    return want < 0 ? (S.active != 0) : (S.phase == want);
-}
-
-// ---------------------------------------------------------------------------
-// finalizers (run by the whole last block of a replica)
-// ---------------------------------------------------------------------------
-// Partial-sum slots of a replica's tile range [b, e): the FP64 kernels write
-// one per tile (stride 1); the persistent mixed kernels write one per run of
-// tiles, at b and at every multiple of their tiles-per-block inside (b, e).
-__device__ __forceinline__ int run_slots(int b, int e, int stride) {
-    const int m0 = (b / stride + 1) * stride;
-    return 1 + (m0 < e ? (e - 1 - m0) / stride + 1 : 0);
-}
-__device__ __forceinline__ int run_slot(int b, int stride, int k) {
-    return k == 0 ? b : (b / stride + 1) * stride + (k - 1) * stride;
-}
-
-// The CG step logic of the finalizers runs in thread 0 on a register copy of
-// its replica's state, loaded at the start so that the loads overlap the
-// block's reduction, and stored back once: done field by field on global
-// memory, the branchy logic waits on one dependent load after another.
-template <typename Real>
-__device__ void finalize_energy(const DevNet<Real>& n, int r, int trial, double* sh) {
-    CGState S;
-    if (threadIdx.x == 0) S = n.st[r];
-    const RepTiles rt = n.rt[r];
-    const int stride = sizeof(Real) == 4 ? n.ptiles[0] : 1;
-    const int nslot = run_slots(rt.fil_begin, rt.fil_end, stride);
-    const int ffk[K_NUM_SPARSE] = {MECH_FF_LINKER, MECH_FF_MOTOR, MECH_FF_EXVOL, MECH_FF_BOUNDARY};
-    double e[MECH_NUM_FF];
-    if constexpr (sizeof(Real) == 4) {
-        // mixed: (hi, lo) pair slots summed compensated in single precision;
-        // the doubles are formed in thread 0 only
-        FF acc[MECH_NUM_FF];
-#pragma unroll 4
-        for (int k = threadIdx.x; k < nslot; k += blockDim.x) {
-            const double* slot = n.part_fil + 4 * (size_t)run_slot(rt.fil_begin, stride, k);
-            add_pair(acc[MECH_FF_STRETCHING], load_pair(slot));
-            add_pair(acc[MECH_FF_BENDING], load_pair(slot + 1));
-        }
-#pragma unroll
-        for (int k = 0; k < K_NUM_SPARSE; ++k) {
-#pragma unroll 4
-            for (int i = rt.sp_begin[k] + threadIdx.x; i < rt.sp_end[k]; i += blockDim.x)
-                add_pair(acc[ffk[k]], load_pair(n.part_sp + i));
-        }
-        block_reduce_ff<MECH_NUM_FF, 0>(acc, nullptr, reinterpret_cast<float*>(sh));
-        if (threadIdx.x != 0) return;
-#pragma unroll
-        for (int k = 0; k < MECH_NUM_FF; ++k) e[k] = (double)acc[k].h + (double)acc[k].l;
-    } else {
-        // every thread issues its loads back to back, then sums in a fixed order
-        double acc[MECH_NUM_FF] = {0, 0, 0, 0, 0, 0};
-#pragma unroll 8
-        for (int k = threadIdx.x; k < nslot; k += blockDim.x) {
-            const int i = run_slot(rt.fil_begin, stride, k);
-            const double2 v = __ldcg(reinterpret_cast<const double2*>(n.part_fil + 4 * (size_t)i));
-            acc[MECH_FF_STRETCHING] += v.x;
-            acc[MECH_FF_BENDING] += v.y;
-        }
-#pragma unroll
-        for (int k = 0; k < K_NUM_SPARSE; ++k) {
-#pragma unroll 8
-            for (int i = rt.sp_begin[k] + threadIdx.x; i < rt.sp_end[k]; i += blockDim.x)
-                acc[ffk[k]] += __ldcg(n.part_sp + i);
-        }
-#pragma unroll
-        for (int k = 0; k < MECH_NUM_FF; ++k) e[k] = warp_sum(acc[k]);
-        const int ops[MECH_NUM_FF] = {0, 0, 0, 0, 0, 0};
-        block_combine<MECH_NUM_FF>(e, ops, sh);
-        if (threadIdx.x != 0) return;
-    }
-    // Pairs whose analytic energy was not usable were evaluated numerically;
-    // add them in pair order.  A failed pair makes the force field report -1
-    // (CylinderExclVolRepulsion.cpp:442-481).
-    const int cnt = min(__ldcg(n.ev_fb_count), kExvolFallbackCap);
-    int last = -1;
-    bool ev_failed = false;
-    for (;;) {
-        int best = -1, bestPair = 0x7fffffff;
-        for (int k = 0; k < cnt; ++k) {
-            const int rep = __ldcg(n.ev_fb_list + 2 * k), pr = __ldcg(n.ev_fb_list + 2 * k + 1);
-            if (rep == r && pr > last && pr < bestPair) { best = k; bestPair = pr; }
-        }
-        if (best < 0) break;
-        const double u = __ldcg(n.ev_fb_energy + best);
-        if (u == -1.0) ev_failed = true;
-        else e[MECH_FF_EXVOL] += u;
-        last = bestPair;
-    }
-    if (ev_failed) e[MECH_FF_EXVOL] = -1.0;
-    double tot = 0.0;
-    bool failed = false;
-    for (int k = 0; k < MECH_NUM_FF; ++k) {
-        S.eval[k] = e[k];
-        tot += e[k];
-        if (e[k] <= -1) failed = true;
-    }
-    S.eval[MECH_NUM_FF] = tot;
-    S.evalFailed = failed;
-    S.numEnergyEval++;
-    const double E = failed ? (1.0 / 0.0) : tot;
-    if (trial && S.phase == PH_LS_TRIAL) {
-        S.Etrial = E;
-        line_search_step(S, E);
-    } else if (S.phase == PH_RECOVER_ENERGY) {
-        S.E0 = E;
-        S.phase = PH_RESET;
-    } else {
-        S.E0 = E;
-    }
-    n.st[r] = S;
-}
-
-// CG bookkeeping after the forces (CGMethod.hpp:1540-1580): max |F|, beta.
-__device__ __forceinline__ void force_step(CGState& S, double mx, double ff, double ffp) {
-    const int ph = S.phase;
-    if (ph == PH_FORCE || ph == PH_RECOVER_FORCE) S.numForceCall++;
-    S.maxF = mx;
-    S.FdotF = ff;
-    S.fbuf ^= 1;
-    if (!isfinite(mx)) {   // CGMethod::maxF throws (CGMethod.hpp:207-210)
-        S.status = MECH_ERR_NONFINITE;
-        S.phase = PH_ERROR;
-        return;
-    }
-    if (ph == PH_FORCE) {
-        S.energyRelChange = fabs(S.newEnergy - S.prevEnergy) / fabs(S.prevEnergy);
-        S.prevEnergy = S.newEnergy;
-        double beta = 0.0;
-        if (S.method == 1) {
-            S.newGrad = ff;
-            beta = S.newGrad / S.lastFdotF;
-        } else if (S.method == 2) {
-            S.newGrad = ff;
-            S.prevGrad = ffp;
-            beta = fmax(0.0, (S.newGrad - S.prevGrad) / S.lastFdotF);
-        }
-        S.beta = beta;
-        // minimum-energy backup once past half the call limit (CGMethod.hpp:1564-1566)
-        if (mx <= 10 * S.gradTol && S.numIter > S.forceCallLimit / 2 && S.totalEnergy <= S.minimumE) {
-            S.minimumE = S.totalEnergy;
-            S.backupPending = 1;
-        }
-        S.phase = PH_DIR;
-    } else if (ph == PH_RECOVER_FORCE) {
-        S.phase = PH_RECOVER_ENERGY;
-    }
-}
-
-template <typename Real>
-__device__ void finalize_force(const DevNet<Real>& n, int r, double* sh) {
-    CGState S;
-    if (threadIdx.x == 0) S = n.st[r];
-    const RepTiles rt = n.rt[r];
-    const int stride = 1;   // k_force_gather writes one slot per tile
-    const int nslot = run_slots(rt.fil_begin, rt.fil_end, stride);
-    double mx, ff, ffp;
-    if constexpr (sizeof(Real) == 4) {
-        // mixed slots hold float maxima and (hi, lo) pairs; sum them compensated
-        // in single precision and form the doubles in thread 0 only
-        FF a[2];
-        float m[1] = {0.f};
-#pragma unroll 8
-        for (int k = threadIdx.x; k < nslot; k += blockDim.x) {
-            const float* p = reinterpret_cast<const float*>(n.part_fil + 4 * (size_t)run_slot(rt.fil_begin, stride, k));
-            const float4 v = __ldcg(reinterpret_cast<const float4*>(p));
-            const float w = __ldcg(p + 4);
-            m[0] = fmaxf(m[0], v.x);
-            a[0].add(v.y);
-            a[0].add(v.z);
-            a[1].add(v.w);
-            a[1].add(w);
-        }
-        block_reduce_pairs<2, 1>(a, m, reinterpret_cast<float*>(sh));
-        if (threadIdx.x != 0) return;
-        mx = (double)m[0];
-        ff = (double)a[0].h + (double)a[0].l;
-        ffp = (double)a[1].h + (double)a[1].l;
-    } else {
-        double a_mx = 0.0, a_ff = 0.0, a_ffp = 0.0;
-#pragma unroll 8
-        for (int k = threadIdx.x; k < nslot; k += blockDim.x) {
-            const int i = run_slot(rt.fil_begin, stride, k);
-            const double2 v = __ldcg(reinterpret_cast<const double2*>(n.part_fil + 4 * (size_t)i));
-            const double w = __ldcg(n.part_fil + 4 * (size_t)i + 2);
-            a_mx = fmax(a_mx, v.x);
-            a_ff += v.y;
-            a_ffp += w;
-        }
-        double red[3] = {warp_max(a_mx), warp_sum(a_ff), warp_sum(a_ffp)};
-        const int ops[3] = {1, 0, 0};
-        block_combine<3>(red, ops, sh);
-        mx = red[0];
-        ff = red[1];
-        ffp = red[2];
-        if (threadIdx.x != 0) return;
-    }
-    force_step(S, mx, ff, ffp);
-    n.st[r] = S;
 }
 
 // ---------------------------------------------------------------------------
@@ -334,6 +132,7 @@ __device__ void after_evaluation(const DevNet<Real>& n, int phase_slot, int* s_f
 // The kernel at the head of every body of the minimizer's while loop.
 template <typename Real>
 __global__ void __launch_bounds__(kBlock) k_body_head(DevNet<Real> n) {
+    MECH_TRACE_KERNEL(n, TK_BODY_HEAD);
     set_conditions(n, true, -1);
 }
 
@@ -342,6 +141,7 @@ __global__ void __launch_bounds__(kBlock) k_body_head(DevNet<Real> n) {
 // ---------------------------------------------------------------------------
 template <typename Real>
 __global__ void __launch_bounds__(kBlock) k_fil_energy(DevNet<Real> n, int want, int trial) {
+    MECH_TRACE_KERNEL(n, TK_FIL_ENERGY);
     __shared__ Pos<Real> xs[kFilTile + 4];
     __shared__ double sh[32 * MECH_NUM_FF];
     __shared__ int s_go, s_xb;
@@ -381,6 +181,10 @@ __global__ void __launch_bounds__(kBlock) k_fil_energy(DevNet<Real> n, int want,
                     pdiff(xs[i + 2], xs[i + 1], r1);
                     eb = bend_energy<Real>(r1, r2, kb, t0);
                 }
+                if (n.terms) {
+                    n.terms[j] = (double)es;
+                    n.terms[(size_t)n.nb + j] = (double)eb;
+                }
             }
         }
         double red[2] = {warp_sum_r(es), warp_sum_r(eb)};
@@ -399,6 +203,7 @@ __global__ void __launch_bounds__(kBlock) k_fil_energy(DevNet<Real> n, int want,
 // ---------------------------------------------------------------------------
 template <typename Real>
 __global__ void __launch_bounds__(kBlock) k_fil_force(DevNet<Real> n, int want) {
+    MECH_TRACE_KERNEL(n, TK_FIL_FORCE);
     __shared__ Pos<Real> xs[kFilTile + 4];
     __shared__ Real fs[(kFilTile + 2) * 3];    // stretch force on the second bead
     __shared__ Real f1[(kFilTile + 2) * 3];    // bending Fr1
@@ -500,6 +305,7 @@ __device__ __forceinline__ void gather_bead(const DevNet<Real>& n, int b, int fb
 
 template <typename Real>
 __global__ void __launch_bounds__(kBlock) k_force_gather(DevNet<Real> n, int want) {
+    MECH_TRACE_KERNEL(n, TK_GATHER);
     __shared__ double sh[32 * 3];
     __shared__ int s_go[kGatherTiles], s_fb[kGatherTiles];
     const int t0 = blockIdx.x * kGatherTiles;
@@ -548,6 +354,7 @@ __global__ void __launch_bounds__(kBlock) k_force_gather(DevNet<Real> n, int wan
 // bead); otherwise 4 beads strided by 64.  The tile's partials combine the
 // two warps of its 64 threads.
 __global__ void __launch_bounds__(kBlock) k_force_gather_mx(DevNet<float> n, int want) {
+    MECH_TRACE_KERNEL(n, TK_GATHER_MX);
     static_assert(kFilTile == 256 && kBlock == 64 * kGatherTiles, "64 threads x 4 beads per tile");
     __shared__ float sh[8][5];   // per warp: F.F (hi, lo), F.Fprev (hi, lo), max
     __shared__ int s_go[kGatherTiles], s_fb[kGatherTiles];
@@ -648,6 +455,7 @@ __global__ void __launch_bounds__(kBlock) k_force_gather_mx(DevNet<float> n, int
 // One block per replica: max |F|, the dots and the CG step logic after the gather.
 template <typename Real>
 __global__ void __launch_bounds__(kBlock) k_finalize_force(DevNet<Real> n, int want) {
+    MECH_TRACE_KERNEL(n, TK_FIN_FORCE);
     __shared__ double sh[32 * 3];
     __shared__ int s_flag;
     const int r = blockIdx.x;
@@ -659,7 +467,8 @@ __global__ void __launch_bounds__(kBlock) k_finalize_force(DevNet<Real> n, int w
 // every kernel of the evaluation has written its partial sums.
 template <typename Real>
 __global__ void __launch_bounds__(kBlock) k_finalize_energy(DevNet<Real> n, int want, int trial) {
-    __shared__ double sh[32 * MECH_NUM_FF];
+    MECH_TRACE_KERNEL(n, TK_FIN_ENERGY);
+    __shared__ double sh[32 * 2 * MECH_NUM_FF];   // block_reduce_ff<12> of a two-trial pass: 32 * 24 floats
     __shared__ int s_flag;
     const int r = blockIdx.x;
     if (replica_selected(n.st[r], want)) finalize_energy(n, r, trial, sh);
@@ -736,8 +545,8 @@ __device__ __forceinline__ StageRange stage_range(int tb, int te, int nb, int ha
 
 // A block's tile descriptors, read once at kernel start (one thread per tile)
 // so the producing thread issues copies without chasing global pointers:
-// (begin, end, replica, bits) with bit 0 = selected by this launch, bit 1 =
-// xbuf, bit 2 = fbuf of the tile's replica, plus that replica's lambda.  A
+// (begin, end, replica, bits) with bit 0 = selected by this launch, bits 1-2 =
+// xbuf, bit 3 = fbuf of the tile's replica, plus that replica's lambda.  A
 // replica's state cannot change while this block still holds unprocessed
 // tiles of it (its finalizer waits for every tile), so the copies stay valid.
 constexpr int kBulkMaxTiles = kFilBulkMaxTiles;
@@ -748,7 +557,7 @@ __device__ __forceinline__ void load_descriptors(const DevNet<float>& n, int t0,
         const Tile t = n.ftile[t0 + k];
         const CGState& S = n.st[t.replica];
         desc[k] = make_int4(t.begin, t.end, t.replica,
-                            (replica_selected(S, want) ? 1 : 0) | (S.xbuf << 1) | (S.fbuf << 2));
+                            (replica_selected(S, want) ? 1 : 0) | (S.xbuf << 1) | (S.fbuf << 3));
         lf[k] = (float)S.lambda;
     }
 }
@@ -757,7 +566,7 @@ __device__ __forceinline__ void load_descriptors(const DevNet<float>& n, int t0,
 // the alignment check is not copied: the barrier is completed without it and
 // the error word records it.
 __device__ void issue_energy_stage(const DevNet<float>& n, int4 t, bool tr, EnergyStage* st, uint64_t* bar) {
-    const float* X = n.x[(t.w >> 1) & 1];
+    const float* X = n.x[(t.w >> 1) & 3];
     const StageRange rg = stage_range(t.x, t.y, n.nb, 1);
     const void* src[4] = {X + 6 * (size_t)rg.xs, n.bpar + 4 * (size_t)t.x, n.d + 3 * (size_t)rg.ds, n.bflag + rg.fs};
     void* dst[4] = {st->x, st->par, st->d, st->flag};
@@ -799,11 +608,12 @@ __device__ __forceinline__ bool idle_range(const DevNet<float>& n, int t0, int t
 }
 
 __global__ void __launch_bounds__(kBlock) k_fil_energy_bulk(DevNet<float> n, int want, int trial) {
+    MECH_TRACE_KERNEL(n, TK_FIL_ENERGY_BULK);
     __shared__ EnergyStage stage[kBulkStages];
     __shared__ __align__(8) uint64_t bar[kBulkStages];
     __shared__ int4 s_desc[kBulkMaxTiles];
     __shared__ float s_lf[kBulkMaxTiles];
-    __shared__ double sh[32 * 2];
+    __shared__ double sh[32 * 4];   // write_run<4>: 32 * 8 floats
     __shared__ int s_abort;
     const int t0 = blockIdx.x * n.ptiles[0], t1 = min(t0 + n.ptiles[0], n.n_ftiles);
     const int nt = t1 - t0;
@@ -829,24 +639,36 @@ __global__ void __launch_bounds__(kBlock) k_fil_energy_bulk(DevNet<float> n, int
                 ++issued;
             }
     }
+    // a two-trial pass (trial == kTrialDual): energies at lambda into slots 0, 1
+    // of the run and at lambda / 2 into slots 2, 3; trial positions into the
+    // two buffers after the current one
+    const bool dual = trial == kTrialDual;
     int cur = -1, first = 0, cnt = 0, xb = 0, j = 0;
     bool go = false;
     float lf = 0.f;
-    FF es, eb;
+    FF es, eb, es2, eb2;
+    auto flush = [&]() {
+        if (dual) {
+            FF a[4] = {es, eb, es2, eb2};
+            write_run<4>(n, first, a, sh);
+        } else {
+            FF a[2] = {es, eb};
+            write_run<2>(n, first, a, sh);
+        }
+    };
     for (int k = 0; k < nt; ++k) {
         const int4 t = s_desc[k];
         if (t.z != cur) {
-            if (cnt) {
-                FF a[2] = {es, eb};
-                write_run<2>(n, first, a, sh);
-            }
+            if (cnt) flush();
             cur = t.z;
             first = t0 + k;
             cnt = 0;
             es = FF();
             eb = FF();
+            es2 = FF();
+            eb2 = FF();
             go = t.w & 1;
-            xb = (t.w >> 1) & 1;
+            xb = (t.w >> 1) & 3;
             lf = s_lf[k];
         }
         if (!go) continue;
@@ -861,24 +683,50 @@ __global__ void __launch_bounds__(kBlock) k_fil_energy_bulk(DevNet<float> n, int
         if (b < t.y) {
             const StageRange rg = stage_range(t.x, t.y, n.nb, 1);
             const int fl = S.flag[b - rg.fs];
-            Pos<float> p0 = load_pos(S.x, b - rg.xs);
-            Pos<float> pp = fl & 1 ? load_pos(S.x, b + 1 - rg.xs) : p0;
-            Pos<float> pm = fl & 2 ? load_pos(S.x, b - 1 - rg.xs) : p0;
+            const Pos<float> q0 = load_pos(S.x, b - rg.xs);
+            const Pos<float> qp = fl & 1 ? load_pos(S.x, b + 1 - rg.xs) : q0;
+            const Pos<float> qm = fl & 2 ? load_pos(S.x, b - 1 - rg.xs) : q0;
+            Pos<float> p0 = q0, pp = qp, pm = qm;
             if (tr) {
-                p0 = moved_f(p0, S.d, b - rg.ds, lf);
-                if (fl & 1) pp = moved_f(pp, S.d, b + 1 - rg.ds, lf);
-                if (fl & 2) pm = moved_f(pm, S.d, b - 1 - rg.ds, lf);
-                store_pos(n.x[xb ^ 1], b, p0);   // materialize the owned trial position
+                p0 = moved_f(q0, S.d, b - rg.ds, lf);
+                if (fl & 1) pp = moved_f(qp, S.d, b + 1 - rg.ds, lf);
+                if (fl & 2) pm = moved_f(qm, S.d, b - 1 - rg.ds, lf);
+                store_pos(n.x[(xb + 1) % 3], b, p0);   // materialize the owned trial position
             }
             const float4 pr = S.par[b - t.x];
+            if (dual && (fl & 1)) {
+                // the second trial, at lambda / 2 (halving is exact in float)
+                const float lh = 0.5f * lf;
+                const Pos<float> h0 = moved_f(q0, S.d, b - rg.ds, lh);
+                const Pos<float> hp = moved_f(qp, S.d, b + 1 - rg.ds, lh);
+                store_pos(n.x[(xb + 2) % 3], b, h0);
+                float r2[3];
+                pdiff(hp, h0, r2);
+                es2.add(stretch_energy<float>(r2[0], r2[1], r2[2], pr.x, pr.y));
+                if (fl & 2) {
+                    const Pos<float> hm = moved_f(qm, S.d, b - 1 - rg.ds, lh);
+                    float r1[3];
+                    pdiff(h0, hm, r1);
+                    eb2.add(bend_energy<float>(r1, r2, pr.z, pr.w));
+                }
+            } else if (dual) {
+                store_pos(n.x[(xb + 2) % 3], b, moved_f(q0, S.d, b - rg.ds, 0.5f * lf));
+            }
             if (fl & 1) {
                 float r2[3];
                 pdiff(pp, p0, r2);
-                es.add(stretch_energy<float>(r2[0], r2[1], r2[2], pr.x, pr.y));
+                const float ts = stretch_energy<float>(r2[0], r2[1], r2[2], pr.x, pr.y);
+                es.add(ts);
+                float tb = 0.f;
                 if (fl & 2) {
                     float r1[3];
                     pdiff(p0, pm, r1);
-                    eb.add(bend_energy<float>(r1, r2, pr.z, pr.w));
+                    tb = bend_energy<float>(r1, r2, pr.z, pr.w);
+                    eb.add(tb);
+                }
+                if (n.terms) {
+                    n.terms[b] = (double)ts;
+                    n.terms[(size_t)n.nb + b] = (double)tb;
                 }
             }
         }
@@ -902,10 +750,7 @@ __global__ void __launch_bounds__(kBlock) k_fil_energy_bulk(DevNet<float> n, int
                 mbar_wait_bounded(&bar[q % kBulkStages], (unsigned)((q / kBulkStages) & 1), kBulkWaitLimit);
         return;
     }
-    if (cnt) {
-        FF a[2] = {es, eb};
-        write_run<2>(n, first, a, sh);
-    }
+    if (cnt) flush();
 }
 
 
@@ -941,7 +786,7 @@ __device__ __forceinline__ ForceRange force_range(int tb, int te, int nb) {
 }
 
 __device__ void issue_force_stage(const DevNet<float>& n, int4 t, ForceStage* st, uint64_t* bar) {
-    const float* X = n.x[(t.w >> 1) & 1];
+    const float* X = n.x[(t.w >> 1) & 3];
     const ForceRange rg = force_range(t.x, t.y, n.nb);
     const void* src[3] = {X + 6 * (size_t)rg.xs, n.bpar + 4 * (size_t)rg.ps, n.bflag + rg.fs};
     void* dst[3] = {st->x, st->par, st->flag};
@@ -971,6 +816,7 @@ __device__ void issue_force_stage(const DevNet<float>& n, int4 t, ForceStage* st
 // is written to the force buffer, where k_force_gather adds the bead's sparse
 // contributions and forms the CG partials.
 __global__ void __launch_bounds__(kBlock) k_fil_force_bulk(DevNet<float> n, int want) {
+    MECH_TRACE_KERNEL(n, TK_FIL_FORCE_BULK);
     __shared__ ForceStage stage[kBulkStages];
     __shared__ __align__(8) uint64_t bar[kBulkStages];
     __shared__ int4 s_desc[kBulkMaxTiles];
@@ -1002,7 +848,7 @@ __global__ void __launch_bounds__(kBlock) k_fil_force_bulk(DevNet<float> n, int 
     for (int k = 0; k < nt; ++k) {
         const int4 t = s_desc[k];
         if (!(t.w & 1)) continue;
-        const int fb = (t.w >> 2) & 1;
+        const int fb = (t.w >> 3) & 1;
         const int sidx = j % kBulkStages;
         if (!mbar_wait_bounded(&bar[sidx], (unsigned)((j / kBulkStages) & 1), kBulkWaitLimit)) {
             atomicOr(n.err, 32u);
@@ -1080,6 +926,7 @@ __global__ void __launch_bounds__(kBlock) k_fil_force_bulk(DevNet<float> n, int 
 
 // Mixed engine: persistent direction update d = F + beta d with the d.F partials.
 __global__ void __launch_bounds__(kBlock) k_direction_mx(DevNet<float> n) {
+    MECH_TRACE_KERNEL(n, TK_DIRECTION_MX);
     __shared__ double sh[32];
     const int t0 = blockIdx.x * n.ptiles[2], t1 = min(t0 + n.ptiles[2], n.n_ftiles);
     int cur = -1, first = 0, cnt = 0, fb = 0, xb = 0, bk = 0;
@@ -1130,7 +977,8 @@ __global__ void __launch_bounds__(kBlock) k_direction_mx(DevNet<float> n) {
 template <typename Real>
 __global__ void __launch_bounds__(kBlock) k_bond_bnd(DevNet<Real> n, int want, int trial, int force, int n_lm_tiles,
                                                      int ev_tiles) {
-    __shared__ double sh[32];
+    MECH_TRACE_KERNEL(n, TK_BOND);
+    __shared__ double sh[64];   // block_reduce_ff<2>: 32 * 4 floats
     __shared__ int s_go, s_xb;
     __shared__ double s_lam;
     __shared__ float s_lf;   // the step rounded once (mixed engine)
@@ -1149,16 +997,19 @@ __global__ void __launch_bounds__(kBlock) k_bond_bnd(DevNet<Real> n, int want, i
     if (!s_go) return;
     const Real* X = n.x[s_xb];
     const bool tr = trial != 0;
-    auto pos = [&](int b) -> Pos<Real> {
+    // a two-trial pass also evaluates the energy at lambda / 2 (mixed engine)
+    const bool dual = sizeof(Real) == 4 && trial == kTrialDual && !force;
+    auto pos_at = [&](int b, float lfs) -> Pos<Real> {
         if constexpr (sizeof(Real) == 4) {
             const Pos<float> p = load_pos(X, b);
-            return tr ? moved_f(p, n.d, b, s_lf) : p;
+            return tr ? moved_f(p, n.d, b, lfs) : p;
         } else {
             return bead_at(X, n.d, b, tr, s_lam);
         }
     };
+    auto pos = [&](int b) -> Pos<Real> { return pos_at(b, s_lf); };
     const int i = t.begin + threadIdx.x;
-    Real e = 0;
+    Real e = 0, e2 = 0;
     if (i < t.end) {
         if (kind == K_BOUNDARY) {
             const int b = n.bb_bead[i];
@@ -1170,6 +1021,10 @@ __global__ void __launch_bounds__(kBlock) k_bond_bnd(DevNet<Real> n, int want, i
             const Real ex = exp(R);
             if (!force) {
                 e = K * ex;
+                if (dual) {
+                    const Real rr2 = plane_dist_p(pl, pos_at(b, 0.5f * s_lf));
+                    e2 = K * exp(-rr2 / sl);
+                }
             } else {
                 const Real f0 = K * ex / sl;
                 Real* c = slot_ptr(n, n.slot_base[K_BOUNDARY] + i);
@@ -1192,6 +1047,13 @@ __global__ void __launch_bounds__(kBlock) k_bond_bnd(DevNet<Real> n, int want, i
             if (!force) {
                 const Real dd = dist - l0;
                 e = (Real)0.5 * k * dd * dd;
+                if (dual) {
+                    const float lh = 0.5f * s_lf;
+                    Real w[3];
+                    bond_vector(pos_at(bs.x, lh), pos_at(bs.y, lh), pos_at(bs.z, lh), pos_at(bs.w, lh), s1, s2, w);
+                    const Real d2 = sqrt(w[0] * w[0] + w[1] * w[1] + w[2] * w[2]) - l0;
+                    e2 = (Real)0.5 * k * d2 * d2;
+                }
             } else {
                 const Real invL = (Real)1 / dist;
                 const Real f0 = k * (dist - l0) * invL;
@@ -1214,10 +1076,21 @@ __global__ void __launch_bounds__(kBlock) k_bond_bnd(DevNet<Real> n, int want, i
     }
     if (!force) {
         if constexpr (sizeof(Real) == 4) {
-            FF a[1];
-            a[0].h = e;
-            block_reduce_ff<1, 0>(a, nullptr, reinterpret_cast<float*>(sh));
-            if (threadIdx.x == 0) store_pair(n.part_sp + ti, a[0].h, a[0].l);
+            if (dual) {
+                FF a[2];
+                a[0].h = e;
+                a[1].h = e2;
+                block_reduce_ff<2, 0>(a, nullptr, reinterpret_cast<float*>(sh));
+                if (threadIdx.x == 0) {
+                    store_pair(n.part_sp + ti, a[0].h, a[0].l);
+                    store_pair(n.part_sp2 + ti, a[1].h, a[1].l);
+                }
+            } else {
+                FF a[1];
+                a[0].h = e;
+                block_reduce_ff<1, 0>(a, nullptr, reinterpret_cast<float*>(sh));
+                if (threadIdx.x == 0) store_pair(n.part_sp + ti, a[0].h, a[0].l);
+            }
         } else {
             const double se = block_sum_r(e, sh);
             if (threadIdx.x == 0) n.part_sp[ti] = se;
@@ -1230,6 +1103,7 @@ __global__ void __launch_bounds__(kBlock) k_bond_bnd(DevNet<Real> n, int want, i
 // ---------------------------------------------------------------------------
 template <typename Real>
 __global__ void __launch_bounds__(kBlock) k_direction(DevNet<Real> n) {
+    MECH_TRACE_KERNEL(n, TK_DIRECTION);
     __shared__ double sh[32];
     __shared__ int s_go, s_fb, s_xb, s_bk;
     __shared__ double s_beta;
@@ -1262,42 +1136,9 @@ __global__ void __launch_bounds__(kBlock) k_direction(DevNet<Real> n) {
     if (threadIdx.x == 0) n.part_fil[4 * (size_t)blockIdx.x + 3] = sdF;
 }
 
-// One block per replica after the direction update: the slope d.F, the
-// conjugacy test and the next iteration's start (CGMethod.hpp:1553-1560).
-template <typename Real>
-__device__ void finalize_direction(const DevNet<Real>& n, int r, double* sh) {
-    CGState S;
-    if (threadIdx.x == 0) S = n.st[r];
-    const RepTiles rt = n.rt[r];
-    double slope;
-    if constexpr (sizeof(Real) == 8) {
-        slope = sum_slots(n.part_fil, 4, 3, rt.fil_begin, rt.fil_end, sh);
-    } else {
-        FF a[1];
-        const int nslot = run_slots(rt.fil_begin, rt.fil_end, n.ptiles[2]);
-        for (int k = threadIdx.x; k < nslot; k += blockDim.x)
-            add_pair(a[0], load_pair(n.part_fil + 4 * (size_t)run_slot(rt.fil_begin, n.ptiles[2], k) + 3));
-        block_reduce_ff<1, 0>(a, nullptr, reinterpret_cast<float*>(sh));
-        slope = threadIdx.x == 0 ? (double)a[0].h + (double)a[0].l : 0.0;
-    }
-    if (threadIdx.x == 0) {
-        if (S.backupPending) {
-            S.backupValid = 1;
-            S.backupPending = 0;
-        }
-        if (slope <= 0) {          // conjugacy lost: reset to steepest descent
-            S.phase = PH_RESET;
-        } else {
-            S.slope = slope;
-            if (S.method >= 1) S.lastFdotF = S.newGrad;
-            begin_iteration(S);
-        }
-        n.st[r] = S;
-    }
-}
-
 template <typename Real>
 __global__ void __launch_bounds__(kBlock) k_finalize_direction(DevNet<Real> n) {
+    MECH_TRACE_KERNEL(n, TK_FIN_DIRECTION);
     __shared__ double sh[32];
     __shared__ int s_flag;
     const int r = blockIdx.x;
@@ -1310,6 +1151,7 @@ __global__ void __launch_bounds__(kBlock) k_finalize_direction(DevNet<Real> n) {
 // replica is resetting (it is in every iteration of the graph).
 template <typename Real>
 __global__ void __launch_bounds__(kBlock) k_reset(DevNet<Real> n) {
+    MECH_TRACE_KERNEL(n, TK_RESET);
     __shared__ int s_go[kGatherTiles], s_fb[kGatherTiles], s_flag;
     const int t0 = blockIdx.x * kGatherTiles;
     if (threadIdx.x < kGatherTiles) {
@@ -1373,6 +1215,7 @@ __global__ void k_dispatch_failed(CGState* st, int R, int* misc_count) {
 // Recovery move: step = maxDist / max_i |d_i|, x += step d (MController.h:273-339).
 template <typename Real>
 __global__ void __launch_bounds__(kBlock) k_recover_maxabs(DevNet<Real> n) {
+    MECH_TRACE_KERNEL(n, TK_RECOVER_MAXABS);
     __shared__ double sh[32];
     __shared__ int s_go, s_flag;
     const Tile t = n.ftile[blockIdx.x];
@@ -1407,6 +1250,7 @@ __global__ void __launch_bounds__(kBlock) k_recover_maxabs(DevNet<Real> n) {
 
 template <typename Real>
 __global__ void __launch_bounds__(kBlock) k_recover_move(DevNet<Real> n) {
+    MECH_TRACE_KERNEL(n, TK_RECOVER_MOVE);
     __shared__ int s_go, s_xb, s_flag;
     __shared__ double s_step;
     const Tile t = n.ftile[blockIdx.x];
@@ -1432,6 +1276,7 @@ __global__ void __launch_bounds__(kBlock) k_recover_move(DevNet<Real> n) {
 
 template <typename Real>
 __global__ void __launch_bounds__(kBlock) k_backup_restore(DevNet<Real> n) {
+    MECH_TRACE_KERNEL(n, TK_BACKUP);
     const Tile t = n.ftile[blockIdx.x];
     const CGState& S = n.st[t.replica];
     if (!S.restore) return;
@@ -1562,8 +1407,9 @@ int launch_part(const DevNet<Real>& n, int which, cudaStream_t s) {
             return 3;
         case 2: if (lm + bb_t > 0) { k_bond_bnd<Real><<<lm + bb_t, kBlock, 0, s>>>(n, -1, 0, 0, lm, ev_t); return 1; } return 0;
         case 3: if (lm + bb_t > 0) { k_bond_bnd<Real><<<lm + bb_t, kBlock, 0, s>>>(n, -1, 0, 1, lm, ev_t); return 1; } return 0;
-        case 4:   // filament energy of a line-search trial (positions x + lambda d formed and written)
-            if constexpr (sizeof(Real) == 4) k_fil_energy_bulk<<<n.pgrid[0], kBlock, 0, s>>>(n, -1, 1);
+        case 4:   // filament energy of a line-search pass (positions x + lambda d formed and written;
+                  // mixed: the two-trial pass, lambda and lambda / 2)
+            if constexpr (sizeof(Real) == 4) k_fil_energy_bulk<<<n.pgrid[0], kBlock, 0, s>>>(n, -1, kTrialDual);
             else k_fil_energy<Real><<<n.n_ftiles, kBlock, 0, s>>>(n, -1, 1);
             return 1;
         case 5:   // filament forces alone
@@ -1578,19 +1424,23 @@ int launch_part(const DevNet<Real>& n, int which, cudaStream_t s) {
     return 0;
 }
 
-// Grid of the mixed engine's persistent filament kernels: every SM full.
-int persistent_blocks(int device, int which) {
-    static int cached_dev = -1, cached[3] = {0, 0, 0};
+// Grid of the mixed engine's persistent filament kernels: every SM holding as
+// many blocks as fit, or at most `per_sm` of them (leaving room on each SM for
+// the kernels of the other lanes).
+int persistent_blocks(int device, int which, int per_sm) {
+    static int cached_dev = -1, sms = 0, occ[3] = {0, 0, 0};
     if (cached_dev != device) {
-        int sms = 0, b[3] = {0, 0, 0};
+        int b[3] = {0, 0, 0};
         cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, device);
         cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b[0], k_fil_energy_bulk, kBlock, 0);
         cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b[1], k_fil_force_bulk, kBlock, 0);
         cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b[2], k_direction_mx, kBlock, 0);
-        for (int k = 0; k < 3; ++k) cached[k] = std::max(1, sms) * std::max(1, b[k]);
+        for (int k = 0; k < 3; ++k) occ[k] = std::max(1, b[k]);
+        sms = std::max(1, sms);
         cached_dev = device;
     }
-    return cached[which];
+    const int per = per_sm > 0 ? std::min(per_sm, occ[which]) : occ[which];
+    return sms * per;
 }
 
 #define MECH_INSTANTIATE(R)                                                             \

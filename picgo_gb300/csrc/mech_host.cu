@@ -7,6 +7,7 @@
 #include <chrono>
 #include <cmath>
 #include <cstdio>
+#include <cstdlib>
 #include <cstring>
 #include <limits>
 #include <map>
@@ -48,6 +49,9 @@ struct ReplicaHost {
     double rmax = 0, bcut = 0;
     // set by the last rebuild
     long long nev = 0, ev_begin = 0, nbb = 0, bb_begin = 0, nbcyl = 0;
+    long long bq_begin = 0;    // first boundary-list entry (plane, cylinder) of this replica
+    std::vector<int> fil_end_cyl;   // per filament: first and last cylinder (replica-local)
+    std::vector<int> fil_type;      // per filament: type of its cylinders
     double cell = 0;
     int gx = 1, gy = 1, gz = 1;
     long long cell_off = 0;
@@ -66,11 +70,11 @@ struct MechContext {
     Lanes lanes() const { return Lanes{stream, side, side2, fork, join, join2}; }
     int R = 0;
     int nb = 0, ncyl = 0, nlk = 0, nmt = 0, nplanes = 0;
-    long long nev = 0, nbb = 0;
+    long long nev = 0, nbb = 0, nbcyl = 0;
     std::vector<ReplicaHost> reps;
     bool have_net = false, have_lists = false;
     // beads
-    DeviceBuffer x[2], f[2], d, xbest, xinit, bflag, bpar;
+    DeviceBuffer x[3], f[2], d, xbest, xinit, bflag, bpar;   // x[2]: mixed engine's second trial buffer
     // cylinders
     DeviceBuffer cyl_b1, cyl_id, cyl_fil, cyl_pos, cyl_rep, cyl_minus, cyl_kex, cyl_type, cyl_l0;
     // linkers / motors
@@ -78,9 +82,9 @@ struct MechContext {
     // boundary
     DeviceBuffer planes, plane_k, plane_slen, bb_k, bb_slen;
     // excluded volume
-    DeviceBuffer ev_bead, ev_k, ev_la, ev_lb, ev_list, ev_list_count, ev_energy;
+    DeviceBuffer ev_bead, ev_k, ev_la, ev_lb, ev_list, ev_list_count, ev_energy, ev_energy2;
     // tiles, partials, state
-    DeviceBuffer ftile, stile, stile_kind, rt, part_fil, part_sp, st, ticket, gticket, err, cond_counter;
+    DeviceBuffer ftile, stile, stile_kind, rt, part_fil, part_sp, part_sp2, st, ticket, gticket, err, cond_counter;
     int graph_mode = MECH_GRAPH_UNROLLED;
     DeviceBuffer contrib, ev_fb_count, ev_fb_list, ev_fb_energy, fb_moments, fb_tickets;
     // rebuild scratch
@@ -104,6 +108,9 @@ struct MechContext {
     // tuning (mech_autotune): tiles per block of the mixed filament energy and
     // force kernels, and a multiplier on the default neighbor-list bin edge
     int tile_cap[2] = {kFilBulkMaxTiles, kFilBulkMaxTiles};
+    // resident blocks per SM of the persistent filament energy / force kernels
+    // (0: as many as fit); fewer leave room for the lanes running beside them
+    int blocks_per_sm[2] = {0, 0};
     double cell_scale = 1.0;
     int sp_tiles_c[K_NUM_SPARSE] = {0, 0, 0, 0};
     int slot_base[K_NUM_SPARSE + 1] = {0, 0, 0, 0, 0};
@@ -118,6 +125,9 @@ struct MechContext {
         cudaEvent_t done = nullptr;
     } snap[2];
     MechTiming timing{};
+#ifdef MECH_TRACE
+    DeviceBuffer trace;   // kernel timeline of the diagnostic build (MECH_TRACE_FILE names the dump)
+#endif
     std::vector<int32_t> cyl_local_first;   // replica-local cylinder -> internal global first bead
 
     ~MechContext() {
@@ -153,6 +163,7 @@ DevNet<Real> make_devnet(MechContext* c) {
     n.R = c->R;
     n.x[0] = c->x[0].as<Real>();
     n.x[1] = c->x[1].as<Real>();
+    n.x[2] = c->x[2].as<Real>();
     n.f[0] = c->f[0].as<Real>();
     n.f[1] = c->f[1].as<Real>();
     n.d = c->d.as<Real>();
@@ -160,12 +171,13 @@ DevNet<Real> make_devnet(MechContext* c) {
     n.ev_list = c->ev_list.as<int>();
     n.ev_list_count = c->ev_list_count.as<int>();
     n.ev_energy = c->ev_energy.as<double>();
+    n.ev_energy2 = c->ev_energy2.as<double>();
     n.bflag = c->bflag.as<uint8_t>();
     n.bpar = c->bpar.as<Real>();
     n.n_ftiles = c->compact ? c->n_ftiles_c : c->n_ftiles;
     n.ftile = (c->compact ? c->ftile_c : c->ftile).as<Tile>();
     for (int k = 0; k < 3; ++k) {
-        n.pgrid[k] = std::max(1, std::min(n.n_ftiles, persistent_blocks(c->device, k)));
+        n.pgrid[k] = std::max(1, std::min(n.n_ftiles, persistent_blocks(c->device, k, k < 2 ? c->blocks_per_sm[k] : 0)));
         n.ptiles[k] = (n.n_ftiles + n.pgrid[k] - 1) / n.pgrid[k];
         // the bulk-staged energy/force kernels keep a block's tile descriptors in shared memory
         if (k < 2) n.ptiles[k] = std::max(1, std::min(n.ptiles[k], c->tile_cap[k]));
@@ -212,11 +224,15 @@ DevNet<Real> make_devnet(MechContext* c) {
     n.fb_tickets = c->fb_tickets.as<int>();
     n.part_fil = c->part_fil.as<double>();
     n.part_sp = c->part_sp.as<double>();
+    n.part_sp2 = c->part_sp2.as<double>();
     n.st = c->st.as<CGState>();
     n.rt = (c->compact ? c->rt_c : c->rt).as<RepTiles>();
     n.ticket = c->ticket.as<int>();
     n.gticket = c->gticket.as<int>();
     n.err = c->err.as<unsigned>();
+#ifdef MECH_TRACE
+    n.trace = c->trace.as<unsigned long long>();
+#endif
     return n;
 }
 
@@ -286,6 +302,83 @@ __global__ void k_gather_pos(const Real* X, const int* perm, int nb, int base, d
     out[3 * (size_t)i + 2] = v[2];
 }
 
+// Boundary load forces of one replica's filament ends (one thread per filament,
+// end and monomer), planes in order as ForceFieldManager::computeLoadForces
+// visits them (ForceFieldManager.cpp:292-311, BoundaryCylinderRepulsion.cpp:122-192,
+// BoundaryCylinderRepulsionExp.cpp:113-118).  ends[2 f] / ends[2 f + 1]: the
+// filament's first (minus-end) and last (plus-end) cylinder, replica-local.
+struct LoadForceArgs {
+    const int* ends;           // [2 * nfil]
+    const int* fil_type;       // [nfil]
+    const double* mon_size;    // per filament type
+    const int* n_mon;          // per filament type
+    int ntypes, nfil, stride;
+    const int* cyl_b1;         // internal first bead of each (global) cylinder
+    int cyl_begin, ncyl;
+    const int* bcnt;           // boundary list entry counts of the last rebuild, replica's first entry
+    int nplanes;
+    const double* planes;      // replica's planes (a, b, c, d)
+    const double* plane_k;
+    const double* plane_slen;
+    double* out;               // [nfil][2][stride]: minus end, then plus end
+};
+template <typename Real>
+__global__ void k_load_forces(const Real* X, LoadForceArgs a) {
+    const long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= 2LL * a.nfil * a.stride) return;
+    const int i = (int)(t % a.stride);
+    const int e = (int)((t / a.stride) % 2);      // 0 minus end, 1 plus end
+    const int f = (int)(t / (2LL * a.stride));
+    const int c = a.ends[2 * f + e];
+    const int ty = a.fil_type[f];
+    double load = 0.0;
+    if (ty >= 0 && ty < a.ntypes && i < a.n_mon[ty] && c >= 0 && c < a.ncyl) {
+        const int b1 = a.cyl_b1[a.cyl_begin + c];
+        double p1[3], p2[3];
+        to_double(load_pos(X, b1), p1);
+        to_double(load_pos(X, b1 + 1), p2);
+        const double* bo = e ? p1 : p2;
+        const double* bd = e ? p2 : p1;
+        double dir[3] = {bd[0] - bo[0], bd[1] - bo[1], bd[2] - bo[2]};
+        double m2 = 0.0;
+        for (int k = 0; k < 3; ++k) m2 = __dadd_rn(m2, __dmul_rn(dir[k], dir[k]));
+        const double nrm = __dsqrt_rn(m2);
+        for (int k = 0; k < 3; ++k) dir[k] = __ddiv_rn(dir[k], nrm);
+        const double step = __dmul_rn((double)i, a.mon_size[ty]);
+        double x[3];
+        for (int k = 0; k < 3; ++k) x[k] = __dadd_rn(bd[k], __dmul_rn(step, dir[k]));
+        for (int p = 0; p < a.nplanes; ++p) {
+            if (!a.bcnt[(long long)p * a.ncyl + c]) continue;
+            const double* pl = a.planes + 4 * p;
+            double dn = 0.0;
+            for (int k = 0; k < 3; ++k) dn = __dadd_rn(dn, __dmul_rn(pl[k], dir[k]));
+            const double proj = fmax(-dn, 0.0);
+            double num = __dmul_rn(pl[0], x[0]);
+            num = __dadd_rn(num, __dmul_rn(pl[1], x[1]));
+            num = __dadd_rn(num, __dmul_rn(pl[2], x[2]));
+            num = __dadd_rn(num, pl[3]);
+            const double den = __dsqrt_rn(__dadd_rn(__dadd_rn(__dmul_rn(pl[0], pl[0]), __dmul_rn(pl[1], pl[1])),
+                                                   __dmul_rn(pl[2], pl[2])));
+            const double R = __ddiv_rn(-__ddiv_rn(num, den), a.plane_slen[p]);
+            const double lf = __ddiv_rn(__dmul_rn(a.plane_k[p], exp(R)), a.plane_slen[p]);
+            load = __dadd_rn(load, __dmul_rn(proj, lf));
+        }
+    }
+    a.out[t] = load;
+}
+
+// Per-cylinder view of the per-bead filament energy terms the energy kernels
+// stored (stretching of cylinder c, bending of the triple centred on its first
+// bead; zero for a filament's first cylinder).
+__global__ void k_terms_by_cylinder(const double* terms, int nb, const int* cyl_b1, int cyl_begin, int ncyl,
+                                    double* stretch, double* bend) {
+    const int c = blockIdx.x * blockDim.x + threadIdx.x;
+    if (c >= ncyl) return;
+    const int b = cyl_b1[cyl_begin + c];
+    stretch[c] = terms[b];
+    bend[c] = terms[(size_t)nb + b];
+}
+
 template <typename Real>
 __global__ void k_gather_coords(const Real* in, const int* perm, int nb, int base, double* out) {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
@@ -348,6 +441,13 @@ static int set_networks(MechContext* c, int R, const MechNetwork* nets) {
         h.ncyl = N.n_cylinders;
         h.cyl_begin = ncyl;
         h.nfil = N.n_filaments;
+        h.fil_end_cyl.resize(2 * (size_t)N.n_filaments);
+        h.fil_type.resize(N.n_filaments);
+        for (int f = 0; f < N.n_filaments; ++f) {
+            h.fil_end_cyl[2 * (size_t)f] = N.fil_cyl_start[f];
+            h.fil_end_cyl[2 * (size_t)f + 1] = N.fil_cyl_start[f + 1] - 1;
+            h.fil_type[f] = N.cyl_type && N.fil_cyl_start[f + 1] > N.fil_cyl_start[f] ? N.cyl_type[N.fil_cyl_start[f]] : 0;
+        }
         h.perm.assign(N.n_beads, -1);
         h.inv.assign(N.n_beads, -1);
         for (int k = 0; k < 3; ++k) h.box[k] = N.box[k];
@@ -485,6 +585,10 @@ static int set_networks(MechContext* c, int R, const MechNetwork* nets) {
     }
     CU(c->x[1].ensure(sizeof(double) * x.size() + kBulkPad));
     CU(cudaMemcpyAsync(c->x[1].p, c->x[0].p, sizeof(double) * x.size(), cudaMemcpyDeviceToDevice, s));
+    if (c->precision == MECH_PREC_MIXED) {   // the second trial buffer of the two-trial line-search passes
+        CU(c->x[2].ensure(sizeof(double) * x.size() + kBulkPad));
+        CU(cudaMemcpyAsync(c->x[2].p, c->x[0].p, sizeof(double) * x.size(), cudaMemcpyDeviceToDevice, s));
+    }
     CU(c->xbest.ensure(sizeof(double) * x.size()));
     CU(c->xinit.ensure(sizeof(double) * x.size()));
     CU(cudaMemcpyAsync(c->xinit.p, c->x[0].p, sizeof(double) * x.size(), cudaMemcpyDeviceToDevice, s));
@@ -573,7 +677,7 @@ static int set_networks(MechContext* c, int R, const MechNetwork* nets) {
 // neighbor lists
 // ===========================================================================
 // Bring every replica's current coordinates to x[0] (a replica whose last
-// accepted step left them in x[1] is copied back) and reset its xbuf.
+// accepted step left them in a trial buffer is copied back) and reset its xbuf.
 static int canonicalize_x(MechContext* c) {
     cudaStream_t s = c->stream;
     CU(cudaMemcpyAsync(c->h_st, c->st.p, sizeof(CGState) * c->R, cudaMemcpyDeviceToHost, s));
@@ -582,7 +686,8 @@ static int canonicalize_x(MechContext* c) {
     for (int r = 0; r < c->R; ++r) {
         if (c->h_st[r].xbuf) {
             const ReplicaHost& h = c->reps[r];
-            CU(cudaMemcpyAsync(c->x[0].as<char>() + 24 * (size_t)h.bead_begin, c->x[1].as<char>() + 24 * (size_t)h.bead_begin,
+            CU(cudaMemcpyAsync(c->x[0].as<char>() + 24 * (size_t)h.bead_begin,
+                               c->x[c->h_st[r].xbuf].as<char>() + 24 * (size_t)h.bead_begin,
                                24 * (size_t)h.nb, cudaMemcpyDeviceToDevice, s));
             c->h_st[r].xbuf = 0;
             moved = true;
@@ -684,8 +789,10 @@ static int rebuild(MechContext* c, double cell_req, MechListInfo* info) {
     CU(c->ev_k.ensure(rs * std::max<long long>(P, 1)));
     CU(c->ev_la.ensure(rs * std::max<long long>(P, 1)));
     CU(c->ev_lb.ensure(rs * std::max<long long>(P, 1)));
-    CU(c->ev_list.ensure(sizeof(int) * 2 * std::max<long long>(P, 1)));
+    // the extended-pass list holds up to two entries per pair (both trials of a two-trial pass)
+    CU(c->ev_list.ensure(sizeof(int) * 4 * std::max<long long>(P, 1)));
     CU(c->ev_energy.ensure(sizeof(double) * std::max<long long>(P, 1)));
+    CU(c->ev_energy2.ensure(sizeof(double) * std::max<long long>(P, 1)));
     CU(c->ev_list_count.ensure(sizeof(int) * 4));
     CU(cudaMemsetAsync(c->ev_list_count.p, 0, sizeof(int) * 4, s));
     if (P > 0) {
@@ -725,9 +832,11 @@ static int rebuild(MechContext* c, double cell_req, MechListInfo* info) {
         bi.planes = c->planes.as<double>();
         bi.cyl_b1 = c->cyl_b1.as<int>();
         bi.cyl_minus = c->cyl_minus.as<uint8_t>();
-        long long nbb = 0;
-        CU(build_boundary(bi, c->pb.mid.as<double>(), c->bbuild, &nbb, s));
+        long long nbb = 0, nbcyl = 0;
+        CU(build_boundary(bi, c->pb.mid.as<double>(), c->bbuild, &nbb, &nbcyl, s));
         c->nbb = nbb;
+        c->nbcyl = nbcyl;
+        for (int r = 0; r < R; ++r) c->reps[r].bq_begin = rq[r];
         std::vector<long long> idx(R + 1);
         for (int r = 0; r < R; ++r) idx[r] = rq[r];
         idx[R] = nq;
@@ -782,6 +891,7 @@ static int rebuild(MechContext* c, double cell_req, MechListInfo* info) {
         if ((rc = upload(c->stile, st, s)) || (rc = upload(c->stile_kind, kind, s)) || (rc = upload(c->rt, c->h_rt, s)))
             return rc;
         CU(c->part_sp.ensure(sizeof(double) * std::max<size_t>(st.size(), 1)));
+        CU(c->part_sp2.ensure(sizeof(double) * std::max<size_t>(st.size(), 1)));
     }
     // contribution slots and the gather index
     c->slot_base[K_LINKER] = 0;
@@ -807,7 +917,7 @@ static int rebuild(MechContext* c, double cell_req, MechListInfo* info) {
     if (info) {
         info->n_exvol_pairs = P;
         info->n_boundary_beads = c->nbb;
-        info->n_boundary_cyl = 0;
+        info->n_boundary_cyl = c->nbcyl;
         info->cell_size = c->reps[0].cell;
         info->n_cells = ncells;
     }
@@ -864,7 +974,13 @@ static int eval_forces(MechContext* c, int replica) {
 }
 
 static constexpr int kBlocksPerGraph = 8;
-static constexpr int kTrialsPerBlock = 2;
+// Line-search launches per iteration block: FP64, two single-trial passes;
+// mixed, one two-trial pass (lambda and lambda / 2).
+template <typename Real>
+static int trial_launches(const DevNet<Real>& n, const Lanes& L) {
+    if constexpr (sizeof(Real) == 4) return launch_energy<Real>(n, PH_LS_TRIAL, kTrialDual, L);
+    return launch_energy<Real>(n, PH_LS_TRIAL, 1, L) + launch_energy<Real>(n, PH_LS_TRIAL, 1, L);
+}
 
 template <typename Real>
 static int capture_iteration_graph(MechContext* c, cudaGraphExec_t* exec, int* nlaunch) {
@@ -873,7 +989,7 @@ static int capture_iteration_graph(MechContext* c, cudaGraphExec_t* exec, int* n
     CU(cudaStreamBeginCapture(c->stream, cudaStreamCaptureModeThreadLocal));
     int k = 0;
     for (int b = 0; b < kBlocksPerGraph; ++b) {
-        for (int t = 0; t < kTrialsPerBlock; ++t) k += launch_energy<Real>(n, PH_LS_TRIAL, 1, c->lanes());
+        k += trial_launches<Real>(n, c->lanes());
         k += launch_forces<Real>(n, PH_FORCE, c->lanes());
         k += launch_direction<Real>(n, c->stream);
         k += launch_dispatch_failed<Real>(n, c->stream);
@@ -881,7 +997,7 @@ static int capture_iteration_graph(MechContext* c, cudaGraphExec_t* exec, int* n
     }
     cudaError_t e = cudaStreamEndCapture(c->stream, &g);
     if (e != cudaSuccess) return set_err(MECH_ERR_CUDA, std::string("graph capture: ") + cudaGetErrorString(e));
-    e = cudaGraphInstantiate(exec, g, 0);
+    e = cudaGraphInstantiate(exec, g, cudaGraphInstantiateFlagUseNodePriority);
     cudaGraphDestroy(g);
     if (e != cudaSuccess) return set_err(MECH_ERR_CUDA, std::string("graph instantiate: ") + cudaGetErrorString(e));
     *nlaunch = k;
@@ -962,7 +1078,9 @@ static int capture_conditional_graph(MechContext* c, cudaGraphExec_t* exec, Cond
         prev = node;
         return capture_into(ip.conditional.phGraph_out[0], nullptr, fn);
     };
-    if ((e = add_if(h[0], [&] { counts->trial = launch_energy<Real>(n, PH_LS_TRIAL, 1, c->lanes()); })) != cudaSuccess)
+    if ((e = add_if(h[0], [&] {
+             counts->trial = launch_energy<Real>(n, PH_LS_TRIAL, sizeof(Real) == 4 ? kTrialDual : 1, c->lanes());
+         })) != cudaSuccess)
         return fail(e, "trial body");
     if ((e = add_if(h[1], [&] { counts->force = launch_forces<Real>(n, PH_FORCE, c->lanes()); })) != cudaSuccess)
         return fail(e, "force body");
@@ -973,7 +1091,7 @@ static int capture_conditional_graph(MechContext* c, cudaGraphExec_t* exec, Cond
              counts->misc += launch_reset<Real>(n, c->stream);
          })) != cudaSuccess)
         return fail(e, "dispatch body");
-    e = cudaGraphInstantiate(exec, g, 0);
+    e = cudaGraphInstantiate(exec, g, cudaGraphInstantiateFlagUseNodePriority);
     cudaGraphDestroy(g);
     g = nullptr;
     if (e != cudaSuccess) return set_err(MECH_ERR_CUDA, std::string("conditional graph, instantiate: ") + cudaGetErrorString(e));
@@ -1377,6 +1495,115 @@ int32_t mech_get_pairs(MechContext* ctx, int32_t r, int32_t* pairs, int64_t cap,
     return MECH_OK;
 }
 
+int32_t mech_get_boundary_list(MechContext* ctx, int32_t r, int32_t* entries, int64_t cap, int64_t* count) {
+    int rc = check_replica(ctx, r);
+    if (rc) return rc;
+    if (!ctx->have_lists) return set_err(MECH_ERR_STATE, "no lists");
+    const ReplicaHost& h = ctx->reps[r];
+    const long long nq = (long long)h.nplanes * h.ncyl;
+    std::vector<int> cnt((size_t)std::max(nq, 1LL));
+    if (nq > 0)
+        CU(cudaMemcpy(cnt.data(), ctx->bbuild.cnt.as<int>() + h.bq_begin, sizeof(int) * nq, cudaMemcpyDeviceToHost));
+    long long k = 0;
+    for (long long q = 0; q < nq; ++q) {
+        if (!cnt[q]) continue;
+        if (entries && k < cap) {
+            entries[2 * k] = (int32_t)(q / h.ncyl);
+            entries[2 * k + 1] = (int32_t)(q % h.ncyl);
+        }
+        ++k;
+    }
+    if (count) *count = k;
+    return MECH_OK;
+}
+
+int32_t mech_load_forces(MechContext* ctx, int32_t r, int32_t n_types, const double* mon_size, const int32_t* n_mon,
+                         int32_t stride, double* plus, double* minus) {
+    int rc = check_replica(ctx, r);
+    if (rc) return rc;
+    if (n_types < 1 || !mon_size || !n_mon || stride < 1 || !plus || !minus)
+        return set_err(MECH_ERR_ARG, "mech_load_forces: bad argument");
+    if (!ctx->have_lists) return set_err(MECH_ERR_STATE, "no lists");
+    CU(cudaSetDevice(ctx->device));
+    if ((rc = pull_states(ctx))) return rc;
+    const ReplicaHost& h = ctx->reps[r];
+    const size_t nout = 2 * (size_t)h.nfil * (size_t)stride;
+    DeviceBuffer ends, types, ms, nm, out;
+    cudaStream_t s = ctx->stream;
+    if ((rc = upload(ends, h.fil_end_cyl, s)) || (rc = upload(types, h.fil_type, s))) return rc;
+    if ((rc = upload(ms, std::vector<double>(mon_size, mon_size + n_types), s)) ||
+        (rc = upload(nm, std::vector<int>(n_mon, n_mon + n_types), s)))
+        return rc;
+    CU(out.ensure(sizeof(double) * nout));
+    LoadForceArgs a{};
+    a.ends = ends.as<int>();
+    a.fil_type = types.as<int>();
+    a.mon_size = ms.as<double>();
+    a.n_mon = nm.as<int>();
+    a.ntypes = n_types;
+    a.nfil = h.nfil;
+    a.stride = stride;
+    a.cyl_b1 = ctx->cyl_b1.as<int>();
+    a.cyl_begin = h.cyl_begin;
+    a.ncyl = h.ncyl;
+    a.bcnt = ctx->bbuild.cnt.as<int>() + h.bq_begin;
+    a.nplanes = h.nplanes;
+    a.planes = ctx->planes.as<double>() + 4 * (size_t)h.plane_begin;
+    a.plane_k = ctx->plane_k.as<double>() + h.plane_begin;
+    a.plane_slen = ctx->plane_slen.as<double>() + h.plane_begin;
+    a.out = out.as<double>();
+    const void* X = ctx->x[ctx->h_st[r].xbuf].p;
+    const unsigned nblk = (unsigned)((nout + 255) / 256);
+    if (ctx->precision == MECH_PREC_FP64) k_load_forces<double><<<nblk, 256, 0, s>>>((const double*)X, a);
+    else k_load_forces<float><<<nblk, 256, 0, s>>>((const float*)X, a);
+    CU(cudaGetLastError());
+    std::vector<double> hout(nout);
+    CU(cudaMemcpyAsync(hout.data(), out.p, sizeof(double) * nout, cudaMemcpyDeviceToHost, s));
+    CU(cudaStreamSynchronize(s));
+    for (int f = 0; f < h.nfil; ++f)
+        for (int i = 0; i < stride; ++i) {
+            minus[(size_t)f * stride + i] = hout[(2 * (size_t)f) * stride + i];
+            plus[(size_t)f * stride + i] = hout[(2 * (size_t)f + 1) * stride + i];
+        }
+    return MECH_OK;
+}
+
+int32_t mech_energy_terms(MechContext* ctx, int32_t r, double* stretch, double* bend) {
+    int rc = check_replica(ctx, r);
+    if (rc) return rc;
+    if (!stretch || !bend) return set_err(MECH_ERR_ARG, "null output");
+    if (!ctx->have_lists && (rc = rebuild(ctx, 0.0, nullptr))) return rc;
+    CU(cudaSetDevice(ctx->device));
+    if ((rc = pull_states(ctx))) return rc;
+    for (int q = 0; q < ctx->R; ++q) ctx->h_st[q].active = (q == r);
+    if ((rc = push_states(ctx))) return rc;
+    const ReplicaHost& h = ctx->reps[r];
+    DeviceBuffer terms, out;
+    CU(terms.ensure(sizeof(double) * 2 * (size_t)ctx->nb));
+    CU(out.ensure(sizeof(double) * 2 * (size_t)h.ncyl));
+    cudaStream_t s = ctx->stream;
+    CU(cudaMemsetAsync(terms.p, 0, sizeof(double) * 2 * (size_t)ctx->nb, s));
+    // the filament energy kernel of a plain evaluation, storing its terms
+    if (ctx->precision == MECH_PREC_FP64) {
+        DevNet<double> n = make_devnet<double>(ctx);
+        n.terms = terms.as<double>();
+        launch_part<double>(n, 0, s);
+    } else {
+        DevNet<float> n = make_devnet<float>(ctx);
+        n.terms = terms.as<double>();
+        launch_part<float>(n, 0, s);
+    }
+    const unsigned nblk = (unsigned)((h.ncyl + 255) / 256);
+    double* o = out.as<double>();
+    k_terms_by_cylinder<<<nblk, 256, 0, s>>>(terms.as<double>(), ctx->nb, ctx->cyl_b1.as<int>(), h.cyl_begin, h.ncyl,
+                                            o, o + h.ncyl);
+    CU(cudaGetLastError());
+    CU(cudaMemcpyAsync(stretch, o, sizeof(double) * h.ncyl, cudaMemcpyDeviceToHost, s));
+    CU(cudaMemcpyAsync(bend, o + h.ncyl, sizeof(double) * h.ncyl, cudaMemcpyDeviceToHost, s));
+    CU(cudaStreamSynchronize(s));
+    return MECH_OK;
+}
+
 int32_t mech_energy(MechContext* ctx, int32_t r, const double* coord, double* per_ff, double* total, double* energy) {
     int rc = check_replica(ctx, r);
     if (rc) return rc;
@@ -1409,8 +1636,37 @@ int32_t mech_minimize(MechContext* ctx, const MechCGParams* params, MechResult* 
     if (!ctx->have_net) return set_err(MECH_ERR_STATE, "no network");
     if (params->method < 0 || params->method > 2) return set_err(MECH_ERR_ARG, "bad method");
     CU(cudaSetDevice(ctx->device));
+#ifdef MECH_TRACE
+    // diagnostic build: every block of every kernel of this minimization appends
+    // (start, end, kernel, block) records; written to $MECH_TRACE_FILE at the end
+    const char* tf = std::getenv("MECH_TRACE_FILE");
+    if (tf) {
+        const unsigned long long cap = 16ull << 20;
+        CU(ctx->trace.ensure(sizeof(unsigned long long) * (2 + 3 * cap)));
+        const unsigned long long hdr[2] = {0ull, cap};
+        CU(cudaMemcpy(ctx->trace.p, hdr, sizeof(hdr), cudaMemcpyHostToDevice));
+    }
+    const int trc = ctx->precision == MECH_PREC_FP64 ? minimize_impl<double>(ctx, params, results)
+                                            : minimize_impl<float>(ctx, params, results);
+    if (tf) {
+        cudaDeviceSynchronize();
+        unsigned long long hdr[2] = {0, 0};
+        cudaMemcpy(hdr, ctx->trace.p, sizeof(hdr), cudaMemcpyDeviceToHost);
+        const unsigned long long nrec = std::min(hdr[0], hdr[1]);
+        std::vector<unsigned long long> rec(3 * nrec);
+        if (nrec) cudaMemcpy(rec.data(), ctx->trace.as<unsigned long long>() + 2, sizeof(unsigned long long) * 3 * nrec,
+                             cudaMemcpyDeviceToHost);
+        if (FILE* fh = std::fopen(tf, "wb")) {
+            std::fwrite(rec.data(), sizeof(unsigned long long), rec.size(), fh);
+            std::fclose(fh);
+        }
+        ctx->trace.release();
+    }
+    return trc;
+#else
     return ctx->precision == MECH_PREC_FP64 ? minimize_impl<double>(ctx, params, results)
                                             : minimize_impl<float>(ctx, params, results);
+#endif
 }
 
 int32_t mech_get_stretch_forces(MechContext* ctx, int32_t r, double* linker_f, double* motor_f) {
@@ -1470,7 +1726,7 @@ static int profile_impl(MechContext* c, int iters, MechProfile* o) {
             fn();
             e = cudaStreamEndCapture(s, &g);
         }
-        if (e == cudaSuccess) e = cudaGraphInstantiate(&ge, g, 0);
+        if (e == cudaSuccess) e = cudaGraphInstantiate(&ge, g, cudaGraphInstantiateFlagUseNodePriority);
         float ms = 0.f;
         if (e == cudaSuccess) e = cudaGraphLaunch(ge, s);   // warm
         if (e == cudaSuccess) {
@@ -1510,13 +1766,13 @@ static int profile_impl(MechContext* c, int iters, MechProfile* o) {
     if (c->ev_list_count.p) CU(cudaMemsetAsync(c->ev_list_count.p, 0, 4 * sizeof(int), s));
     CU(cudaMemsetAsync(n.ev_fb_count, 0, sizeof(int), s));
     // a line-search trial: positions x + lambda d formed and materialized on the fly
-    o->ms_trial_energy_eval = timeit([&] { launch_energy<Real>(n, -1, 1, c->lanes()); });
+    o->ms_trial_energy_eval = timeit([&] { launch_energy<Real>(n, -1, sizeof(Real) == 4 ? kTrialDual : 1, c->lanes()); });
     // every replica finished: each launch of an iteration block reads its phase and exits
     const std::vector<CGState> saved(c->h_st, c->h_st + c->R);
     for (int r = 0; r < c->R; ++r) c->h_st[r].phase = PH_DONE;
     if ((rc = push_states(c))) return rc;
     o->ms_iteration_idle = timeit([&] {
-        for (int t = 0; t < kTrialsPerBlock; ++t) launch_energy<Real>(n, PH_LS_TRIAL, 1, c->lanes());
+        trial_launches<Real>(n, c->lanes());
         launch_forces<Real>(n, PH_FORCE, c->lanes());
         launch_direction<Real>(n, s);
         launch_dispatch_failed<Real>(n, s);
@@ -1570,6 +1826,8 @@ static int autotune_impl(MechContext* c, int flags, MechTuning* out) {
             *out = it->second;
             c->tile_cap[0] = out->energy_tiles_per_block;
             c->tile_cap[1] = out->force_tiles_per_block;
+            c->blocks_per_sm[0] = out->energy_blocks_per_sm;
+            c->blocks_per_sm[1] = out->force_blocks_per_sm;
             c->cell_scale = out->cell_scale;
             return MECH_OK;
         }
@@ -1577,6 +1835,8 @@ static int autotune_impl(MechContext* c, int flags, MechTuning* out) {
     MechTuning t{};
     t.energy_tiles_per_block = c->tile_cap[0];
     t.force_tiles_per_block = c->tile_cap[1];
+    t.energy_blocks_per_sm = c->blocks_per_sm[0];
+    t.force_blocks_per_sm = c->blocks_per_sm[1];
     t.cell_scale = c->cell_scale;
     cudaStream_t s = c->stream;
     if ((rc = pull_states(c))) return rc;
@@ -1921,6 +2181,8 @@ int32_t mech_set_tuning(MechContext* ctx, const MechTuning* t) {
         return set_err(MECH_ERR_ARG, "tuning out of range");
     ctx->tile_cap[0] = t->energy_tiles_per_block;
     ctx->tile_cap[1] = t->force_tiles_per_block;
+    ctx->blocks_per_sm[0] = std::max(0, t->energy_blocks_per_sm);
+    ctx->blocks_per_sm[1] = std::max(0, t->force_blocks_per_sm);
     ctx->cell_scale = t->cell_scale;
     return MECH_OK;
 }

@@ -34,6 +34,13 @@ constexpr int kSparseTile = 256;  // interactions per sparse tile (one block)
 constexpr int kFilBulkMaxTiles = 64;   // filament tiles per block of the bulk-staged mixed kernels
 constexpr int kExvolFallbackCap = 4096;
 constexpr int kFbChunks = 64;       // work split of one numeric force fallback
+// `trial` argument of the evaluation kernels: 0 plain evaluation at x, 1 one
+// line-search trial at x + lambda d, 2 (mixed engine) two trials in one pass,
+// at x + lambda d and at x + (lambda / 2) d, the next step of the backtracking
+// search, with the second trial's energies in their own partial slots
+constexpr int kTrialDual = 2;
+// the ext-pass list marks entries of the second trial with this bit of the pair index
+constexpr int kExtSecond = 1 << 30;
 
 enum Kind : int { K_LINKER = 0, K_MOTOR = 1, K_EXVOL = 2, K_BOUNDARY = 3, K_NUM_SPARSE = 4 };
 
@@ -118,7 +125,10 @@ template <typename Real>
 struct DevNet {
     int nb;                 // beads, all replicas
     int R;
-    Real* x[2];             // positions: double[3] per bead (FP64) or float hi[3], lo[3] per bead (mixed)
+    // positions: double[3] per bead (FP64) or float hi[3], lo[3] per bead
+    // (mixed); x[xbuf] is current, the others receive line-search trial
+    // positions (FP64: one trial buffer; mixed: two, for lambda and lambda / 2)
+    Real* x[3];
     Real* f[2];
     Real* d;
     Real* xbest;
@@ -156,6 +166,9 @@ struct DevNet {
     int* fb_tickets;        // [cap]
     // mixed precision: pairs evaluated in FP64 (compacted list) and per-pair energies
     int* ev_list; int* ev_list_count; double* ev_energy;
+    // mixed-precision line-search passes at lambda and lambda / 2: the second
+    // trial's per-pair excluded-volume energies and sparse tile partials
+    double* ev_energy2; double* part_sp2;
     // partial sums
     double* part_fil;       // [n_ftiles * 4]
     double* part_sp;        // [n_stiles]
@@ -166,7 +179,52 @@ struct DevNet {
     int* gticket;           // whole-grid ticket
     unsigned* err;          // device error word
     GraphConds cond;
+    // diagnostic (mech_energy_terms; null otherwise): the filament energy
+    // kernels also store each bead's stretching [b] and bending [nb + b] term
+    double* terms;
+    // kernel timeline (builds with MECH_TRACE only; null otherwise):
+    // [0] records written, [1] capacity, then (start ns, end ns, kernel << 32 | block) per block
+    unsigned long long* trace;
 };
+
+// Kernel ids of the timeline records.
+enum TraceKernel : unsigned {
+    TK_FIL_ENERGY = 1, TK_FIL_FORCE, TK_GATHER, TK_FIN_FORCE, TK_FIN_ENERGY, TK_FIL_ENERGY_BULK, TK_FIL_FORCE_BULK,
+    TK_DIRECTION_MX, TK_BOND, TK_DIRECTION, TK_FIN_DIRECTION, TK_RESET, TK_RECOVER_MAXABS, TK_RECOVER_MOVE,
+    TK_BACKUP, TK_EXVOL_FB_FORCE, TK_EXVOL, TK_EXVOL_EXT, TK_EXVOL_TAIL, TK_BODY_HEAD, TK_GATHER_MX,
+};
+
+#if defined(__CUDACC__) && defined(MECH_TRACE)
+// Thread 0 of every block appends (start, end, kernel, block) to the timeline
+// when it leaves the kernel's scope.
+struct TraceGuard {
+    unsigned long long* buf;
+    unsigned kid;
+    unsigned long long t0;
+    __device__ static unsigned long long now() {
+        unsigned long long t;
+        asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
+        return t;
+    }
+    __device__ TraceGuard(unsigned long long* b, unsigned k) : buf(b), kid(k), t0(0) {
+        if (buf && threadIdx.x == 0) t0 = now();
+    }
+    __device__ ~TraceGuard() {
+        if (buf && threadIdx.x == 0) {
+            const unsigned long long t1 = now();
+            const unsigned long long i = atomicAdd(buf, 1ull);
+            if (i < buf[1]) {
+                buf[2 + 3 * i] = t0;
+                buf[3 + 3 * i] = t1;
+                buf[4 + 3 * i] = ((unsigned long long)kid << 32) | blockIdx.x;
+            }
+        }
+    }
+};
+#define MECH_TRACE_KERNEL(n, kid) TraceGuard mech_trace_guard_((n).trace, (kid))
+#else
+#define MECH_TRACE_KERNEL(n, kid) ((void)0)
+#endif
 
 #ifdef __CUDACC__
 // Where the contribution of slot `slot` (= slot_base[kind] + interaction * beads + bead) is written.
@@ -204,8 +262,8 @@ template <typename Real> int launch_backup_restore(const DevNet<Real>& n, cudaSt
 // 0 filament energy, 1 filament force, 2 bond/boundary energy, 3 bond/boundary force
 template <typename Real> int launch_part(const DevNet<Real>& n, int which, cudaStream_t s);
 // blocks of the mixed engine's persistent filament kernels on `device`
-// (which: 0 energy, 1 force, 2 direction)
-int persistent_blocks(int device, int which);
+// (which: 0 energy, 1 force, 2 direction), at most per_sm per SM (0: no cap)
+int persistent_blocks(int device, int which, int per_sm);
 
 // Records the text mech_last_error returns on this thread; returns `code`.
 int set_error_text(int code, const std::string& msg);

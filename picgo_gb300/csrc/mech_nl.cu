@@ -289,7 +289,7 @@ __device__ __forceinline__ int rep_of(const BndInput& in, long long q) {
     }
     return lo;
 }
-__global__ void k_bnd_count(BndInput in, const double* mid, int* cnt) {
+__global__ void k_bnd_count(BndInput in, const double* mid, int* cnt, int* ncyl) {
     const long long q = (long long)blockIdx.x * blockDim.x + threadIdx.x;
     if (q >= in.nq) return;
     const int r = rep_of(in, q);
@@ -305,7 +305,10 @@ __global__ void k_bnd_count(BndInput in, const double* mid, int* cnt) {
     num = __dadd_rn(num, pl[3]);
     const double nrm = __dsqrt_rn(__dadd_rn(__dadd_rn(__dmul_rn(pl[0], pl[0]), __dmul_rn(pl[1], pl[1])), __dmul_rn(pl[2], pl[2])));
     const double d = __ddiv_rn(num, nrm);
-    cnt[q] = d < in.cutoff[r] ? (in.cyl_minus[c] ? 2 : 1) : 0;
+    const bool listed = d < in.cutoff[r];
+    cnt[q] = listed ? (in.cyl_minus[c] ? 2 : 1) : 0;
+    const unsigned m = __ballot_sync(__activemask(), listed);
+    if (m && (threadIdx.x & 31) == __ffs(__activemask()) - 1) atomicAdd(ncyl, __popc(m));
 }
 
 __global__ void k_bnd_write(BndInput in, const int* cnt, const int* off, int* bb_bead, int* bb_plane) {
@@ -331,23 +334,28 @@ __global__ void k_bnd_write(BndInput in, const int* cnt, const int* off, int* bb
     }
 }
 
-cudaError_t build_boundary(const BndInput& in, const double* mid, BndBuild& bb, long long* nbeads, cudaStream_t s) {
+cudaError_t build_boundary(const BndInput& in, const double* mid, BndBuild& bb, long long* nbeads, long long* ncyl,
+                           cudaStream_t s) {
     cudaError_t e;
     if ((e = bb.cnt.ensure(sizeof(int) * (size_t)(in.nq + 1))) != cudaSuccess) return e;
     if ((e = bb.off.ensure(sizeof(int) * (size_t)(in.nq + 1))) != cudaSuccess) return e;
+    if ((e = bb.ncyl.ensure(sizeof(int))) != cudaSuccess) return e;
+    if ((e = cudaMemsetAsync(bb.ncyl.p, 0, sizeof(int), s)) != cudaSuccess) return e;
     const int tb = 256;
     const unsigned nblk = (unsigned)((in.nq + tb - 1) / tb);
-    if (in.nq > 0) k_bnd_count<<<nblk, tb, 0, s>>>(in, mid, bb.cnt.as<int>());
+    if (in.nq > 0) k_bnd_count<<<nblk, tb, 0, s>>>(in, mid, bb.cnt.as<int>(), bb.ncyl.as<int>());
     if ((e = exclusive_scan_i32(bb.cnt.as<int>(), bb.off.as<int>(), in.nq, bb.scan_tmp, s)) != cudaSuccess) return e;
-    int total = 0;
+    int total = 0, listed = 0;
     if ((e = cudaMemcpyAsync(&total, bb.off.as<int>() + in.nq, sizeof(int), cudaMemcpyDeviceToHost, s)) != cudaSuccess)
         return e;
+    if ((e = cudaMemcpyAsync(&listed, bb.ncyl.p, sizeof(int), cudaMemcpyDeviceToHost, s)) != cudaSuccess) return e;
     if ((e = cudaStreamSynchronize(s)) != cudaSuccess) return e;
     if ((e = bb.bead.ensure(sizeof(int) * (size_t)(total > 0 ? total : 1))) != cudaSuccess) return e;
     if ((e = bb.plane.ensure(sizeof(int) * (size_t)(total > 0 ? total : 1))) != cudaSuccess) return e;
     if (in.nq > 0 && total > 0)
         k_bnd_write<<<nblk, tb, 0, s>>>(in, bb.cnt.as<int>(), bb.off.as<int>(), bb.bead.as<int>(), bb.plane.as<int>());
     *nbeads = total;
+    *ncyl = listed;
     return cudaGetLastError();
 }
 

@@ -44,10 +44,14 @@ struct BndInput {
 };
 
 struct BndBuild {
-    DeviceBuffer cnt, off, bead, plane, scan_tmp;
+    DeviceBuffer cnt, off, bead, plane, scan_tmp, ncyl;
 };
 
-cudaError_t build_boundary(const BndInput& in, const double* mid, BndBuild& bb, long long* nbeads, cudaStream_t s);
+// cnt[q] (kept until the next rebuild) is 0 for an entry q = (plane, cylinder)
+// outside the list, else the beads it contributes (2 for a minus-end cylinder);
+// *ncyl receives the number of listed (plane, cylinder) entries.
+cudaError_t build_boundary(const BndInput& in, const double* mid, BndBuild& bb, long long* nbeads, long long* ncyl,
+                           cudaStream_t s);
 
 struct CsrInput {
     int nb;

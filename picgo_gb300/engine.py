@@ -116,6 +116,8 @@ class Engine:
         self.nbeads = [n.n_beads for n in nets]
         self.nlinkers = [int(n.lk_cyl.shape[0]) for n in nets]
         self.nmotors = [int(n.mt_cyl.shape[0]) for n in nets]
+        self._nfil = [int(n.n_filaments) for n in nets]
+        self._ncyl = [int(n.n_cyl) for n in nets]
 
     def set_network(self, net) -> None:
         self.set_networks([net])
@@ -141,6 +143,34 @@ class Engine:
         out = np.empty((max(cnt.value, 1), 2), np.int32)
         check(self._L.mech_get_pairs(self._ctx, replica, _ptr(out, _i32p), cnt.value, C.byref(cnt)))
         return out[:cnt.value]
+
+    def boundary_list(self, replica: int = 0) -> np.ndarray:
+        """BoundaryCylinderNL entries (plane, cylinder) of the last rebuild, plane by plane."""
+        cnt = C.c_int64()
+        check(self._L.mech_get_boundary_list(self._ctx, replica, None, 0, C.byref(cnt)))
+        out = np.empty((max(cnt.value, 1), 2), np.int32)
+        check(self._L.mech_get_boundary_list(self._ctx, replica, _ptr(out, _i32p), cnt.value, C.byref(cnt)))
+        return out[:cnt.value]
+
+    def load_forces(self, mon_size=(2.7,), n_mon=(40,), replica: int = 0):
+        """Boundary load forces on the filament ends (plus, minus), each [n_filaments, max n_mon]."""
+        ms = np.ascontiguousarray(mon_size, dtype=np.float64)
+        nm = np.ascontiguousarray(n_mon, dtype=np.int32)
+        nfil = self._nfil[replica]
+        stride = int(nm.max())
+        plus = np.zeros((nfil, stride))
+        minus = np.zeros((nfil, stride))
+        check(self._L.mech_load_forces(self._ctx, replica, len(ms), _ptr(ms, _dp), _ptr(nm, _i32p), stride,
+                                       _ptr(plus, _dp), _ptr(minus, _dp)))
+        return plus, minus
+
+    def energy_terms(self, replica: int = 0):
+        """Per-cylinder stretching and bending energy terms in the engine's arithmetic (before summing)."""
+        n = self._ncyl[replica]
+        st = np.zeros(n)
+        bd = np.zeros(n)
+        check(self._L.mech_energy_terms(self._ctx, replica, _ptr(st, _dp), _ptr(bd, _dp)))
+        return st, bd
 
     # -- evaluation --------------------------------------------------------
     def energies(self, coord: np.ndarray | None = None, replica: int = 0):
