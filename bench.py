@@ -207,6 +207,10 @@ def run_ours(args, rank, world, dist):
     barrier()
     e2e_value = e2e_calls / (sum(e2e_ms) / 1e3)
 
+    # the mixed end state of the last step: coordinates, forces, energy and max |F| as the minimizer reported them
+    end_state = {"coord": eng.coords(), "forces": eng.last_forces(), "energy": r["energies_after"][6],
+                 "max_force": r["grad_inf_norm"], "iterations": r["num_iter"]}
+
     # ---- dominant kernel: per-launch device time with CUDA events on the engine's stream ----
     eng.reset_coords()
     eng.rebuild()
@@ -214,11 +218,13 @@ def run_ours(args, rank, world, dist):
     rs = 4 if args.precision == "mixed" else 8
     nb = prof["n_beads"]
     # Algorithmic bytes per launch (each input read once, each output written once).  The
-    # dominant kernel of a minimization is the filament energy of a line-search trial: it
-    # runs once or twice per iteration and reads positions (24 B), flags (1 B), the four
-    # per-bead constants and the direction, and writes the trial positions (24 B).
+    # dominant kernel of a minimization is the filament energy of a line-search pass: it
+    # reads positions (24 B), flags (1 B), the four per-bead constants and the direction,
+    # and writes the trial positions (24 B per trial: the mixed engine evaluates lambda and
+    # lambda / 2 in one pass, FP64 one trial).
+    trial_writes = 48 if args.precision == "mixed" else 24
     kernels = {
-        "fil_energy_trial": (prof["ms_fil_energy_trial"], nb * (24 + 1 + 4 * rs + 3 * rs + 24)),
+        "fil_energy_trial": (prof["ms_fil_energy_trial"], nb * (24 + 1 + 4 * rs + 3 * rs + trial_writes)),
         "fil_force": (prof["ms_fil_force_kernel"], nb * (24 + 1 + 4 * rs + 3 * rs)),
         "force_gather": (prof["ms_force_gather"],
                          nb * (3 * rs * 3 + 4) + prof["n_slots"] * 3 * rs),
@@ -265,7 +271,46 @@ def run_ours(args, rank, world, dist):
     if dist is not None:
         out["value"] = force_calls_all / (total_ms / 1e3)
     out["value"] = round(out["value"], 2)
-    return out, net
+    return out, net, end_state
+
+
+def mixed_end_state_report(net, end, threads: int):
+    """The mixed minimizer's end state on the 1M-cylinder network, measured against FP64.
+
+    * same coordinates: the GPU FP64 path and the CPU oracle evaluated at the mixed end
+      coordinates with the minimization's own neighbor lists (built once at the start):
+      relative energy difference, largest force-component difference, FP64 max |F|;
+    * FP64 polish: FP64 CG continued from the mixed end state to the same 1 pN tolerance
+      (iterations, relative energy change, bead displacement RMS / max): zero iterations and
+      no change when the mixed end state already is an FP64 equilibrium of that tolerance.
+    """
+    import numpy as np
+    import oracle
+    from picgo_gb300 import Engine
+    x_m, f_m = end["coord"], end["forces"]
+    out = {"mixed": {"energy": end["energy"], "max_force_pN": end["max_force"], "iterations": end["iterations"]}}
+    with Engine("fp64", int(os.environ.get("LOCAL_RANK", "0"))) as eng:
+        eng.set_network(net)
+        eng.set_coords(x_m)
+        _, e64, _ = eng.energies()
+        f64 = eng.forces()
+        out["fp64_at_mixed_end"] = {"energy": e64, "energy_rel_diff": abs(end["energy"] - e64) / abs(e64),
+                                    "max_force_pN": float(np.abs(f64).max()),
+                                    "force_max_abs_diff_pN": float(np.abs(f_m - f64).max())}
+        t0 = time.perf_counter()
+        r = eng.minimize(cg())[0]
+        x_p = eng.coords()
+        d = np.linalg.norm(x_p - x_m, axis=1)
+        out["fp64_polish_to_1pN"] = {"iterations": r["num_iter"], "seconds": round(time.perf_counter() - t0, 3),
+                                     "energy_rel_change": abs(r["energies_after"][6] - e64) / abs(e64),
+                                     "max_force_pN": r["grad_inf_norm"],
+                                     "displacement_rms_nm": float(np.sqrt((d ** 2).mean())),
+                                     "displacement_max_nm": float(d.max())}
+    with oracle.threads(threads):
+        vec = oracle.vectorize(net)
+        e_o = oracle.energy(vec, x_m)
+    out["oracle_at_mixed_end"] = {"energy": e_o, "energy_rel_diff": abs(end["energy"] - e_o) / abs(e_o)}
+    return out
 
 
 def fp64_compare(args, net):
@@ -334,20 +379,23 @@ def c3_report(seed: int = 20261203 + 1):
     return out
 
 
-def c5_report(n_params: int = 8, seed: int = 20261203 + 5):
+def c5_report(n_params: int = 64, seed: int = 20261203 + 5):
     """Implicit adjoint on the 2,000 x 30 network with 5,000 linkers (k ~ U(4, 12),
-    l0 ~ U(20, 40)): L = E(x*) + mean over filaments |end - start|^2; the adjoint
-    gradient of L in per-linker k and l0 against central differences
-    (h = 1e-4 relative, each side re-equilibrated from x*) on `n_params` random
-    parameters, FP64 engine."""
+    l0 ~ U(20, 40)): L = E(x*) + mean over filaments |end - start|^2.  The adjoint
+    gradient of L in per-linker k and l0 (GPU FP64: CG, Newton refinement to 1e-9 pN,
+    one Hessian CG solve) against central differences (h = 1e-4 relative) of the FP64
+    reference on `n_params` random parameters: each side re-equilibrated from x* by
+    Newton refinement alone (x*(theta +- h) is a 1e-4 perturbation of x*), its loss
+    evaluated by the CPU oracle at the refined coordinates with the device's lists."""
     import numpy as np
+    import oracle
     from picgo_gb300 import Engine, make_network
     from picgo_gb300.autograd import EquilibriumOptions, equilibrate
     net = make_network("c5", seed=seed)
     fcs = np.asarray(net.fil_cyl_start)
     first, last = net.cyl_b1[fcs[:-1]], net.cyl_b2[fcs[1:] - 1]
 
-    def loss(x):
+    def reg(x):
         d = x[last] - x[first]
         g = np.zeros_like(x)
         np.add.at(g, last, 2.0 * d / len(first))
@@ -362,17 +410,21 @@ def c5_report(n_params: int = 8, seed: int = 20261203 + 5):
         eng.set_network(net)
         t0 = time.perf_counter()
         xs, es, info = equilibrate(eng, net.coord, k0, l00, EquilibriumOptions())
+        # the neighbor lists of x*, as the oracle builds them for the loss: rebuild there and refine again
+        x_lists = xs
+        eng.rebuild()
+        info = eng.newton_refine(30, 1e-9)
+        xs = eng.coords()
         out["equilibrate_s"] = round(time.perf_counter() - t0, 2)
         out["equilibrium_max_force_pN"] = info["max_force"]
-        lx, g = loss(xs)
+        lx, g = reg(xs)
         t0 = time.perf_counter()
         gk, gl, ainfo = eng.adjoint(g, 1.0)
         out["adjoint_s"] = round(time.perf_counter() - t0, 3)
         out["adjoint_cg"] = {k: ainfo[k] for k in ("iterations", "converged", "rel_residual")}
         rng = np.random.default_rng(seed)
         picks = rng.choice(len(k0), size=max(1, n_params // 2), replace=False)
-        fd_opts = EquilibriumOptions(rebuild_at_minimum=False)
-        rows, worst = [], 0.0
+        rows, worst, t_fd = [], 0.0, time.perf_counter()
         for j in picks:
             for which in ("k", "l0"):
                 base = k0 if which == "k" else l00
@@ -382,13 +434,22 @@ def c5_report(n_params: int = 8, seed: int = 20261203 + 5):
                     p = base.copy()
                     p[j] += sgn * h
                     kk, ll = (p, l00) if which == "k" else (k0, p)
-                    xe, ee, _ = equilibrate(eng, xs, kk, ll, fd_opts)
-                    vals.append(ee + loss(xe)[0])
+                    eng.set_coords(xs)
+                    eng.set_linker_params(kk, ll)
+                    ninfo = eng.newton_refine(30, 1e-9)
+                    xe = eng.coords()
+                    side = net.copy()
+                    side.lk_k, side.lk_l0 = kk, ll
+                    vec = oracle.vectorize(side, x_lists)   # the device's lists
+                    vals.append(oracle.energy(vec, xe) + reg(xe)[0])
                 fd = (vals[0] - vals[1]) / (2 * h)
                 adj = float((gk if which == "k" else gl)[j])
                 rel = abs(adj - fd) / max(abs(fd), 1e-12)
                 worst = max(worst, rel)
-                rows.append({"param": f"{which}[{int(j)}]", "adjoint": adj, "fd": fd, "rel_err": rel})
+                rows.append({"param": f"{which}[{int(j)}]", "adjoint": adj, "fd": fd, "rel_err": rel,
+                             "newton_max_force_pN": ninfo["max_force"]})
+        eng.set_linker_params(k0, l00)
+        out["fd_s"] = round(time.perf_counter() - t_fd, 2)
         out["checks"] = rows
         out["max_rel_err"] = worst
     return out
@@ -467,6 +528,19 @@ def cpu_sample(net, seconds: float, threads: int = 1):
             "seconds": round(dt, 2), "energy_evals_per_force_eval": round(res.numEnergyCall / max(1, res.numForceCall), 3)}
 
 
+def cpu_time_to_1pN(net, threads: int):
+    """The oracle's CG from the seeded start to max|F| < 1 pN, unbounded (wall time)."""
+    import oracle
+    vec = oracle.vectorize(net)
+    with oracle.threads(threads):
+        t0 = time.perf_counter()
+        x, f, res = oracle.minimize(vec, net.coord, oracle.cg_params(energyRelTol=0.0, forceCallLimit=10_000_000))
+        dt = time.perf_counter() - t0
+    return {"time_to_1pN_s": round(dt, 2), "cores": threads, "cg_iterations": res.numIter,
+            "force_calls": res.numForceCall, "energy_calls": res.numEnergyCall, "final_max_force_pN": res.gradInfNorm,
+            "force_evals_per_s": round(res.numForceCall / dt, 3)}
+
+
 def host_threads() -> int:
     try:
         return max(1, len(os.sched_getaffinity(0)))
@@ -540,10 +614,14 @@ def main():
     ap.add_argument("--precision", choices=["mixed", "fp64"], default="mixed")
     ap.add_argument("--cpu-seconds", type=float, default=20.0)
     ap.add_argument("--no-fp64", action="store_true")
+    ap.add_argument("--cpu-full", action="store_true",
+                    help="also run the oracle's CG to 1 pN unbounded: the 200 x 20 network serially and on all host "
+                         "threads, and this workload on all host threads (minutes)")
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--no-c3", action="store_true", help="skip the mixed-vs-FP64 end-state report on the small network")
     ap.add_argument("--c5", type=int, default=0, metavar="P",
-                    help="only run the implicit-adjoint check on P parameters of the 2,000 x 30 network")
+                    help="only run the implicit-adjoint check on P parameters of the 2,000 x 30 network (64 in the "
+                         "configuration)")
     ap.add_argument("--c4", type=int, default=0, metavar="R",
                     help="only run the batched-ensemble comparison on R replicas and print its JSON line")
     ap.add_argument("--probe", action="store_true",
@@ -581,19 +659,28 @@ def main():
         if dist is not None:
             dist.destroy_process_group()
         return
-    out, net = run_ours(args, rank, world, dist)
+    out, net, end = run_ours(args, rank, world, dist)
     if rank == 0:
         if not args.no_fp64 and args.precision == "mixed":
             f = fp64_compare(args, net)
             out["fp64"] = f
             out["mixed_vs_fp64_time_to_1pN"] = round(f["time_to_1pN_s"] / out["time_to_1pN_s"], 3)
             out["mixed_vs_fp64_evals_per_s"] = round(out["value"] / max(f["force_evals_per_s"], 1e-9), 3)
+            out["mixed_vs_fp64_us_per_iteration"] = round(
+                (f["time_to_1pN_s"] / f["cg_iterations"]) / (out["time_to_1pN_s"] / out["cg_iterations"]), 3)
+            out["mixed_end_state"] = mixed_end_state_report(net, end, host_threads())
         if not args.no_c3:
             out["c3_mixed_vs_fp64"] = c3_report()
         if not args.no_cpu and world == 1:
             out["cpu_baseline"] = cpu_sample(net, args.cpu_seconds * 0.6, host_threads())
             one = cpu_sample(net, args.cpu_seconds * 0.4, 1)
             out["cpu_baseline_1thread"] = {k: one[k] for k in ("value", "unit", "cores", "seconds")}
+            if args.cpu_full:
+                from picgo_gb300 import make_network
+                out["cpu_baseline"]["time_to_1pN"] = cpu_time_to_1pN(net, host_threads())
+                c1 = make_network("c1", seed=20261203 + 1)
+                out["cpu_c1_time_to_1pN"] = {"threads": cpu_time_to_1pN(c1, host_threads()),
+                                             "serial": cpu_time_to_1pN(c1, 1)}
         print(json.dumps(out))
     if dist is not None:
         dist.destroy_process_group()

@@ -607,7 +607,7 @@ __device__ __forceinline__ bool idle_range(const DevNet<float>& n, int t0, int t
     return *s_flag != 0;
 }
 
-__global__ void __launch_bounds__(kBlock) k_fil_energy_bulk(DevNet<float> n, int want, int trial) {
+__global__ void __launch_bounds__(kBlock, 4) k_fil_energy_bulk(DevNet<float> n, int want, int trial) {
     MECH_TRACE_KERNEL(n, TK_FIL_ENERGY_BULK);
     __shared__ EnergyStage stage[kBulkStages];
     __shared__ __align__(8) uint64_t bar[kBulkStages];
@@ -683,50 +683,40 @@ __global__ void __launch_bounds__(kBlock) k_fil_energy_bulk(DevNet<float> n, int
         if (b < t.y) {
             const StageRange rg = stage_range(t.x, t.y, n.nb, 1);
             const int fl = S.flag[b - rg.fs];
-            const Pos<float> q0 = load_pos(S.x, b - rg.xs);
-            const Pos<float> qp = fl & 1 ? load_pos(S.x, b + 1 - rg.xs) : q0;
-            const Pos<float> qm = fl & 2 ? load_pos(S.x, b - 1 - rg.xs) : q0;
-            Pos<float> p0 = q0, pp = qp, pm = qm;
-            if (tr) {
-                p0 = moved_f(q0, S.d, b - rg.ds, lf);
-                if (fl & 1) pp = moved_f(qp, S.d, b + 1 - rg.ds, lf);
-                if (fl & 2) pm = moved_f(qm, S.d, b - 1 - rg.ds, lf);
-                store_pos(n.x[(xb + 1) % 3], b, p0);   // materialize the owned trial position
-            }
             const float4 pr = S.par[b - t.x];
-            if (dual && (fl & 1)) {
-                // the second trial, at lambda / 2 (halving is exact in float)
-                const float lh = 0.5f * lf;
-                const Pos<float> h0 = moved_f(q0, S.d, b - rg.ds, lh);
-                const Pos<float> hp = moved_f(qp, S.d, b + 1 - rg.ds, lh);
-                store_pos(n.x[(xb + 2) % 3], b, h0);
-                float r2[3];
-                pdiff(hp, h0, r2);
-                es2.add(stretch_energy<float>(r2[0], r2[1], r2[2], pr.x, pr.y));
-                if (fl & 2) {
-                    const Pos<float> hm = moved_f(qm, S.d, b - 1 - rg.ds, lh);
-                    float r1[3];
-                    pdiff(h0, hm, r1);
-                    eb2.add(bend_energy<float>(r1, r2, pr.z, pr.w));
+            // one trial per pass of this loop (two in a two-trial pass: lambda,
+            // then lambda / 2, exact in float), so the second reuses the registers
+            // of the first
+#pragma unroll 1
+            for (int ch = 0; ch < (dual ? 2 : 1); ++ch) {
+                const float lch = ch ? 0.5f * lf : lf;
+                Pos<float> p0 = load_pos(S.x, b - rg.xs);
+                Pos<float> pp = fl & 1 ? load_pos(S.x, b + 1 - rg.xs) : p0;
+                Pos<float> pm = fl & 2 ? load_pos(S.x, b - 1 - rg.xs) : p0;
+                if (tr) {
+                    p0 = moved_f(p0, S.d, b - rg.ds, lch);
+                    if (fl & 1) pp = moved_f(pp, S.d, b + 1 - rg.ds, lch);
+                    if (fl & 2) pm = moved_f(pm, S.d, b - 1 - rg.ds, lch);
+                    store_pos(n.x[(xb + 1 + ch) % 3], b, p0);   // materialize the owned trial position
                 }
-            } else if (dual) {
-                store_pos(n.x[(xb + 2) % 3], b, moved_f(q0, S.d, b - rg.ds, 0.5f * lf));
-            }
-            if (fl & 1) {
-                float r2[3];
-                pdiff(pp, p0, r2);
-                const float ts = stretch_energy<float>(r2[0], r2[1], r2[2], pr.x, pr.y);
-                es.add(ts);
-                float tb = 0.f;
-                if (fl & 2) {
-                    float r1[3];
-                    pdiff(p0, pm, r1);
-                    tb = bend_energy<float>(r1, r2, pr.z, pr.w);
-                    eb.add(tb);
-                }
-                if (n.terms) {
-                    n.terms[b] = (double)ts;
-                    n.terms[(size_t)n.nb + b] = (double)tb;
+                if (fl & 1) {
+                    float r2[3];
+                    pdiff(pp, p0, r2);
+                    const float ts = stretch_energy<float>(r2[0], r2[1], r2[2], pr.x, pr.y);
+                    if (ch) es2.add(ts);
+                    else es.add(ts);
+                    float tb = 0.f;
+                    if (fl & 2) {
+                        float r1[3];
+                        pdiff(p0, pm, r1);
+                        tb = bend_energy<float>(r1, r2, pr.z, pr.w);
+                        if (ch) eb2.add(tb);
+                        else eb.add(tb);
+                    }
+                    if (n.terms && !ch) {
+                        n.terms[b] = (double)ts;
+                        n.terms[(size_t)n.nb + b] = (double)tb;
+                    }
                 }
             }
         }

@@ -109,8 +109,13 @@ struct MechContext {
     // force kernels, and a multiplier on the default neighbor-list bin edge
     int tile_cap[2] = {kFilBulkMaxTiles, kFilBulkMaxTiles};
     // resident blocks per SM of the persistent filament energy / force kernels
-    // (0: as many as fit); fewer leave room for the lanes running beside them
-    int blocks_per_sm[2] = {0, 0};
+    // (0: as many as fit); fewer leave room for the lanes running beside them.
+    // The force kernel defaults to 3 of its 4: the fourth block's registers
+    // would keep the excluded-volume lane's extended-precision pass (102
+    // registers x 128 threads) waiting for a slot while the forces stream
+    // (measured on the 1M-cylinder network: 157 against 173 us per iteration
+    // over the first 300 iterations, no change later in the run).
+    int blocks_per_sm[2] = {0, 3};
     double cell_scale = 1.0;
     int sp_tiles_c[K_NUM_SPARSE] = {0, 0, 0, 0};
     int slot_base[K_NUM_SPARSE + 1] = {0, 0, 0, 0, 0};
@@ -177,10 +182,18 @@ DevNet<Real> make_devnet(MechContext* c) {
     n.n_ftiles = c->compact ? c->n_ftiles_c : c->n_ftiles;
     n.ftile = (c->compact ? c->ftile_c : c->ftile).as<Tile>();
     for (int k = 0; k < 3; ++k) {
-        n.pgrid[k] = std::max(1, std::min(n.n_ftiles, persistent_blocks(c->device, k, k < 2 ? c->blocks_per_sm[k] : 0)));
+        const int per_sm = k < 2 ? c->blocks_per_sm[k] : 0;
+        const int resident = persistent_blocks(c->device, k, per_sm);
+        n.pgrid[k] = std::max(1, std::min(n.n_ftiles, resident));
         n.ptiles[k] = (n.n_ftiles + n.pgrid[k] - 1) / n.pgrid[k];
-        // the bulk-staged energy/force kernels keep a block's tile descriptors in shared memory
-        if (k < 2) n.ptiles[k] = std::max(1, std::min(n.ptiles[k], c->tile_cap[k]));
+        if (k < 2) {
+            // the bulk-staged energy/force kernels keep a block's tile descriptors in
+            // shared memory (at most kFilBulkMaxTiles); a tuned smaller run length adds
+            // waves, unless a residency cap is set, which the grid then keeps to
+            n.ptiles[k] = std::max(1, std::min(n.ptiles[k], c->tile_cap[k]));
+            if (per_sm > 0) n.ptiles[k] = std::max(n.ptiles[k], (n.n_ftiles + resident - 1) / resident);
+            n.ptiles[k] = std::min(n.ptiles[k], kFilBulkMaxTiles);
+        }
         n.pgrid[k] = (n.n_ftiles + n.ptiles[k] - 1) / n.ptiles[k];
     }
     n.n_lk = c->nlk;
@@ -1854,9 +1867,11 @@ static int autotune_impl(MechContext* c, int flags, MechTuning* out) {
                 if (cap > kFilBulkMaxTiles) continue;
                 c->tile_cap[which] = cap;
                 const DevNet<Real> n = make_devnet<Real>(c);
-                launch_part<Real>(n, which, s);   // warm
+                // the energy kernel as the minimizer runs it: a line-search pass
+                const int part = which == 0 ? 4 : 1;
+                launch_part<Real>(n, part, s);   // warm
                 cudaEventRecord(e0, s);
-                for (int i = 0; i < 10; ++i) launch_part<Real>(n, which, s);
+                for (int i = 0; i < 10; ++i) launch_part<Real>(n, part, s);
                 cudaEventRecord(e1, s);
                 CU(cudaEventSynchronize(e1));
                 float ms = 0.f;
