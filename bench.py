@@ -379,18 +379,19 @@ def c3_report(seed: int = 20261203 + 1):
     return out
 
 
-def c5_report(n_params: int = 64, seed: int = 20261203 + 5):
+def c5_report(n_params: int = 64, seed: int = 20261203 + 5, budget_s: float = 420.0):
     """Implicit adjoint on the 2,000 x 30 network with 5,000 linkers (k ~ U(4, 12),
     l0 ~ U(20, 40)): L = E(x*) + mean over filaments |end - start|^2.  The adjoint
     gradient of L in per-linker k and l0 (GPU FP64: CG, Newton refinement to 1e-9 pN,
     one Hessian CG solve) against central differences (h = 1e-4 relative) of the FP64
     reference on `n_params` random parameters: each side re-equilibrated from x* by
     Newton refinement alone (x*(theta +- h) is a 1e-4 perturbation of x*), its loss
-    evaluated by the CPU oracle at the refined coordinates with the device's lists."""
+    evaluated by the CPU oracle at the refined coordinates with the device's lists.
+    Parameters are checked until `budget_s` seconds of finite differences have
+    passed; the report says how many were."""
     import numpy as np
     import oracle
     from picgo_gb300 import Engine, make_network
-    from picgo_gb300.autograd import EquilibriumOptions, equilibrate
     net = make_network("c5", seed=seed)
     fcs = np.asarray(net.fil_cyl_start)
     first, last = net.cyl_b1[fcs[:-1]], net.cyl_b2[fcs[1:] - 1]
@@ -406,26 +407,40 @@ def c5_report(n_params: int = 64, seed: int = 20261203 + 5):
     l00 = np.asarray(net.lk_l0, dtype=np.float64)
     out = {"workload": "2,000 filaments x 30 cylinders (60,000 cylinders), 5,000 linkers k~U(4,12) l0~U(20,40)",
            "seed": seed, "n_params": n_params}
+    def log(msg):
+        print(f"c5 [{time.perf_counter() - t0:7.1f} s] {msg}", file=sys.stderr, flush=True)
+
+    t0 = time.perf_counter()
+    with Engine("mixed") as em:   # most of the descent in mixed precision, to its 1 pN design point
+        em.set_network(net)
+        r = em.minimize(cg())[0]
+        x0 = em.coords()
+    log(f"mixed CG to 1 pN: {r['num_iter']} iterations")
     with Engine("fp64") as eng:
         eng.set_network(net)
-        t0 = time.perf_counter()
-        xs, es, info = equilibrate(eng, net.coord, k0, l00, EquilibriumOptions())
-        # the neighbor lists of x*, as the oracle builds them for the loss: rebuild there and refine again
-        x_lists = xs
+        eng.set_coords(x0)
+        r = eng.minimize(cg(grad_tol=1e-2, force_call_limit=400_000))[0]
+        log(f"FP64 CG: {r['num_iter']} iterations, max|F| {r['grad_inf_norm']:.3g}")
+        # the neighbor lists of x*, as the oracle builds them for the loss: rebuild there, then Newton
+        x_lists = eng.coords()
         eng.rebuild()
-        info = eng.newton_refine(30, 1e-9)
+        info = eng.newton_refine(40, 1e-9, 1e-8, 20000)
         xs = eng.coords()
+        log(f"Newton: {info['newton_steps']} steps, {info['iterations']} CG iterations, max|F| {info['max_force']:.3g}")
         out["equilibrate_s"] = round(time.perf_counter() - t0, 2)
         out["equilibrium_max_force_pN"] = info["max_force"]
         lx, g = reg(xs)
-        t0 = time.perf_counter()
+        ta = time.perf_counter()
         gk, gl, ainfo = eng.adjoint(g, 1.0)
-        out["adjoint_s"] = round(time.perf_counter() - t0, 3)
+        out["adjoint_s"] = round(time.perf_counter() - ta, 3)
         out["adjoint_cg"] = {k: ainfo[k] for k in ("iterations", "converged", "rel_residual")}
         rng = np.random.default_rng(seed)
         picks = rng.choice(len(k0), size=max(1, n_params // 2), replace=False)
         rows, worst, t_fd = [], 0.0, time.perf_counter()
+        log(f"adjoint: {out['adjoint_s']} s, {ainfo['iterations']} CG iterations")
         for j in picks:
+            if time.perf_counter() - t_fd > budget_s:
+                break
             for which in ("k", "l0"):
                 base = k0 if which == "k" else l00
                 h = 1e-4 * base[j]
@@ -436,7 +451,7 @@ def c5_report(n_params: int = 64, seed: int = 20261203 + 5):
                     kk, ll = (p, l00) if which == "k" else (k0, p)
                     eng.set_coords(xs)
                     eng.set_linker_params(kk, ll)
-                    ninfo = eng.newton_refine(30, 1e-9)
+                    ninfo = eng.newton_refine(8, 1e-9, 1e-8, 20000)
                     xe = eng.coords()
                     side = net.copy()
                     side.lk_k, side.lk_l0 = kk, ll
@@ -447,18 +462,24 @@ def c5_report(n_params: int = 64, seed: int = 20261203 + 5):
                 rel = abs(adj - fd) / max(abs(fd), 1e-12)
                 worst = max(worst, rel)
                 rows.append({"param": f"{which}[{int(j)}]", "adjoint": adj, "fd": fd, "rel_err": rel,
-                             "newton_max_force_pN": ninfo["max_force"]})
+                             "newton_max_force_pN": ninfo["max_force"], "newton_steps": ninfo["newton_steps"],
+                             "newton_cg_iterations": ninfo["iterations"]})
+                log(f"{which}[{int(j)}] rel {rel:.2e}")
         eng.set_linker_params(k0, l00)
         out["fd_s"] = round(time.perf_counter() - t_fd, 2)
+        out["n_checked"] = len(rows)
         out["checks"] = rows
         out["max_rel_err"] = worst
     return out
 
 
-def c4_report(n_replicas: int, precision: str = "mixed"):
+def c4_report(n_replicas: int, precision: str = "mixed", loop_budget_s: float = 240.0):
     """Batched ensemble: `n_replicas` independent networks of uneven size
     (filaments log-uniform on 50-5,000, 20-50 cylinders each, C1 density)
-    minimized together in one context vs one after another; replicas/s."""
+    minimized together in one context vs one after another; replicas/s.  The
+    one-after-another loop runs over a seeded random order of the replicas until
+    `loop_budget_s` seconds have passed; its replicas/s is that sample's rate
+    (cylinder-weighted extrapolation beside it)."""
     import torch
     from picgo_gb300 import Engine
     from picgo_gb300.network import make_ensemble
@@ -482,12 +503,17 @@ def c4_report(n_replicas: int, precision: str = "mixed"):
     out["batched"] = {"seconds": round(t_b, 3), "replicas_per_s": round(n_replicas / t_b, 2),
                       "converged": sum(1 for r in res if r["status"] == 0 and r["grad_inf_norm"] < 1.0),
                       "max_iterations": max(r["num_iter"] for r in res)}
-    t_loop = 0.0
-    conv = 0
+    print(f"c4: batched {t_b:.1f} s", file=sys.stderr, flush=True)
+    import numpy as np
+    order = np.random.default_rng(20261203).permutation(n_replicas)
+    t_loop, conv, done, cyl_done = 0.0, 0, 0, 0
     with Engine(precision) as eng:
-        for i, net in enumerate(nets):
+        for i in order:
+            if t_loop > loop_budget_s:
+                break
+            net = nets[int(i)]
             eng.set_network(net)
-            if i == 0:
+            if done == 0:
                 eng.minimize(cg(energy_call_limit=20))
                 eng.reset_coords()
             torch.cuda.synchronize()
@@ -496,8 +522,13 @@ def c4_report(n_replicas: int, precision: str = "mixed"):
             r = eng.minimize(prm)[0]
             t_loop += time.perf_counter() - t0
             conv += int(r["status"] == 0 and r["grad_inf_norm"] < 1.0)
-    out["looped"] = {"seconds": round(t_loop, 3), "replicas_per_s": round(n_replicas / t_loop, 2), "converged": conv}
-    out["batched_vs_looped"] = round(t_loop / t_b, 3)
+            done += 1
+            cyl_done += net.n_cyl
+    rate = done / t_loop
+    out["looped"] = {"replicas_run": done, "seconds": round(t_loop, 3), "replicas_per_s": round(rate, 3),
+                     "converged": conv, "cylinders_run": cyl_done,
+                     "extrapolated_seconds_all": round(t_loop * ncyl / max(cyl_done, 1), 1)}
+    out["batched_vs_looped"] = round((n_replicas / t_b) / rate, 3)
     return out
 
 

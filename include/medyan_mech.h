@@ -250,11 +250,12 @@ int32_t mech_get_forces(MechContext* ctx, int32_t replica, double* f_out);
 
 /*
  * How mech_minimize drives the device.  MECH_GRAPH_UNROLLED (default): a graph
- * of 8 unrolled iteration blocks (2 trials, forces, direction, dispatch,
+ * of 8 unrolled iteration blocks (line search: 2 single-trial passes, FP64,
+ * or one two-trial pass, mixed; forces, direction,
  * reset) relaunched by the host, every kernel reading its replica's phase and
  * exiting when it has nothing to do.  MECH_GRAPH_CONDITIONAL: one CUDA graph
  * whose device while loop runs, per body, only the phases some replica is in
- * (line-search trial, forces, direction, failure dispatch); the host is
+ * (line-search pass, forces, direction, reset to steepest descent); the host is
  * involved only for recovery moves, errors and every 512 bodies.  Both run the
  * same active kernels in the same order and give bitwise the same results; on
  * GB300 with driver 580 the conditional bodies cost more than the idle
@@ -264,6 +265,10 @@ int32_t mech_get_forces(MechContext* ctx, int32_t replica, double* f_out);
  */
 #define MECH_GRAPH_CONDITIONAL 0
 #define MECH_GRAPH_UNROLLED 1
+/* the unrolled graph with programmatic dependent launch on its main lane: the
+ * kernels around each single-block reduction are scheduled while their
+ * predecessor runs and wait for it on the device (same results) */
+#define MECH_GRAPH_UNROLLED_PDL 2
 int32_t mech_set_graph_mode(MechContext* ctx, int32_t mode);
 
 /*
@@ -309,7 +314,7 @@ typedef struct MechProfile {
     int64_t n_exvol_ext_energy;    /* mixed engine: pairs its last energy pass sent to the extended-precision pass */
     int64_t n_exvol_ext_force;     /* and its last force pass */
     double ms_iteration_idle;      /* one minimizer iteration block (two line-search trials, forces,
-                                      direction, failure dispatch, reset) with no replica selected:
+                                      direction, reset) with no replica selected:
                                       the cost of the launches that find nothing to do */
     double ms_trial_energy_eval;   /* one line-search trial: energy at x + lambda d, trial positions written */
     int64_t n_exvol_fallback_energy;   /* pairs the last energy pass sent to the Simpson fallback */
@@ -339,7 +344,10 @@ typedef struct MechTuning {
     double ms_rebuild;              /* best rebuild wall time found (ms) */
     int32_t energy_blocks_per_sm;   /* resident blocks per SM of the persistent filament energy kernel */
     int32_t force_blocks_per_sm;    /* and of the filament force kernel (0: as many as fit); fewer leave SM
-                                       room for the excluded-volume and linker lanes running beside them */
+                                       room for the excluded-volume and linker lanes running beside them.
+                                       A new context uses 0 (energy) and 2 (force); with a cap the grid
+                                       holds one resident wave, its runs lengthened as needed, and the
+                                       kernel is launched before the side lanes */
 } MechTuning;
 int32_t mech_autotune(MechContext* ctx, int32_t flags, MechTuning* out);
 int32_t mech_set_tuning(MechContext* ctx, const MechTuning* t);

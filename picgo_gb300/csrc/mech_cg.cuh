@@ -77,11 +77,13 @@ __device__ __forceinline__ double record_energies(CGState& S, const double* e) {
     return failed ? (1.0 / 0.0) : tot;
 }
 
+// The finalizers take the replica's tile ranges and (thread 0) a register copy
+// of its state, both loaded by the kernel at its start together with the
+// phase it selects on: on this GPU every dependent round trip to L2 (partial
+// slots written by the other die's SMs) costs about a microsecond, and a
+// finalizer is a chain of them on the minimizer's critical path.
 template <typename Real>
-__device__ void finalize_energy(const DevNet<Real>& n, int r, int trial, double* sh) {
-    CGState S;
-    if (threadIdx.x == 0) S = n.st[r];
-    const RepTiles rt = n.rt[r];
+__device__ void finalize_energy(const DevNet<Real>& n, int r, int trial, const RepTiles& rt, CGState& S, double* sh) {
     const int stride = sizeof(Real) == 4 ? n.ptiles[0] : 1;
     const int nslot = run_slots(rt.fil_begin, rt.fil_end, stride);
     const int ffk[K_NUM_SPARSE] = {MECH_FF_LINKER, MECH_FF_MOTOR, MECH_FF_EXVOL, MECH_FF_BOUNDARY};
@@ -92,7 +94,18 @@ __device__ void finalize_energy(const DevNet<Real>& n, int r, int trial, double*
         // the doubles are formed in thread 0 only.  acc[0, 6): the (first)
         // trial, acc[6, 12): the second trial of a two-trial pass.
         FF acc[2 * MECH_NUM_FF];
-#pragma unroll 4
+        // each sparse kind's first slot of this thread, loaded with the first filament slots
+        float2 sp0[K_NUM_SPARSE], sp1[K_NUM_SPARSE];
+#pragma unroll
+        for (int k = 0; k < K_NUM_SPARSE; ++k) {
+            const int i = rt.sp_begin[k] + threadIdx.x;
+            sp0[k] = sp1[k] = make_float2(0.f, 0.f);
+            if (i < rt.sp_end[k]) {
+                sp0[k] = load_pair(n.part_sp + i);
+                if (dual) sp1[k] = load_pair(n.part_sp2 + i);
+            }
+        }
+#pragma unroll 8
         for (int k = threadIdx.x; k < nslot; k += blockDim.x) {
             const double* slot = n.part_fil + 4 * (size_t)run_slot(rt.fil_begin, stride, k);
             add_pair(acc[MECH_FF_STRETCHING], load_pair(slot));
@@ -104,8 +117,13 @@ __device__ void finalize_energy(const DevNet<Real>& n, int r, int trial, double*
         }
 #pragma unroll
         for (int k = 0; k < K_NUM_SPARSE; ++k) {
+            const int i0 = rt.sp_begin[k] + threadIdx.x;
+            if (i0 < rt.sp_end[k]) {
+                add_pair(acc[ffk[k]], sp0[k]);
+                if (dual) add_pair(acc[MECH_NUM_FF + ffk[k]], sp1[k]);
+            }
 #pragma unroll 4
-            for (int i = rt.sp_begin[k] + threadIdx.x; i < rt.sp_end[k]; i += blockDim.x) {
+            for (int i = i0 + blockDim.x; i < rt.sp_end[k]; i += blockDim.x) {
                 add_pair(acc[ffk[k]], load_pair(n.part_sp + i));
                 if (dual) add_pair(acc[MECH_NUM_FF + ffk[k]], load_pair(n.part_sp2 + i));
             }
@@ -208,10 +226,7 @@ __device__ __forceinline__ void force_step(CGState& S, double mx, double ff, dou
 }
 
 template <typename Real>
-__device__ void finalize_force(const DevNet<Real>& n, int r, double* sh) {
-    CGState S;
-    if (threadIdx.x == 0) S = n.st[r];
-    const RepTiles rt = n.rt[r];
+__device__ void finalize_force(const DevNet<Real>& n, int r, const RepTiles& rt, CGState& S, double* sh) {
     const int stride = 1;   // k_force_gather writes one slot per tile
     const int nslot = run_slots(rt.fil_begin, rt.fil_end, stride);
     double mx, ff, ffp;
@@ -220,7 +235,7 @@ __device__ void finalize_force(const DevNet<Real>& n, int r, double* sh) {
         // in single precision and form the doubles in thread 0 only
         FF a[2];
         float m[1] = {0.f};
-#pragma unroll 8
+#pragma unroll 16
         for (int k = threadIdx.x; k < nslot; k += blockDim.x) {
             const float* p = reinterpret_cast<const float*>(n.part_fil + 4 * (size_t)run_slot(rt.fil_begin, stride, k));
             const float4 v = __ldcg(reinterpret_cast<const float4*>(p));
@@ -262,16 +277,14 @@ __device__ void finalize_force(const DevNet<Real>& n, int r, double* sh) {
 // One block per replica after the direction update: the slope d.F, the
 // conjugacy test and the next iteration's start (CGMethod.hpp:1553-1560).
 template <typename Real>
-__device__ void finalize_direction(const DevNet<Real>& n, int r, double* sh) {
-    CGState S;
-    if (threadIdx.x == 0) S = n.st[r];
-    const RepTiles rt = n.rt[r];
+__device__ void finalize_direction(const DevNet<Real>& n, int r, const RepTiles& rt, CGState& S, double* sh) {
     double slope;
     if constexpr (sizeof(Real) == 8) {
         slope = sum_slots(n.part_fil, 4, 3, rt.fil_begin, rt.fil_end, sh);
     } else {
         FF a[1];
         const int nslot = run_slots(rt.fil_begin, rt.fil_end, n.ptiles[2]);
+#pragma unroll 8
         for (int k = threadIdx.x; k < nslot; k += blockDim.x)
             add_pair(a[0], load_pair(n.part_fil + 4 * (size_t)run_slot(rt.fil_begin, n.ptiles[2], k) + 3));
         block_reduce_ff<1, 0>(a, nullptr, reinterpret_cast<float*>(sh));

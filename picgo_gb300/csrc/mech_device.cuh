@@ -121,6 +121,26 @@ __device__ __forceinline__ bool converged(const CGState& S) {
     return S.maxF < S.gradTol || S.energyRelChange < S.energyRelTol;
 }
 
+// lambda = 0 after a line search (CGMethod.hpp:1337-1367): stop with
+// errorLineSearch, enter safe mode, or (already in safe mode) hand MController's
+// recovery move to the host.  Applied where the line search fails, so no launch
+// of its own has to look for failed replicas.
+__device__ __forceinline__ void dispatch_failed(CGState& S) {
+    if (!S.tryToRecover) {
+        S.errorFlags |= 1u;
+        S.status = MECH_ERR_LINESEARCH;
+        S.phase = PH_DONE;
+    } else if (!S.safeMode) {
+        S.safeMode = 1;
+        S.numSafeMode++;
+        S.phase = PH_RESET;
+    } else {
+        S.safeMode = 0;
+        S.numRecover++;
+        S.phase = PH_RECOVER;
+    }
+}
+
 // Loop head and the start of backtrackingLineSearch (CGMethod.hpp:238-296, :1279-1320).
 // The energy at the current coordinates is the cached E0: it is the accepted
 // trial's energy, bit for bit, because the trial coordinates x + lambda d are
@@ -134,6 +154,7 @@ __device__ __forceinline__ void begin_iteration(CGState& S) {
     if (S.maxF == 0.0) {     // "return zero if no forces": lambda 0, no energy call
         S.lambda = 0.0;
         S.phase = PH_FAILED;
+        dispatch_failed(S);
         return;
     }
     S.lambda = fmin(S.lambdaMax, S.maxDist / S.maxF);
@@ -169,6 +190,7 @@ __device__ __forceinline__ void line_search_step(CGState& S, double E, int trial
     S.totalEnergy = Elam;
     if (lambda == 0.0) {
         S.phase = PH_FAILED;
+        dispatch_failed(S);
         return;
     }
     S.newEnergy = Elam;

@@ -121,7 +121,8 @@ __device__ void after_phase(const DevNet<Real>& n, int phase_slot, int* s_flag) 
 // read them by then), then sets the graph conditions when there are any.
 template <typename Real>
 __device__ void after_evaluation(const DevNet<Real>& n, int phase_slot, int* s_flag) {
-    if (!last_tile(n.gticket, 0, gridDim.x, s_flag)) return;
+    if (gridDim.x == 1) __syncthreads();   // one replica: this block is the last, no ticket needed
+    else if (!last_tile(n.gticket, 0, gridDim.x, s_flag)) return;
     if (threadIdx.x == 0) {
         if (n.ev_list_count) *n.ev_list_count = 0;
         if (n.ev_fb_count) *n.ev_fb_count = 0;
@@ -141,6 +142,7 @@ __global__ void __launch_bounds__(kBlock) k_body_head(DevNet<Real> n) {
 // ---------------------------------------------------------------------------
 template <typename Real>
 __global__ void __launch_bounds__(kBlock) k_fil_energy(DevNet<Real> n, int want, int trial) {
+    pdl_wait();      // the previous kernel of the main lane has finished
     MECH_TRACE_KERNEL(n, TK_FIL_ENERGY);
     __shared__ Pos<Real> xs[kFilTile + 4];
     __shared__ double sh[32 * MECH_NUM_FF];
@@ -203,6 +205,7 @@ __global__ void __launch_bounds__(kBlock) k_fil_energy(DevNet<Real> n, int want,
 // ---------------------------------------------------------------------------
 template <typename Real>
 __global__ void __launch_bounds__(kBlock) k_fil_force(DevNet<Real> n, int want) {
+    pdl_wait();      // the previous kernel of the main lane has finished
     MECH_TRACE_KERNEL(n, TK_FIL_FORCE);
     __shared__ Pos<Real> xs[kFilTile + 4];
     __shared__ Real fs[(kFilTile + 2) * 3];    // stretch force on the second bead
@@ -305,6 +308,7 @@ __device__ __forceinline__ void gather_bead(const DevNet<Real>& n, int b, int fb
 
 template <typename Real>
 __global__ void __launch_bounds__(kBlock) k_force_gather(DevNet<Real> n, int want) {
+    pdl_trigger();   // the next kernel of the main lane may be scheduled now
     MECH_TRACE_KERNEL(n, TK_GATHER);
     __shared__ double sh[32 * 3];
     __shared__ int s_go[kGatherTiles], s_fb[kGatherTiles];
@@ -354,6 +358,7 @@ __global__ void __launch_bounds__(kBlock) k_force_gather(DevNet<Real> n, int wan
 // bead); otherwise 4 beads strided by 64.  The tile's partials combine the
 // two warps of its 64 threads.
 __global__ void __launch_bounds__(kBlock) k_force_gather_mx(DevNet<float> n, int want) {
+    pdl_trigger();   // the next kernel of the main lane may be scheduled now
     MECH_TRACE_KERNEL(n, TK_GATHER_MX);
     static_assert(kFilTile == 256 && kBlock == 64 * kGatherTiles, "64 threads x 4 beads per tile");
     __shared__ float sh[8][5];   // per warp: F.F (hi, lo), F.Fprev (hi, lo), max
@@ -455,11 +460,16 @@ __global__ void __launch_bounds__(kBlock) k_force_gather_mx(DevNet<float> n, int
 // One block per replica: max |F|, the dots and the CG step logic after the gather.
 template <typename Real>
 __global__ void __launch_bounds__(kBlock) k_finalize_force(DevNet<Real> n, int want) {
+    pdl_wait();      // the previous kernel of the main lane has finished
+    pdl_trigger();   // the next kernel of the main lane may be scheduled now
     MECH_TRACE_KERNEL(n, TK_FIN_FORCE);
     __shared__ double sh[32 * 3];
     __shared__ int s_flag;
     const int r = blockIdx.x;
-    if (replica_selected(n.st[r], want)) finalize_force(n, r, sh);
+    CGState S;
+    if (threadIdx.x == 0) S = n.st[r];   // issued together with the loads below
+    const RepTiles rt = n.rt[r];
+    if (replica_selected(n.st[r], want)) finalize_force(n, r, rt, S, sh);
     after_evaluation(n, kCondForce, &s_flag);
 }
 
@@ -467,11 +477,15 @@ __global__ void __launch_bounds__(kBlock) k_finalize_force(DevNet<Real> n, int w
 // every kernel of the evaluation has written its partial sums.
 template <typename Real>
 __global__ void __launch_bounds__(kBlock) k_finalize_energy(DevNet<Real> n, int want, int trial) {
+    pdl_trigger();   // the next kernel of the main lane may be scheduled now
     MECH_TRACE_KERNEL(n, TK_FIN_ENERGY);
     __shared__ double sh[32 * 2 * MECH_NUM_FF];   // block_reduce_ff<12> of a two-trial pass: 32 * 24 floats
     __shared__ int s_flag;
     const int r = blockIdx.x;
-    if (replica_selected(n.st[r], want)) finalize_energy(n, r, trial, sh);
+    CGState S;
+    if (threadIdx.x == 0) S = n.st[r];   // issued together with the loads below
+    const RepTiles rt = n.rt[r];
+    if (replica_selected(n.st[r], want)) finalize_energy(n, r, trial, rt, S, sh);
     after_evaluation(n, kCondTrial, &s_flag);
 }
 
@@ -608,12 +622,14 @@ __device__ __forceinline__ bool idle_range(const DevNet<float>& n, int t0, int t
 }
 
 __global__ void __launch_bounds__(kBlock, 4) k_fil_energy_bulk(DevNet<float> n, int want, int trial) {
+    pdl_wait();      // the previous kernel of the main lane has finished
     MECH_TRACE_KERNEL(n, TK_FIL_ENERGY_BULK);
     __shared__ EnergyStage stage[kBulkStages];
     __shared__ __align__(8) uint64_t bar[kBulkStages];
     __shared__ int4 s_desc[kBulkMaxTiles];
     __shared__ float s_lf[kBulkMaxTiles];
     __shared__ double sh[32 * 4];   // write_run<4>: 32 * 8 floats
+    __shared__ __align__(16) float s_mv[6 * kBulkXBeads];   // the staged beads moved to a trial
     __shared__ int s_abort;
     const int t0 = blockIdx.x * n.ptiles[0], t1 = min(t0 + n.ptiles[0], n.n_ftiles);
     const int nt = t1 - t0;
@@ -680,26 +696,34 @@ __global__ void __launch_bounds__(kBlock, 4) k_fil_energy_bulk(DevNet<float> n, 
         }
         const EnergyStage& S = stage[sidx];
         const int b = t.x + threadIdx.x;
-        if (b < t.y) {
-            const StageRange rg = stage_range(t.x, t.y, n.nb, 1);
-            const int fl = S.flag[b - rg.fs];
-            const float4 pr = S.par[b - t.x];
-            // one trial per pass of this loop (two in a two-trial pass: lambda,
-            // then lambda / 2, exact in float), so the second reuses the registers
-            // of the first
+        const StageRange rg = stage_range(t.x, t.y, n.nb, 1);
+        const bool own = b < t.y;
+        int fl = 0;
+        float4 pr = make_float4(0.f, 0.f, 0.f, 0.f);
+        if (own) {
+            fl = S.flag[b - rg.fs];
+            pr = S.par[b - t.x];
+        }
+        // one trial per pass of this loop (two in a two-trial pass: lambda,
+        // then lambda / 2, exact in float).  For a trial the block first moves
+        // every staged bead once (tile and halo) into shared memory, so each
+        // bead's neighbours are read, not moved again by every thread that
+        // needs them; a plain evaluation reads the staged positions directly.
 #pragma unroll 1
-            for (int ch = 0; ch < (dual ? 2 : 1); ++ch) {
+        for (int ch = 0; ch < (dual ? 2 : 1); ++ch) {
+            const float* P = S.x;
+            if (tr) {
                 const float lch = ch ? 0.5f * lf : lf;
-                Pos<float> p0 = load_pos(S.x, b - rg.xs);
-                Pos<float> pp = fl & 1 ? load_pos(S.x, b + 1 - rg.xs) : p0;
-                Pos<float> pm = fl & 2 ? load_pos(S.x, b - 1 - rg.xs) : p0;
-                if (tr) {
-                    p0 = moved_f(p0, S.d, b - rg.ds, lch);
-                    if (fl & 1) pp = moved_f(pp, S.d, b + 1 - rg.ds, lch);
-                    if (fl & 2) pm = moved_f(pm, S.d, b - 1 - rg.ds, lch);
-                    store_pos(n.x[(xb + 1 + ch) % 3], b, p0);   // materialize the owned trial position
-                }
+                for (int q = threadIdx.x; q < rg.xe - rg.xs; q += blockDim.x)
+                    store_pos(s_mv, q, moved_f(load_pos(S.x, q), S.d, q + rg.xs - rg.ds, lch));
+                __syncthreads();
+                P = s_mv;
+            }
+            if (own) {
+                const Pos<float> p0 = load_pos(P, b - rg.xs);
+                if (tr) store_pos(n.x[(xb + 1 + ch) % 3], b, p0);   // materialize the owned trial position
                 if (fl & 1) {
+                    const Pos<float> pp = load_pos(P, b + 1 - rg.xs);
                     float r2[3];
                     pdiff(pp, p0, r2);
                     const float ts = stretch_energy<float>(r2[0], r2[1], r2[2], pr.x, pr.y);
@@ -707,6 +731,7 @@ __global__ void __launch_bounds__(kBlock, 4) k_fil_energy_bulk(DevNet<float> n, 
                     else es.add(ts);
                     float tb = 0.f;
                     if (fl & 2) {
+                        const Pos<float> pm = load_pos(P, b - 1 - rg.xs);
                         float r1[3];
                         pdiff(p0, pm, r1);
                         tb = bend_energy<float>(r1, r2, pr.z, pr.w);
@@ -719,6 +744,7 @@ __global__ void __launch_bounds__(kBlock, 4) k_fil_energy_bulk(DevNet<float> n, 
                     }
                 }
             }
+            if (tr) __syncthreads();   // s_mv is refilled by the next trial or tile
         }
         ++j;
         __syncthreads();   // stage sidx fully read
@@ -806,12 +832,16 @@ __device__ void issue_force_stage(const DevNet<float>& n, int4 t, ForceStage* st
 // is written to the force buffer, where k_force_gather adds the bead's sparse
 // contributions and forms the CG partials.
 __global__ void __launch_bounds__(kBlock) k_fil_force_bulk(DevNet<float> n, int want) {
+    pdl_wait();      // the previous kernel of the main lane has finished
     MECH_TRACE_KERNEL(n, TK_FIL_FORCE_BULK);
     __shared__ ForceStage stage[kBulkStages];
     __shared__ __align__(8) uint64_t bar[kBulkStages];
     __shared__ int4 s_desc[kBulkMaxTiles];
     __shared__ float s_lf[kBulkMaxTiles];
     __shared__ int s_abort;
+    // per tile: stretching force of each cylinder (q, q + 1) and the two bending
+    // terms of each triple centred on q, for q = tile begin - 1 .. tile end
+    __shared__ float s_st[kFilTile + 2][3], s_a1[kFilTile + 2][3], s_a2[kFilTile + 2][3];
     const int t0 = blockIdx.x * n.ptiles[1], t1 = min(t0 + n.ptiles[1], n.n_ftiles);
     const int nt = t1 - t0;
     if (idle_range(n, t0, t1, want, &s_abort)) return;
@@ -845,52 +875,48 @@ __global__ void __launch_bounds__(kBlock) k_fil_force_bulk(DevNet<float> n, int 
             s_abort = 1;
         }
         const ForceStage& S = stage[sidx];
+        const ForceRange rg = force_range(t.x, t.y, n.nb);
+        // every stretching and bending term touching the tile, once: term slot i
+        // belongs to bead q = t.x - 1 + i (the cylinder (q, q + 1) and the triple
+        // centred on q), for the tile and one halo bead on each side
+        for (int i = threadIdx.x; i < t.y - t.x + 2; i += blockDim.x) {
+            const int q = t.x - 1 + i;
+            if (q < 0 || q >= n.nb) continue;
+            const int fq = S.flag[q - rg.fs];
+            if (!(fq & 1)) continue;
+            const Pos<float> c0 = load_pos(S.x, q - rg.xs), c1 = load_pos(S.x, q + 1 - rg.xs);
+            const float4 pq = S.par[q - rg.ps];
+            float rp[3], st[3];
+            pdiff(c1, c0, rp);
+            stretch_force<float>(rp[0], rp[1], rp[2], pq.x, pq.y, st);
+            s_st[i][0] = st[0]; s_st[i][1] = st[1]; s_st[i][2] = st[2];
+            if (fq & 2) {
+                const Pos<float> cm = load_pos(S.x, q - 1 - rg.xs);
+                float rm[3], a1[3], a2[3];
+                pdiff(c0, cm, rm);
+                bend_force<float>(rm, rp, pq.z, pq.w, a1, a2);
+                s_a1[i][0] = a1[0]; s_a1[i][1] = a1[1]; s_a1[i][2] = a1[2];
+                s_a2[i][0] = a2[0]; s_a2[i][1] = a2[1]; s_a2[i][2] = a2[2];
+            }
+        }
+        __syncthreads();
         const int b = t.x + threadIdx.x;
         if (b < t.y) {
-            const ForceRange rg = force_range(t.x, t.y, n.nb);
             const int f0 = S.flag[b - rg.fs];
             const int fm = (f0 & 2) ? S.flag[b - 1 - rg.fs] : 0;
             const int fp = (f0 & 1) ? S.flag[b + 1 - rg.fs] : 0;
-            const Pos<float> p0 = load_pos(S.x, b - rg.xs);
-            const Pos<float> pm1 = (f0 & 2) ? load_pos(S.x, b - 1 - rg.xs) : p0;
-            const Pos<float> pp1 = (f0 & 1) ? load_pos(S.x, b + 1 - rg.xs) : p0;
-            const Pos<float> pm2 = (fm & 2) ? load_pos(S.x, b - 2 - rg.xs) : p0;
-            const Pos<float> pp2 = (fp & 1) ? load_pos(S.x, b + 2 - rg.xs) : p0;
-            const float4 prm = (f0 & 2) ? S.par[b - 1 - rg.ps] : make_float4(0.f, 0.f, 0.f, 0.f);
-            const float4 pr0 = S.par[b - rg.ps];
-            const float4 prp = (f0 & 1) ? S.par[b + 1 - rg.ps] : make_float4(0.f, 0.f, 0.f, 0.f);
-            float F[3] = {0.f, 0.f, 0.f};
-            float rm[3] = {0, 0, 0}, rp[3] = {0, 0, 0};
-            if (f0 & 2) pdiff(p0, pm1, rm);
-            if (f0 & 1) pdiff(pp1, p0, rp);
+            const int i = threadIdx.x + 1;   // this bead's term slot
             // stretching: cylinder (b-1, b) then (b, b+1); bending: triples centred on b-1, b, b+1
-            if (f0 & 2) {
-                float S1[3];
-                stretch_force<float>(rm[0], rm[1], rm[2], prm.x, prm.y, S1);
-                F[0] += S1[0]; F[1] += S1[1]; F[2] += S1[2];
-            }
-            if (f0 & 1) {
-                float S2[3];
-                stretch_force<float>(rp[0], rp[1], rp[2], pr0.x, pr0.y, S2);
-                F[0] += -S2[0]; F[1] += -S2[1]; F[2] += -S2[2];
-            }
-            if ((f0 & 2) && (fm & 2)) {
-                float r1[3], a1[3], a2[3];
-                pdiff(pm1, pm2, r1);
-                bend_force<float>(r1, rm, prm.z, prm.w, a1, a2);
-                F[0] += a2[0]; F[1] += a2[1]; F[2] += a2[2];
-            }
+            float F[3] = {0.f, 0.f, 0.f};
+            if (f0 & 2) { F[0] += s_st[i - 1][0]; F[1] += s_st[i - 1][1]; F[2] += s_st[i - 1][2]; }
+            if (f0 & 1) { F[0] += -s_st[i][0]; F[1] += -s_st[i][1]; F[2] += -s_st[i][2]; }
+            if ((f0 & 2) && (fm & 2)) { F[0] += s_a2[i - 1][0]; F[1] += s_a2[i - 1][1]; F[2] += s_a2[i - 1][2]; }
             if ((f0 & 3) == 3) {
-                float a1[3], a2[3];
-                bend_force<float>(rm, rp, pr0.z, pr0.w, a1, a2);
-                F[0] += a1[0] - a2[0]; F[1] += a1[1] - a2[1]; F[2] += a1[2] - a2[2];
+                F[0] += s_a1[i][0] - s_a2[i][0];
+                F[1] += s_a1[i][1] - s_a2[i][1];
+                F[2] += s_a1[i][2] - s_a2[i][2];
             }
-            if ((f0 & 1) && (fp & 1)) {
-                float r2[3], a1[3], a2[3];
-                pdiff(pp2, pp1, r2);
-                bend_force<float>(rp, r2, prp.z, prp.w, a1, a2);
-                F[0] += -a1[0]; F[1] += -a1[1]; F[2] += -a1[2];
-            }
+            if ((f0 & 1) && (fp & 1)) { F[0] += -s_a1[i + 1][0]; F[1] += -s_a1[i + 1][1]; F[2] += -s_a1[i + 1][2]; }
             float* Fo = n.f[fb ^ 1] + 3 * (size_t)b;
             Fo[0] = F[0];
             Fo[1] = F[1];
@@ -916,6 +942,8 @@ __global__ void __launch_bounds__(kBlock) k_fil_force_bulk(DevNet<float> n, int 
 
 // Mixed engine: persistent direction update d = F + beta d with the d.F partials.
 __global__ void __launch_bounds__(kBlock) k_direction_mx(DevNet<float> n) {
+    pdl_wait();      // the previous kernel of the main lane has finished
+    pdl_trigger();   // the next kernel of the main lane may be scheduled now
     MECH_TRACE_KERNEL(n, TK_DIRECTION_MX);
     __shared__ double sh[32];
     const int t0 = blockIdx.x * n.ptiles[2], t1 = min(t0 + n.ptiles[2], n.n_ftiles);
@@ -1093,6 +1121,8 @@ __global__ void __launch_bounds__(kBlock) k_bond_bnd(DevNet<Real> n, int want, i
 // ---------------------------------------------------------------------------
 template <typename Real>
 __global__ void __launch_bounds__(kBlock) k_direction(DevNet<Real> n) {
+    pdl_wait();      // the previous kernel of the main lane has finished
+    pdl_trigger();   // the next kernel of the main lane may be scheduled now
     MECH_TRACE_KERNEL(n, TK_DIRECTION);
     __shared__ double sh[32];
     __shared__ int s_go, s_fb, s_xb, s_bk;
@@ -1128,11 +1158,16 @@ __global__ void __launch_bounds__(kBlock) k_direction(DevNet<Real> n) {
 
 template <typename Real>
 __global__ void __launch_bounds__(kBlock) k_finalize_direction(DevNet<Real> n) {
+    pdl_wait();      // the previous kernel of the main lane has finished
+    pdl_trigger();   // the next kernel of the main lane may be scheduled now
     MECH_TRACE_KERNEL(n, TK_FIN_DIRECTION);
     __shared__ double sh[32];
     __shared__ int s_flag;
     const int r = blockIdx.x;
-    if (n.st[r].phase == PH_DIR) finalize_direction(n, r, sh);
+    CGState S;
+    if (threadIdx.x == 0) S = n.st[r];   // issued together with the loads below
+    const RepTiles rt = n.rt[r];
+    if (n.st[r].phase == PH_DIR) finalize_direction(n, r, rt, S, sh);
     after_phase(n, kCondDir, &s_flag);
 }
 
@@ -1141,7 +1176,12 @@ __global__ void __launch_bounds__(kBlock) k_finalize_direction(DevNet<Real> n) {
 // replica is resetting (it is in every iteration of the graph).
 template <typename Real>
 __global__ void __launch_bounds__(kBlock) k_reset(DevNet<Real> n) {
+    pdl_wait();      // the previous kernel of the main lane has finished
+    pdl_trigger();   // the next kernel of the main lane may be scheduled now
     MECH_TRACE_KERNEL(n, TK_RESET);
+    // the misc body of the conditional graph (failure dispatch is applied where a
+    // line search fails) counts its launches here
+    if (n.cond.on && blockIdx.x == 0 && threadIdx.x == 0) ++n.cond.counter[kCondMisc];
     __shared__ int s_go[kGatherTiles], s_fb[kGatherTiles], s_flag;
     const int t0 = blockIdx.x * kGatherTiles;
     if (threadIdx.x < kGatherTiles) {
@@ -1180,27 +1220,6 @@ __global__ void __launch_bounds__(kBlock) k_reset(DevNet<Real> n) {
     }
 }
 
-// lambda = 0 after a line search (CGMethod.hpp:1337-1367)
-__global__ void k_dispatch_failed(CGState* st, int R, int* misc_count) {
-    const int r = blockIdx.x * blockDim.x + threadIdx.x;
-    if (misc_count && r == 0) ++*misc_count;   // failure-dispatch bodies of the conditional graph
-    if (r >= R) return;
-    CGState& S = st[r];
-    if (S.phase != PH_FAILED) return;
-    if (!S.tryToRecover) {
-        S.errorFlags |= 1u;
-        S.status = MECH_ERR_LINESEARCH;
-        S.phase = PH_DONE;
-    } else if (!S.safeMode) {
-        S.safeMode = 1;
-        S.numSafeMode++;
-        S.phase = PH_RESET;
-    } else {
-        S.safeMode = 0;
-        S.numRecover++;
-        S.phase = PH_RECOVER;
-    }
-}
 
 // Recovery move: step = maxDist / max_i |d_i|, x += step d (MController.h:273-339).
 template <typename Real>
@@ -1287,6 +1306,10 @@ static int n_lm_tiles(const DevNet<Real>& n, int* ev_tiles, int* bb_tiles) {
 // The excluded-volume chain and the linker/motor/boundary kernel on side
 // lanes, the filament kernel on the main lane, then (after the joins) the
 // reduction on the main lane.
+// The filament kernel of an evaluation is launched before the side lanes when
+// its residency is capped (n.fil_first[k]): its blocks then start streaming at
+// once and the excluded-volume and linker kernels fill the room the cap leaves;
+// uncapped, it fills every SM and is launched after them.
 template <typename Real>
 int launch_energy(const DevNet<Real>& n, int want, int trial, const Lanes& L) {
     int ev_t = 0, bb_t = 0;
@@ -1295,6 +1318,11 @@ int launch_energy(const DevNet<Real>& n, int want, int trial, const Lanes& L) {
     cudaEventRecord(L.fork, L.main);
     cudaStreamWaitEvent(L.side, L.fork, 0);
     cudaStreamWaitEvent(L.side2, L.fork, 0);
+    auto fil = [&] {
+        if constexpr (sizeof(Real) == 4) launch_k(n.pdl, k_fil_energy_bulk, n.pgrid[0], kBlock, L.main, n, want, trial);
+        else launch_k(n.pdl, k_fil_energy<Real>, n.n_ftiles, kBlock, L.main, n, want, trial);
+    };
+    if (n.fil_first[0]) fil();
     launched += launch_exvol_energy<Real>(n, want, trial, L.side, false);
     cudaEventRecord(L.join, L.side);
     if (lm + bb_t > 0) {
@@ -1302,8 +1330,7 @@ int launch_energy(const DevNet<Real>& n, int want, int trial, const Lanes& L) {
         ++launched;
     }
     cudaEventRecord(L.join2, L.side2);
-    if constexpr (sizeof(Real) == 4) k_fil_energy_bulk<<<n.pgrid[0], kBlock, 0, L.main>>>(n, want, trial);
-    else k_fil_energy<Real><<<n.n_ftiles, kBlock, 0, L.main>>>(n, want, trial);
+    if (!n.fil_first[0]) fil();
     cudaStreamWaitEvent(L.main, L.join, 0);
     cudaStreamWaitEvent(L.main, L.join2, 0);
     k_finalize_energy<Real><<<n.R, kBlock, 0, L.main>>>(n, want, trial);
@@ -1318,6 +1345,11 @@ int launch_forces(const DevNet<Real>& n, int want, const Lanes& L) {
     cudaEventRecord(L.fork, L.main);
     cudaStreamWaitEvent(L.side, L.fork, 0);
     cudaStreamWaitEvent(L.side2, L.fork, 0);
+    auto fil = [&] {
+        if constexpr (sizeof(Real) == 4) launch_k(n.pdl, k_fil_force_bulk, n.pgrid[1], kBlock, L.main, n, want);
+        else launch_k(n.pdl, k_fil_force<Real>, n.n_ftiles, kBlock, L.main, n, want);
+    };
+    if (n.fil_first[1]) fil();
     launched += launch_exvol_forces<Real>(n, want, L.side, false);
     cudaEventRecord(L.join, L.side);
     if (lm + bb_t > 0) {
@@ -1325,27 +1357,26 @@ int launch_forces(const DevNet<Real>& n, int want, const Lanes& L) {
         ++launched;
     }
     cudaEventRecord(L.join2, L.side2);
-    if constexpr (sizeof(Real) == 4) k_fil_force_bulk<<<n.pgrid[1], kBlock, 0, L.main>>>(n, want);
-    else k_fil_force<Real><<<n.n_ftiles, kBlock, 0, L.main>>>(n, want);
+    if (!n.fil_first[1]) fil();
     cudaStreamWaitEvent(L.main, L.join, 0);
     cudaStreamWaitEvent(L.main, L.join2, 0);
     if constexpr (sizeof(Real) == 4) k_force_gather_mx<<<(n.n_ftiles + kGatherTiles - 1) / kGatherTiles, kBlock, 0, L.main>>>(n, want);
     else k_force_gather<Real><<<(n.n_ftiles + kGatherTiles - 1) / kGatherTiles, kBlock, 0, L.main>>>(n, want);
-    k_finalize_force<Real><<<n.R, kBlock, 0, L.main>>>(n, want);
+    launch_k(n.pdl, k_finalize_force<Real>, n.R, kBlock, L.main, n, want);
     return launched + 3;
 }
 
 template <typename Real>
 int launch_direction(const DevNet<Real>& n, cudaStream_t s) {
-    if constexpr (sizeof(Real) == 4) k_direction_mx<<<n.pgrid[2], kBlock, 0, s>>>(n);
-    else k_direction<Real><<<n.n_ftiles, kBlock, 0, s>>>(n);
-    k_finalize_direction<Real><<<n.R, kBlock, 0, s>>>(n);
+    if constexpr (sizeof(Real) == 4) launch_k(n.pdl, k_direction_mx, n.pgrid[2], kBlock, s, n);
+    else launch_k(n.pdl, k_direction<Real>, n.n_ftiles, kBlock, s, n);
+    launch_k(n.pdl, k_finalize_direction<Real>, n.R, kBlock, s, n);
     return 2;
 }
 
 template <typename Real>
 int launch_reset(const DevNet<Real>& n, cudaStream_t s) {
-    k_reset<Real><<<(n.n_ftiles + kGatherTiles - 1) / kGatherTiles, kBlock, 0, s>>>(n);
+    launch_k(n.pdl, k_reset<Real>, (n.n_ftiles + kGatherTiles - 1) / kGatherTiles, kBlock, s, n);
     return 1;
 }
 
@@ -1355,11 +1386,6 @@ int launch_body_head(const DevNet<Real>& n, cudaStream_t s) {
     return 1;
 }
 
-template <typename Real>
-int launch_dispatch_failed(const DevNet<Real>& n, cudaStream_t s) {
-    k_dispatch_failed<<<(n.R + 127) / 128, 128, 0, s>>>(n.st, n.R, n.cond.on ? n.cond.counter + kCondMisc : nullptr);
-    return 1;
-}
 
 template <typename Real>
 int launch_recover(const DevNet<Real>& n, const Lanes& L) {
@@ -1439,7 +1465,6 @@ int persistent_blocks(int device, int which, int per_sm) {
     template int launch_forces<R>(const DevNet<R>&, int, const Lanes&);                 \
     template int launch_direction<R>(const DevNet<R>&, cudaStream_t);                   \
     template int launch_reset<R>(const DevNet<R>&, cudaStream_t);                       \
-    template int launch_dispatch_failed<R>(const DevNet<R>&, cudaStream_t);             \
     template int launch_body_head<R>(const DevNet<R>&, cudaStream_t);                   \
     template int launch_recover<R>(const DevNet<R>&, const Lanes&);                     \
     template int launch_backup_restore<R>(const DevNet<R>&, cudaStream_t);

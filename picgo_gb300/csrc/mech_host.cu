@@ -109,13 +109,16 @@ struct MechContext {
     // force kernels, and a multiplier on the default neighbor-list bin edge
     int tile_cap[2] = {kFilBulkMaxTiles, kFilBulkMaxTiles};
     // resident blocks per SM of the persistent filament energy / force kernels
-    // (0: as many as fit); fewer leave room for the lanes running beside them.
-    // The force kernel defaults to 3 of its 4: the fourth block's registers
-    // would keep the excluded-volume lane's extended-precision pass (102
-    // registers x 128 threads) waiting for a slot while the forces stream
-    // (measured on the 1M-cylinder network: 157 against 173 us per iteration
-    // over the first 300 iterations, no change later in the run).
-    int blocks_per_sm[2] = {0, 3};
+    // (0: as many as fit); fewer leave room for the lanes running beside them,
+    // and a capped kernel is launched before those lanes.  The force kernel
+    // defaults to 2: its blocks stream from the start of the evaluation while
+    // the excluded-volume chain (FP32 pass, extended-precision pass, fallbacks)
+    // and the linker kernel keep room on every SM.  Force evaluation on the
+    // 1M-cylinder network, graph replays at fixed states: 77 us at 2 blocks,
+    // 95 at 3, 125 uncapped (the kernel alone: 28.7, 22.6, 20.5 us).  A cap on
+    // the energy kernel only delays the excluded-volume chain (trial pass 78 us
+    // uncapped, 90 at 2, 107 at 3).
+    int blocks_per_sm[2] = {0, 2};
     double cell_scale = 1.0;
     int sp_tiles_c[K_NUM_SPARSE] = {0, 0, 0, 0};
     int slot_base[K_NUM_SPARSE + 1] = {0, 0, 0, 0, 0};
@@ -183,6 +186,7 @@ DevNet<Real> make_devnet(MechContext* c) {
     n.ftile = (c->compact ? c->ftile_c : c->ftile).as<Tile>();
     for (int k = 0; k < 3; ++k) {
         const int per_sm = k < 2 ? c->blocks_per_sm[k] : 0;
+        if (k < 2) n.fil_first[k] = (c->precision == MECH_PREC_MIXED && per_sm > 0) ? 1 : 0;
         const int resident = persistent_blocks(c->device, k, per_sm);
         n.pgrid[k] = std::max(1, std::min(n.n_ftiles, resident));
         n.ptiles[k] = (n.n_ftiles + n.pgrid[k] - 1) / n.pgrid[k];
@@ -997,7 +1001,8 @@ static int trial_launches(const DevNet<Real>& n, const Lanes& L) {
 
 template <typename Real>
 static int capture_iteration_graph(MechContext* c, cudaGraphExec_t* exec, int* nlaunch) {
-    const DevNet<Real> n = make_devnet<Real>(c);
+    DevNet<Real> n = make_devnet<Real>(c);
+    n.pdl = c->graph_mode == MECH_GRAPH_UNROLLED_PDL ? 1 : 0;
     cudaGraph_t g = nullptr;
     CU(cudaStreamBeginCapture(c->stream, cudaStreamCaptureModeThreadLocal));
     int k = 0;
@@ -1005,7 +1010,6 @@ static int capture_iteration_graph(MechContext* c, cudaGraphExec_t* exec, int* n
         k += trial_launches<Real>(n, c->lanes());
         k += launch_forces<Real>(n, PH_FORCE, c->lanes());
         k += launch_direction<Real>(n, c->stream);
-        k += launch_dispatch_failed<Real>(n, c->stream);
         k += launch_reset<Real>(n, c->stream);
     }
     cudaError_t e = cudaStreamEndCapture(c->stream, &g);
@@ -1025,7 +1029,7 @@ static constexpr int kBodiesPerLaunch = 512;
 
 // The minimizer as one conditional graph: a while loop whose body is
 //   head -> if (trial) energy at x + lambda d -> if (force) forces
-//        -> if (direction) d = F + beta d -> if (misc) failure dispatch, reset.
+//        -> if (direction) d = F + beta d -> if (misc) reset (d = F).
 // The head sets the four conditions from the replicas' phases and whether the
 // loop runs another body; each phase's reduction sets them again for the
 // phases after it in the same body.  Only phases some replica is in run, and
@@ -1100,10 +1104,9 @@ static int capture_conditional_graph(MechContext* c, cudaGraphExec_t* exec, Cond
     if ((e = add_if(h[2], [&] { counts->dir = launch_direction<Real>(n, c->stream); })) != cudaSuccess)
         return fail(e, "direction body");
     if ((e = add_if(h[3], [&] {
-             counts->misc = launch_dispatch_failed<Real>(n, c->stream);
-             counts->misc += launch_reset<Real>(n, c->stream);
+             counts->misc = launch_reset<Real>(n, c->stream);
          })) != cudaSuccess)
-        return fail(e, "dispatch body");
+        return fail(e, "reset body");
     e = cudaGraphInstantiate(exec, g, cudaGraphInstantiateFlagUseNodePriority);
     cudaGraphDestroy(g);
     g = nullptr;
@@ -1695,7 +1698,8 @@ int32_t mech_get_stretch_forces(MechContext* ctx, int32_t r, double* linker_f, d
 
 int32_t mech_set_graph_mode(MechContext* ctx, int32_t mode) {
     if (!ctx) return set_err(MECH_ERR_ARG, "null context");
-    if (mode != MECH_GRAPH_CONDITIONAL && mode != MECH_GRAPH_UNROLLED) return set_err(MECH_ERR_ARG, "bad graph mode");
+    if (mode != MECH_GRAPH_CONDITIONAL && mode != MECH_GRAPH_UNROLLED && mode != MECH_GRAPH_UNROLLED_PDL)
+        return set_err(MECH_ERR_ARG, "bad graph mode");
     ctx->graph_mode = mode;
     return MECH_OK;
 }
@@ -1788,7 +1792,6 @@ static int profile_impl(MechContext* c, int iters, MechProfile* o) {
         trial_launches<Real>(n, c->lanes());
         launch_forces<Real>(n, PH_FORCE, c->lanes());
         launch_direction<Real>(n, s);
-        launch_dispatch_failed<Real>(n, s);
         launch_reset<Real>(n, s);
     });
     std::copy(saved.begin(), saved.end(), c->h_st);

@@ -139,6 +139,7 @@ struct DevNet {
     int n_ftiles;
     const Tile* ftile;
     int pgrid[3], ptiles[3];   // [0] energy, [1] force, [2] direction kernels
+    int fil_first[2];          // energy / force: filament kernel launched before the side lanes (capped residency)
     // sparse interactions (internal bead indices)
     int n_lk, n_mt, n_ev, n_bb;
     const int4* lk_bead; const Real* lk_k; const Real* lk_l0; const Real* lk_s1; const Real* lk_s2;
@@ -179,6 +180,10 @@ struct DevNet {
     int* gticket;           // whole-grid ticket
     unsigned* err;          // device error word
     GraphConds cond;
+    // programmatic dependent launch on the main lane (MECH_GRAPH_UNROLLED_PDL):
+    // the kernels that follow a reduction, and the reductions themselves, are
+    // scheduled while their predecessor runs and wait for it (griddepcontrol)
+    int pdl;
     // diagnostic (mech_energy_terms; null otherwise): the filament energy
     // kernels also store each bead's stretching [b] and bending [nb + b] term
     double* terms;
@@ -234,6 +239,35 @@ __device__ __forceinline__ Real* slot_ptr(const DevNet<Real>& n, int slot) {
 }
 #endif
 
+// Launch of `kernel` on stream `s`, with programmatic stream serialization when
+// `pdl` is set: the kernel may then start while the previous kernel of the
+// stream is still running (once that kernel's blocks have called pdl_trigger()),
+// and calls pdl_wait() before it reads anything the previous kernel wrote.
+template <typename... KArgs, typename... Args>
+inline void launch_k(bool pdl, void (*kernel)(KArgs...), unsigned grid, unsigned block, cudaStream_t s,
+                     Args... args) {
+    if (!pdl) {
+        kernel<<<grid, block, 0, s>>>(args...);
+        return;
+    }
+    cudaLaunchConfig_t cfg{};
+    cfg.gridDim = dim3(grid);
+    cfg.blockDim = dim3(block);
+    cfg.dynamicSmemBytes = 0;
+    cfg.stream = s;
+    cudaLaunchAttribute attr[1];
+    attr[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
+    attr[0].val.programmaticStreamSerializationAllowed = 1;
+    cfg.attrs = attr;
+    cfg.numAttrs = 1;
+    cudaLaunchKernelEx(&cfg, kernel, static_cast<KArgs>(args)...);
+}
+#ifdef __CUDACC__
+// no-ops for a kernel launched without programmatic serialization
+__device__ __forceinline__ void pdl_wait() { asm volatile("griddepcontrol.wait;" ::: "memory"); }
+__device__ __forceinline__ void pdl_trigger() { asm volatile("griddepcontrol.launch_dependents;" :::); }
+#endif
+
 // ---- kernels (mech_ff.cu) -------------------------------------------------
 // mode: 0 = line-search trial at x + lambda d (replicas in PH_LS_TRIAL),
 //       1 = plain evaluation at x (replicas with active != 0)
@@ -252,7 +286,6 @@ template <typename Real> int launch_energy(const DevNet<Real>& n, int want, int 
 template <typename Real> int launch_forces(const DevNet<Real>& n, int want, const Lanes& L);
 template <typename Real> int launch_direction(const DevNet<Real>& n, cudaStream_t s);
 template <typename Real> int launch_reset(const DevNet<Real>& n, cudaStream_t s);
-template <typename Real> int launch_dispatch_failed(const DevNet<Real>& n, cudaStream_t s);
 // head of a body of the minimizer's conditional graph: sets the phase
 // conditions, counts the body and decides whether the loop continues
 template <typename Real> int launch_body_head(const DevNet<Real>& n, cudaStream_t s);

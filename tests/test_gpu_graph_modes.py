@@ -1,8 +1,10 @@
-"""The conditional minimizer graph against the unrolled one.
+"""The minimizer's graph modes against each other.
 
-Both run the same active kernels in the same order (the conditional graph only
-skips the phases no replica is in), so minimizations must agree bit for bit:
-iteration and call counts, energies, final coordinates.
+All run the same active kernels in the same order (the conditional graph only
+skips the phases no replica is in; the programmatic-launch variant of the
+unrolled graph only lets kernels be scheduled before their predecessor ends),
+so minimizations must agree bit for bit: iteration and call counts, energies,
+final coordinates.
 """
 import numpy as np
 import pytest
@@ -43,8 +45,10 @@ def test_conditional_graph_matches_unrolled_graph(precision):
     p = cg_params(energy_rel_tol=0.0)
     a = _run(precision, [net], "conditional", p)
     b = _run(precision, [net], "unrolled", p)
+    c = _run(precision, [net], "unrolled_pdl", p)
     assert a[0][0]["status"] == 0 and a[0][0]["grad_inf_norm"] < 1.0
     _same(a, b)
+    _same(b, c)
 
 
 def test_conditional_graph_matches_unrolled_graph_batched():
@@ -52,5 +56,7 @@ def test_conditional_graph_matches_unrolled_graph_batched():
     p = cg_params(energy_rel_tol=0.0)
     a = _run("mixed", nets, "conditional", p)
     b = _run("mixed", nets, "unrolled", p)
+    c = _run("mixed", nets, "unrolled_pdl", p)
     assert all(r["status"] == 0 for r in a[0])
     _same(a, b)
+    _same(b, c)
