@@ -379,7 +379,7 @@ def c3_report(seed: int = 20261203 + 1):
     return out
 
 
-def c5_report(n_params: int = 64, seed: int = 20261203 + 5, budget_s: float = 420.0):
+def c5_report(n_params: int = 64, seed: int = 20261203 + 5, budget_s: float = 240.0):
     """Implicit adjoint on the 2,000 x 30 network with 5,000 linkers (k ~ U(4, 12),
     l0 ~ U(20, 40)): L = E(x*) + mean over filaments |end - start|^2.  The adjoint
     gradient of L in per-linker k and l0 (GPU FP64: CG, Newton refinement to 1e-9 pN,
@@ -387,8 +387,11 @@ def c5_report(n_params: int = 64, seed: int = 20261203 + 5, budget_s: float = 42
     reference on `n_params` random parameters: each side re-equilibrated from x* by
     Newton refinement alone (x*(theta +- h) is a 1e-4 perturbation of x*), its loss
     evaluated by the CPU oracle at the refined coordinates with the device's lists.
-    Parameters are checked until `budget_s` seconds of finite differences have
-    passed; the report says how many were."""
+    The lists stay those the FP64 minimization was run with (built at its start):
+    E is the energy of that fixed list, as in one MEDYAN minimization, and a list
+    rebuilt at x* after the long descent would hold pairs that moved into contact
+    while no term kept them apart.  Parameters are checked until `budget_s` seconds
+    of finite differences have passed; the report says how many were."""
     import numpy as np
     import oracle
     from picgo_gb300 import Engine, make_network
@@ -419,16 +422,32 @@ def c5_report(n_params: int = 64, seed: int = 20261203 + 5, budget_s: float = 42
     with Engine("fp64") as eng:
         eng.set_network(net)
         eng.set_coords(x0)
-        r = eng.minimize(cg(grad_tol=1e-2, force_call_limit=400_000))[0]
-        log(f"FP64 CG: {r['num_iter']} iterations, max|F| {r['grad_inf_norm']:.3g}")
-        # the neighbor lists of x*, as the oracle builds them for the loss: rebuild there, then Newton
-        x_lists = eng.coords()
-        eng.rebuild()
-        info = eng.newton_refine(40, 1e-9, 1e-8, 20000)
+        eng.rebuild()   # the lists of this minimization, at x0; kept through Newton, adjoint and FD
+        x_lists = x0
+        # FP64 CG to 1e-2 pN, then damped Newton; where Newton meets negative
+        # curvature the CG end was not a strict minimum (it descends from
+        # there), so CG and Newton alternate until Newton converges on a
+        # positive-definite Hessian or the equilibration budget runs out
+        stages = []
+        for stage in range(8):
+            r = eng.minimize(cg(grad_tol=1e-2, force_call_limit=400_000))[0]
+            info = eng.newton_refine(40, 1e-9, 1e-8, 20000)
+            stages.append({"cg_iterations": r["num_iter"], "cg_max_force_pN": r["grad_inf_norm"],
+                           "newton_steps": info["newton_steps"], "newton_cg_iterations": info["iterations"],
+                           "newton_max_force_pN": info["max_force"],
+                           "negative_curvature": info["negative_curvature"]})
+            log(f"stage {stage}: FP64 CG {r['num_iter']} iterations to {r['grad_inf_norm']:.3g} pN; Newton "
+                f"{info['newton_steps']} steps, {info['iterations']} CG iterations, max|F| {info['max_force']:.3g}, "
+                f"negative curvature {info['negative_curvature']}")
+            if info["max_force"] < 1e-6 and not info["negative_curvature"]:
+                break
+            if time.perf_counter() - t0 > 0.6 * budget_s:
+                break
         xs = eng.coords()
-        log(f"Newton: {info['newton_steps']} steps, {info['iterations']} CG iterations, max|F| {info['max_force']:.3g}")
+        out["equilibration_stages"] = stages
         out["equilibrate_s"] = round(time.perf_counter() - t0, 2)
         out["equilibrium_max_force_pN"] = info["max_force"]
+        out["strict_minimum"] = bool(info["max_force"] < 1e-6 and not info["negative_curvature"])
         lx, g = reg(xs)
         ta = time.perf_counter()
         gk, gl, ainfo = eng.adjoint(g, 1.0)
@@ -628,6 +647,13 @@ def probe(args):
         elif args.evals > 0:
             out["profile"] = eng.profile(args.evals)
         else:
+            if args.skip_calls > 0:
+                # descend first without a timeline (a diagnostic build writes one
+                # per minimization when MECH_TRACE_FILE is set)
+                dump = os.environ.pop("MECH_TRACE_FILE", None)
+                eng.minimize(cg(energy_call_limit=args.skip_calls))
+                if dump is not None:
+                    os.environ["MECH_TRACE_FILE"] = dump
             t0 = time.perf_counter()
             r = eng.minimize(cg(energy_call_limit=args.energy_calls))[0]
             out["seconds"] = round(time.perf_counter() - t0, 4)
@@ -660,6 +686,8 @@ def main():
     ap.add_argument("--workload", default="c2", help="probe: network config name (c1, c2, c5)")
     ap.add_argument("--seed", type=int, default=None, help="probe: network seed (default: the config's)")
     ap.add_argument("--energy-calls", type=int, default=40, help="probe: energy calls of the bounded minimization")
+    ap.add_argument("--skip-calls", type=int, default=0,
+                    help="probe: energy calls of an earlier minimization from the start, without a timeline")
     ap.add_argument("--evals", type=int, default=0, help="probe: launches per evaluation kernel (mech_profile)")
     ap.add_argument("--forces", type=int, default=0, help="probe: only this many mech_forces calls")
     ap.add_argument("--energies", type=int, default=0, help="probe: only this many mech_energy calls")

@@ -406,8 +406,9 @@ int32_t mech_adjoint(MechContext* ctx, int32_t replica, const double* dL_dx, dou
 
 /* Newton refinement of every replica's equilibrium (run after mech_minimize):
  * dx = (H + shift I)^-1 F by CG (truncated at non-positive curvature), then
- * x += alpha dx with alpha halved from 1 until max |F| decreases; repeated
- * until max |F| < force_tol, max_steps steps, or no decrease. */
+ * x += alpha dx, alpha halved from 1 until the energy drops or max |F|
+ * halves (shift grows tenfold when no alpha does); repeated until
+ * max |F| < force_tol, max_steps steps, or no progress. */
 int32_t mech_newton_refine(MechContext* ctx, int32_t max_steps, double force_tol, const MechSolveParams* sp,
                            MechSolveInfo* info);
 

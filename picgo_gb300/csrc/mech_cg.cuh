@@ -37,8 +37,9 @@ __device__ __forceinline__ int run_slot(int b, int stride, int k) {
 // added in pair order (only entries recorded at step `lam` when `match_lam`).
 // A failed pair makes the force field report -1 (CylinderExclVolRepulsion.cpp:442-481).
 template <typename Real>
-__device__ void add_fallback_energies(const DevNet<Real>& n, int r, bool match_lam, double lam, double* e) {
-    const int cnt = min(__ldcg(n.ev_fb_count), kExvolFallbackCap);
+__device__ void add_fallback_energies(const DevNet<Real>& n, int r, int fb_count, bool match_lam, double lam,
+                                      double* e) {
+    const int cnt = min(fb_count, kExvolFallbackCap);
     int last = -1;
     bool ev_failed = false;
     for (;;) {
@@ -89,6 +90,10 @@ __device__ void finalize_energy(const DevNet<Real>& n, int r, int trial, const R
     const int ffk[K_NUM_SPARSE] = {MECH_FF_LINKER, MECH_FF_MOTOR, MECH_FF_EXVOL, MECH_FF_BOUNDARY};
     double e[MECH_NUM_FF], e2[MECH_NUM_FF];
     const bool dual = sizeof(Real) == 4 && trial == kTrialDual;
+    // the fallback list's length, loaded now so that thread 0's step logic does
+    // not wait on it at the end
+    const int fb_count = threadIdx.x == 0 ? __ldcg(n.ev_fb_count) : 0;
+    MECH_TRACE_STAMP(ts_load);
     if constexpr (sizeof(Real) == 4) {
         // mixed: (hi, lo) pair slots summed compensated in single precision;
         // the doubles are formed in thread 0 only.  acc[0, 6): the (first)
@@ -128,18 +133,36 @@ __device__ void finalize_energy(const DevNet<Real>& n, int r, int trial, const R
                 if (dual) add_pair(acc[MECH_NUM_FF + ffk[k]], load_pair(n.part_sp2 + i));
             }
         }
+        MECH_TRACE_SECTION(n, TK_SEC_FE_LOAD, ts_load);
+        MECH_TRACE_STAMP(ts_red);
         if (dual) {
             block_reduce_ff<2 * MECH_NUM_FF, 0>(acc, nullptr, reinterpret_cast<float*>(sh));
         } else {
             FF (&a6)[MECH_NUM_FF] = *reinterpret_cast<FF(*)[MECH_NUM_FF]>(acc);
             block_reduce_ff<MECH_NUM_FF, 0>(a6, nullptr, reinterpret_cast<float*>(sh));
         }
-        if (threadIdx.x != 0) return;
+        MECH_TRACE_SECTION(n, TK_SEC_FE_REDUCE, ts_red);
+        if (threadIdx.x >= 32) return;
+        // hi + lo in double, one pair per lane of warp 0: an FP64 warp
+        // instruction costs the same with 1 or 12 active lanes, so the
+        // conversions take 3 warp instructions instead of 36 in thread 0
+        const int lane = threadIdx.x;
+        float ph = 0.f, pl = 0.f;
+#pragma unroll
+        for (int k = 0; k < 2 * MECH_NUM_FF; ++k) {
+            const float h = __shfl_sync(0xffffffffu, acc[k].h, 0), l = __shfl_sync(0xffffffffu, acc[k].l, 0);
+            if (lane == k) {
+                ph = h;
+                pl = l;
+            }
+        }
+        const double v = (double)ph + (double)pl;
 #pragma unroll
         for (int k = 0; k < MECH_NUM_FF; ++k) {
-            e[k] = (double)acc[k].h + (double)acc[k].l;
-            e2[k] = (double)acc[MECH_NUM_FF + k].h + (double)acc[MECH_NUM_FF + k].l;
+            e[k] = __shfl_sync(0xffffffffu, v, k);
+            e2[k] = __shfl_sync(0xffffffffu, v, MECH_NUM_FF + k);
         }
+        if (threadIdx.x != 0) return;
     } else {
         // every thread issues its loads back to back, then sums in a fixed order
         double acc[MECH_NUM_FF] = {0, 0, 0, 0, 0, 0};
@@ -162,9 +185,10 @@ __device__ void finalize_energy(const DevNet<Real>& n, int r, int trial, const R
         block_combine<MECH_NUM_FF>(e, ops, sh);
         if (threadIdx.x != 0) return;
     }
+    MECH_TRACE_STAMP(ts_tail);
     const double lam = S.lambda;   // the (first) trial's step, before the line search moves it
     const int xb = S.xbuf;
-    add_fallback_energies(n, r, dual, lam, e);
+    add_fallback_energies(n, r, fb_count, dual, lam, e);
     const double E = record_energies(S, e);
     if (trial && S.phase == PH_LS_TRIAL) {
         S.Etrial = E;
@@ -173,7 +197,7 @@ __device__ void finalize_energy(const DevNet<Real>& n, int r, int trial, const R
         if (dual && S.phase == PH_LS_TRIAL) {
             // rejected at lambda and halved: the reference's next trial, at
             // lambda / 2, was evaluated by the same pass (positions in the third buffer)
-            add_fallback_energies(n, r, true, S.lambda, e2);
+            add_fallback_energies(n, r, fb_count, true, S.lambda, e2);
             const double E2 = record_energies(S, e2);
             S.Etrial = E2;
             line_search_step(S, E2, (xb + 2) % 3);
@@ -187,6 +211,7 @@ __device__ void finalize_energy(const DevNet<Real>& n, int r, int trial, const R
         S.E0 = E;
     }
     n.st[r] = S;
+    MECH_TRACE_SECTION(n, TK_SEC_FE_TAIL, ts_tail);
 }
 
 // CG bookkeeping after the forces (CGMethod.hpp:1540-1580): max |F|, beta.
@@ -227,15 +252,18 @@ __device__ __forceinline__ void force_step(CGState& S, double mx, double ff, dou
 
 template <typename Real>
 __device__ void finalize_force(const DevNet<Real>& n, int r, const RepTiles& rt, CGState& S, double* sh) {
-    const int stride = 1;   // k_force_gather writes one slot per tile
+    // k_force_gather writes one slot per tile, k_force_gather_mx one per run of
+    // a replica's tiles in a block
+    const int stride = sizeof(Real) == 4 ? kGatherTiles : 1;
     const int nslot = run_slots(rt.fil_begin, rt.fil_end, stride);
     double mx, ff, ffp;
+    MECH_TRACE_STAMP(ts_load);
     if constexpr (sizeof(Real) == 4) {
         // mixed slots hold float maxima and (hi, lo) pairs; sum them compensated
         // in single precision and form the doubles in thread 0 only
         FF a[2];
         float m[1] = {0.f};
-#pragma unroll 16
+#pragma unroll 4
         for (int k = threadIdx.x; k < nslot; k += blockDim.x) {
             const float* p = reinterpret_cast<const float*>(n.part_fil + 4 * (size_t)run_slot(rt.fil_begin, stride, k));
             const float4 v = __ldcg(reinterpret_cast<const float4*>(p));
@@ -246,7 +274,10 @@ __device__ void finalize_force(const DevNet<Real>& n, int r, const RepTiles& rt,
             a[1].add(v.w);
             a[1].add(w);
         }
+        MECH_TRACE_SECTION(n, TK_SEC_FF_LOAD, ts_load);
+        MECH_TRACE_STAMP(ts_red);
         block_reduce_pairs<2, 1>(a, m, reinterpret_cast<float*>(sh));
+        MECH_TRACE_SECTION(n, TK_SEC_FF_REDUCE, ts_red);
         if (threadIdx.x != 0) return;
         mx = (double)m[0];
         ff = (double)a[0].h + (double)a[0].l;
@@ -270,8 +301,10 @@ __device__ void finalize_force(const DevNet<Real>& n, int r, const RepTiles& rt,
         ffp = red[2];
         if (threadIdx.x != 0) return;
     }
+    MECH_TRACE_STAMP(ts_tail);
     force_step(S, mx, ff, ffp);
     n.st[r] = S;
+    MECH_TRACE_SECTION(n, TK_SEC_FF_TAIL, ts_tail);
 }
 
 // One block per replica after the direction update: the slope d.F, the

@@ -184,8 +184,8 @@ __global__ void __launch_bounds__(kBlock) k_fil_energy(DevNet<Real> n, int want,
                     eb = bend_energy<Real>(r1, r2, kb, t0);
                 }
                 if (n.terms) {
-                    n.terms[j] = (double)es;
-                    n.terms[(size_t)n.nb + j] = (double)eb;
+                    n.terms[j] = es;
+                    n.terms[(size_t)n.nb + j] = eb;
                 }
             }
         }
@@ -283,7 +283,6 @@ __global__ void __launch_bounds__(kBlock) k_fil_force(DevNet<Real> n, int want) 
 // before the per-tile reductions, so a thread keeps several beads' loads in
 // flight; the mixed engine's version is k_force_gather_mx below.
 // ---------------------------------------------------------------------------
-constexpr int kGatherTiles = 4;
 
 template <typename Real>
 __device__ __forceinline__ void gather_bead(const DevNet<Real>& n, int b, int fb, Real& mx, Real& ff, Real& ffp) {
@@ -355,25 +354,29 @@ __global__ void __launch_bounds__(kBlock) k_force_gather(DevNet<Real> n, int wan
 // whose force records (4 x 12 B) move as three 16-byte vectors, when the tile
 // starts on a multiple of 4 beads (always, unless a replica before it has a
 // bead count that is not; a partial group at the tile's end goes bead by
-// bead); otherwise 4 beads strided by 64.  The tile's partials combine the
-// two warps of its 64 threads.
+// bead); otherwise 4 beads strided by 64.  The block's partials combine, in
+// warp order, the warps of each run of its tiles that belong to one replica,
+// into the slot of the run's first tile (run_slot with stride kGatherTiles),
+// so the force finalizer reads a quarter of the slots one per tile would take.
 __global__ void __launch_bounds__(kBlock) k_force_gather_mx(DevNet<float> n, int want) {
     pdl_trigger();   // the next kernel of the main lane may be scheduled now
     MECH_TRACE_KERNEL(n, TK_GATHER_MX);
     static_assert(kFilTile == 256 && kBlock == 64 * kGatherTiles, "64 threads x 4 beads per tile");
     __shared__ float sh[8][5];   // per warp: F.F (hi, lo), F.Fprev (hi, lo), max
-    __shared__ int s_go[kGatherTiles], s_fb[kGatherTiles];
+    __shared__ int s_go[kGatherTiles], s_fb[kGatherTiles], s_rep[kGatherTiles];
     const int t0 = blockIdx.x * kGatherTiles;
     if (threadIdx.x < kGatherTiles) {
         const int ti = t0 + threadIdx.x;
-        int go = 0, fb = 0;
+        int go = 0, fb = 0, rep = -1;
         if (ti < n.n_ftiles) {
-            const CGState& S = n.st[n.ftile[ti].replica];
+            rep = n.ftile[ti].replica;
+            const CGState& S = n.st[rep];
             go = replica_selected(S, want);
             fb = S.fbuf;
         }
         s_go[threadIdx.x] = go;
         s_fb[threadIdx.x] = fb;
+        s_rep[threadIdx.x] = rep;
     }
     __syncthreads();
     const int j = threadIdx.x >> 6, tt = threadIdx.x & 63;
@@ -442,18 +445,23 @@ __global__ void __launch_bounds__(kBlock) k_force_gather_mx(DevNet<float> n, int
         sh[w][4] = mx;
     }
     __syncthreads();
-    if (threadIdx.x < kGatherTiles && s_go[threadIdx.x]) {
-        // the tile's two warps, combined with an error-free sum
-        const int a = 2 * threadIdx.x, b = a + 1;
-        float s1, e1, s2, e2, h, l;
-        two_sum(sh[a][0], sh[b][0], s1, e1);
-        fast_two_sum(s1, __fadd_rn(e1, __fadd_rn(sh[a][1], sh[b][1])), h, l);
-        const float ffh = h, ffl = l;
-        two_sum(sh[a][2], sh[b][2], s2, e2);
-        fast_two_sum(s2, __fadd_rn(e2, __fadd_rn(sh[a][3], sh[b][3])), h, l);
-        float* p = reinterpret_cast<float*>(n.part_fil + 4 * (size_t)(t0 + threadIdx.x));
-        *reinterpret_cast<float4*>(p) = make_float4(fmaxf(sh[a][4], sh[b][4]), ffh, ffl, h);
-        p[4] = l;
+    const int j0 = threadIdx.x;
+    if (j0 < kGatherTiles && s_go[j0] && (j0 == 0 || s_rep[j0 - 1] != s_rep[j0])) {
+        // thread j0 starts a run: its tile and the following tiles of the same
+        // replica, their warps' pairs added in order to compensated sums
+        FF f1, f2;
+        float m = 0.f;
+        for (int j = j0; j < kGatherTiles && s_rep[j] == s_rep[j0]; ++j)
+            for (int w = 2 * j; w < 2 * j + 2; ++w) {
+                f1.add(sh[w][0]);
+                f1.add(sh[w][1]);
+                f2.add(sh[w][2]);
+                f2.add(sh[w][3]);
+                m = fmaxf(m, sh[w][4]);
+            }
+        float* p = reinterpret_cast<float*>(n.part_fil + 4 * (size_t)(t0 + j0));
+        *reinterpret_cast<float4*>(p) = make_float4(m, f1.h, f1.l, f2.h);
+        p[4] = f2.l;
     }
 }
 
@@ -739,8 +747,8 @@ __global__ void __launch_bounds__(kBlock, 4) k_fil_energy_bulk(DevNet<float> n, 
                         else eb.add(tb);
                     }
                     if (n.terms && !ch) {
-                        n.terms[b] = (double)ts;
-                        n.terms[(size_t)n.nb + b] = (double)tb;
+                        n.terms[b] = ts;
+                        n.terms[(size_t)n.nb + b] = tb;
                     }
                 }
             }

@@ -387,7 +387,8 @@ __global__ void k_load_forces(const Real* X, LoadForceArgs a) {
 // Per-cylinder view of the per-bead filament energy terms the energy kernels
 // stored (stretching of cylinder c, bending of the triple centred on its first
 // bead; zero for a filament's first cylinder).
-__global__ void k_terms_by_cylinder(const double* terms, int nb, const int* cyl_b1, int cyl_begin, int ncyl,
+template <typename Real>
+__global__ void k_terms_by_cylinder(const Real* terms, int nb, const int* cyl_b1, int cyl_begin, int ncyl,
                                     double* stretch, double* bend) {
     const int c = blockIdx.x * blockDim.x + threadIdx.x;
     if (c >= ncyl) return;
@@ -1595,24 +1596,27 @@ int32_t mech_energy_terms(MechContext* ctx, int32_t r, double* stretch, double* 
     if ((rc = push_states(ctx))) return rc;
     const ReplicaHost& h = ctx->reps[r];
     DeviceBuffer terms, out;
-    CU(terms.ensure(sizeof(double) * 2 * (size_t)ctx->nb));
+    const size_t rs = real_size(ctx);
+    CU(terms.ensure(rs * 2 * (size_t)ctx->nb));
     CU(out.ensure(sizeof(double) * 2 * (size_t)h.ncyl));
     cudaStream_t s = ctx->stream;
-    CU(cudaMemsetAsync(terms.p, 0, sizeof(double) * 2 * (size_t)ctx->nb, s));
+    CU(cudaMemsetAsync(terms.p, 0, rs * 2 * (size_t)ctx->nb, s));
     // the filament energy kernel of a plain evaluation, storing its terms
+    const unsigned nblk = (unsigned)((h.ncyl + 255) / 256);
+    double* o = out.as<double>();
     if (ctx->precision == MECH_PREC_FP64) {
         DevNet<double> n = make_devnet<double>(ctx);
         n.terms = terms.as<double>();
         launch_part<double>(n, 0, s);
+        k_terms_by_cylinder<<<nblk, 256, 0, s>>>(terms.as<double>(), ctx->nb, ctx->cyl_b1.as<int>(), h.cyl_begin,
+                                                h.ncyl, o, o + h.ncyl);
     } else {
         DevNet<float> n = make_devnet<float>(ctx);
-        n.terms = terms.as<double>();
+        n.terms = terms.as<float>();
         launch_part<float>(n, 0, s);
+        k_terms_by_cylinder<<<nblk, 256, 0, s>>>(terms.as<float>(), ctx->nb, ctx->cyl_b1.as<int>(), h.cyl_begin,
+                                                h.ncyl, o, o + h.ncyl);
     }
-    const unsigned nblk = (unsigned)((h.ncyl + 255) / 256);
-    double* o = out.as<double>();
-    k_terms_by_cylinder<<<nblk, 256, 0, s>>>(terms.as<double>(), ctx->nb, ctx->cyl_b1.as<int>(), h.cyl_begin, h.ncyl,
-                                            o, o + h.ncyl);
     CU(cudaGetLastError());
     CU(cudaMemcpyAsync(stretch, o, sizeof(double) * h.ncyl, cudaMemcpyDeviceToHost, s));
     CU(cudaMemcpyAsync(bend, o + h.ncyl, sizeof(double) * h.ncyl, cudaMemcpyDeviceToHost, s));

@@ -30,6 +30,7 @@
 namespace mech {
 
 constexpr int kFilTile = 256;     // beads per filament tile (one block)
+constexpr int kGatherTiles = 4;   // filament tiles per block of the force gather kernels
 constexpr int kSparseTile = 256;  // interactions per sparse tile (one block)
 constexpr int kFilBulkMaxTiles = 64;   // filament tiles per block of the bulk-staged mixed kernels
 constexpr int kExvolFallbackCap = 4096;
@@ -185,8 +186,10 @@ struct DevNet {
     // scheduled while their predecessor runs and wait for it (griddepcontrol)
     int pdl;
     // diagnostic (mech_energy_terms; null otherwise): the filament energy
-    // kernels also store each bead's stretching [b] and bending [nb + b] term
-    double* terms;
+    // kernels also store each bead's stretching [b] and bending [nb + b] term,
+    // in the engine's precision (a conversion to double in the mixed kernels
+    // would be scheduled whether or not the store happens)
+    Real* terms;
     // kernel timeline (builds with MECH_TRACE only; null otherwise):
     // [0] records written, [1] capacity, then (start ns, end ns, kernel << 32 | block) per block
     unsigned long long* trace;
@@ -197,6 +200,9 @@ enum TraceKernel : unsigned {
     TK_FIL_ENERGY = 1, TK_FIL_FORCE, TK_GATHER, TK_FIN_FORCE, TK_FIN_ENERGY, TK_FIL_ENERGY_BULK, TK_FIL_FORCE_BULK,
     TK_DIRECTION_MX, TK_BOND, TK_DIRECTION, TK_FIN_DIRECTION, TK_RESET, TK_RECOVER_MAXABS, TK_RECOVER_MOVE,
     TK_BACKUP, TK_EXVOL_FB_FORCE, TK_EXVOL, TK_EXVOL_EXT, TK_EXVOL_TAIL, TK_BODY_HEAD, TK_GATHER_MX,
+    // sections of the energy / force finalizers (thread 0's view): partial
+    // loads, block reduction, the CG step logic and the state store
+    TK_SEC_FE_LOAD, TK_SEC_FE_REDUCE, TK_SEC_FE_TAIL, TK_SEC_FF_LOAD, TK_SEC_FF_REDUCE, TK_SEC_FF_TAIL,
 };
 
 #if defined(__CUDACC__) && defined(MECH_TRACE)
@@ -214,21 +220,29 @@ struct TraceGuard {
     __device__ TraceGuard(unsigned long long* b, unsigned k) : buf(b), kid(k), t0(0) {
         if (buf && threadIdx.x == 0) t0 = now();
     }
-    __device__ ~TraceGuard() {
-        if (buf && threadIdx.x == 0) {
-            const unsigned long long t1 = now();
-            const unsigned long long i = atomicAdd(buf, 1ull);
-            if (i < buf[1]) {
-                buf[2 + 3 * i] = t0;
-                buf[3 + 3 * i] = t1;
-                buf[4 + 3 * i] = ((unsigned long long)kid << 32) | blockIdx.x;
-            }
+    __device__ static void record(unsigned long long* b, unsigned k, unsigned long long a, unsigned long long e) {
+        const unsigned long long i = atomicAdd(b, 1ull);
+        if (i < b[1]) {
+            b[2 + 3 * i] = a;
+            b[3 + 3 * i] = e;
+            b[4 + 3 * i] = ((unsigned long long)k << 32) | blockIdx.x;
         }
+    }
+    __device__ ~TraceGuard() {
+        if (buf && threadIdx.x == 0) record(buf, kid, t0, now());
     }
 };
 #define MECH_TRACE_KERNEL(n, kid) TraceGuard mech_trace_guard_((n).trace, (kid))
+// a section of a single-block kernel, as seen by thread 0: from stamp `t` to now
+#define MECH_TRACE_STAMP(t) const unsigned long long t = threadIdx.x == 0 ? TraceGuard::now() : 0ull
+#define MECH_TRACE_SECTION(n, kid, t)                                                  \
+    do {                                                                               \
+        if ((n).trace && threadIdx.x == 0) TraceGuard::record((n).trace, (kid), (t), TraceGuard::now()); \
+    } while (0)
 #else
 #define MECH_TRACE_KERNEL(n, kid) ((void)0)
+#define MECH_TRACE_STAMP(t) ((void)0)
+#define MECH_TRACE_SECTION(n, kid, t) ((void)0)
 #endif
 
 #ifdef __CUDACC__

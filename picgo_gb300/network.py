@@ -47,7 +47,7 @@ CONFIGS = {
     # rest length are the adjoint parameters.
     "c5": dict(n_filaments=2000, n_cyl_per_filament=30, box=None,
                n_linkers=5000, linker_k=(4.0, 12.0), linker_l0=(20.0, 40.0),
-               n_motors=0),
+               n_motors=0, linker_tension=True),
 }
 
 CYLINDER_SIZE = 108.0          # nm, full actin cylinder
@@ -285,14 +285,30 @@ def make_network(config: str | dict = "c1", seed: int | None = None, *, n_filame
         pos = rng.uniform(0.0, 1.0, size=(n, 2))
         kk = (rng.uniform(kval[0], kval[1], size=n) if isinstance(kval, tuple)
               else np.full(n, float(kval)))
+        c1a, c1b = coord[b1[cyl[:, 0]]], coord[b2[cyl[:, 0]]]
+        c2a, c2b = coord[b1[cyl[:, 1]]], coord[b2[cyl[:, 1]]]
+
+        def attach_dist(ps):
+            p1 = c1a * (1 - ps[:, :1]) + ps[:, :1] * c1b
+            p2 = c2a * (1 - ps[:, 1:]) + ps[:, 1:] * c2b
+            return np.sqrt(np.sum((p2 - p1) ** 2, axis=1))
+
         if l0spec is None:   # rest length = distance at creation
-            c1a, c1b = coord[b1[cyl[:, 0]]], coord[b2[cyl[:, 0]]]
-            c2a, c2b = coord[b1[cyl[:, 1]]], coord[b2[cyl[:, 1]]]
-            p1 = c1a * (1 - pos[:, :1]) + pos[:, :1] * c1b
-            p2 = c2a * (1 - pos[:, 1:]) + pos[:, 1:] * c2b
-            ll = np.sqrt(np.sum((p2 - p1) ** 2, axis=1))
+            ll = attach_dist(pos)
         else:
             ll = rng.uniform(l0spec[0], l0spec[1], size=n)
+            if kind == "linker" and cfg.get("linker_tension"):
+                # attachment points redrawn until the linker starts stretched
+                # (distance >= rest length); a compressed harmonic linker
+                # has negative transverse stiffness and makes the energy
+                # non-convex where it sits.  Linkers still compressed after
+                # 64 draws start at rest (rest length = distance).
+                for _ in range(64):
+                    bad = attach_dist(pos) < ll
+                    if not bad.any():
+                        break
+                    pos[bad] = rng.uniform(0.0, 1.0, size=(int(bad.sum()), 2))
+                ll = np.minimum(ll, attach_dist(pos))
         return cyl, pos, kk, ll, n_cand
 
     lk_cyl, lk_pos, lk_k, lk_l0, lk_cand = bonds(int(cfg["n_linkers"]), cfg.get("linker_k", 8.0),

@@ -78,3 +78,18 @@ def test_ensemble_sizes_stay_in_their_ranges():
         assert 10 <= net.n_filaments <= 60
         assert np.all((counts >= 5) & (counts <= 9))
         assert np.all((net.coord > 0) & (net.coord < net.box))
+
+
+def test_c5_linkers_start_stretched_with_rest_lengths_in_range():
+    """The adjoint workload's linkers: k ~ U(4, 12), rest length ~ U(20, 40) nm,
+    attached where the attachment points are at least the rest length apart."""
+    net = make_network("c5", seed=20261208)
+    x = net.coord
+    p1 = x[net.cyl_b1[net.lk_cyl[:, 0]]] * (1 - net.lk_pos[:, :1]) + net.lk_pos[:, :1] * x[net.cyl_b2[net.lk_cyl[:, 0]]]
+    p2 = x[net.cyl_b1[net.lk_cyl[:, 1]]] * (1 - net.lk_pos[:, 1:]) + net.lk_pos[:, 1:] * x[net.cyl_b2[net.lk_cyl[:, 1]]]
+    d = np.sqrt(((p2 - p1) ** 2).sum(1))
+    assert len(d) == 5000
+    assert np.all(d >= net.lk_l0 - 1e-9)
+    assert net.lk_l0.min() >= 0.0 and net.lk_l0.max() <= 40.0
+    assert np.mean((net.lk_l0 >= 20.0) & (net.lk_l0 <= 40.0)) > 0.99
+    assert net.lk_k.min() >= 4.0 and net.lk_k.max() <= 12.0
