@@ -156,6 +156,8 @@ def run_ours(args, rank, world, dist):
 
     eng = Engine(args.precision, local)
     eng.set_network(net)
+    if args.graph_mode != "unrolled":
+        eng.set_graph_mode(args.graph_mode)
     tuning = eng.autotune()   # launch geometry and bin edge, outside the timed region
 
     def step():
@@ -256,6 +258,7 @@ def run_ours(args, rank, world, dist):
                    "seed": SEED, "precision": args.precision, "cg": "Polak-Ribiere, backtracking, gradTol 1 pN, "
                    "maxDist 1, lambdaMax 0.01, energyRelTol 0 (run to 1 pN)",
                    "l2": "flushed (256 MB write) between timed steps", "parallelism": f"replicas x{world}",
+                   "graph_mode": args.graph_mode,
                    "tuning": {k: (round(v, 4) if isinstance(v, float) else v) for k, v in tuning.items()}},
         "time_to_1pN_s": round(ms_per_step / 1e3, 4),
         "cg_iterations": results[-1]["num_iter"], "force_calls_per_step": results[-1]["num_force_call"],
@@ -671,6 +674,8 @@ def main():
     ap.add_argument("--precision", choices=["mixed", "fp64"], default="mixed")
     ap.add_argument("--cpu-seconds", type=float, default=20.0)
     ap.add_argument("--no-fp64", action="store_true")
+    ap.add_argument("--graph-mode", default="unrolled", choices=["unrolled", "unrolled_pdl", "unrolled_coop", "conditional"],
+                    help="how the minimizer drives the device (the mixed run; the FP64 comparison keeps the default)")
     ap.add_argument("--cpu-full", action="store_true",
                     help="also run the oracle's CG to 1 pN unbounded: the 200 x 20 network serially and on all host "
                          "threads, and this workload on all host threads (minutes)")

@@ -269,6 +269,14 @@ int32_t mech_get_forces(MechContext* ctx, int32_t replica, double* f_out);
  * kernels around each single-block reduction are scheduled while their
  * predecessor runs and wait for it on the device (same results) */
 #define MECH_GRAPH_UNROLLED_PDL 2
+/* the unrolled graph with each iteration's tail after the force lanes (force
+ * gather, force reduction, direction update, its reduction, reset) run as one
+ * cooperative launch whose blocks meet at grid barriers instead of five
+ * launches (mixed contexts with one replica; other contexts use
+ * MECH_GRAPH_UNROLLED).  Same work units, partial slots and reduction order:
+ * bitwise the same results.  A grid barrier that waits too long ends the
+ * minimization with MECH_ERR_ITER_LIMIT. */
+#define MECH_GRAPH_UNROLLED_COOP 3
 int32_t mech_set_graph_mode(MechContext* ctx, int32_t mode);
 
 /*

@@ -250,8 +250,11 @@ __device__ __forceinline__ void force_step(CGState& S, double mx, double ff, dou
     }
 }
 
+// `store`: write the state back (k_tail_coop runs this in every block on the
+// block's own copy and stores it from one block).
 template <typename Real>
-__device__ void finalize_force(const DevNet<Real>& n, int r, const RepTiles& rt, CGState& S, double* sh) {
+__device__ void finalize_force(const DevNet<Real>& n, int r, const RepTiles& rt, CGState& S, double* sh,
+                               bool store = true) {
     // k_force_gather writes one slot per tile, k_force_gather_mx one per run of
     // a replica's tiles in a block
     const int stride = sizeof(Real) == 4 ? kGatherTiles : 1;
@@ -303,14 +306,15 @@ __device__ void finalize_force(const DevNet<Real>& n, int r, const RepTiles& rt,
     }
     MECH_TRACE_STAMP(ts_tail);
     force_step(S, mx, ff, ffp);
-    n.st[r] = S;
+    if (store) n.st[r] = S;
     MECH_TRACE_SECTION(n, TK_SEC_FF_TAIL, ts_tail);
 }
 
 // One block per replica after the direction update: the slope d.F, the
 // conjugacy test and the next iteration's start (CGMethod.hpp:1553-1560).
 template <typename Real>
-__device__ void finalize_direction(const DevNet<Real>& n, int r, const RepTiles& rt, CGState& S, double* sh) {
+__device__ void finalize_direction(const DevNet<Real>& n, int r, const RepTiles& rt, CGState& S, double* sh,
+                                   bool store = true) {
     double slope;
     if constexpr (sizeof(Real) == 8) {
         slope = sum_slots(n.part_fil, 4, 3, rt.fil_begin, rt.fil_end, sh);
@@ -335,7 +339,7 @@ __device__ void finalize_direction(const DevNet<Real>& n, int r, const RepTiles&
             if (S.method >= 1) S.lastFdotF = S.newGrad;
             begin_iteration(S);
         }
-        n.st[r] = S;
+        if (store) n.st[r] = S;
     }
 }
 

@@ -358,13 +358,20 @@ __global__ void __launch_bounds__(kBlock) k_force_gather(DevNet<Real> n, int wan
 // warp order, the warps of each run of its tiles that belong to one replica,
 // into the slot of the run's first tile (run_slot with stride kGatherTiles),
 // so the force finalizer reads a quarter of the slots one per tile would take.
-__global__ void __launch_bounds__(kBlock) k_force_gather_mx(DevNet<float> n, int want) {
-    pdl_trigger();   // the next kernel of the main lane may be scheduled now
-    MECH_TRACE_KERNEL(n, TK_GATHER_MX);
+struct GatherMxShared {
+    float sh[8][5];   // per warp: F.F (hi, lo), F.Fprev (hi, lo), max
+    int go[kGatherTiles], fb[kGatherTiles], rep[kGatherTiles];
+};
+
+// One gather unit (kGatherTiles consecutive tiles): the body of a
+// k_force_gather_mx block, also run unit after unit by k_tail_coop.
+__device__ void gather_mx_unit(const DevNet<float>& n, int want, int unit, GatherMxShared& g) {
     static_assert(kFilTile == 256 && kBlock == 64 * kGatherTiles, "64 threads x 4 beads per tile");
-    __shared__ float sh[8][5];   // per warp: F.F (hi, lo), F.Fprev (hi, lo), max
-    __shared__ int s_go[kGatherTiles], s_fb[kGatherTiles], s_rep[kGatherTiles];
-    const int t0 = blockIdx.x * kGatherTiles;
+    float (&sh)[8][5] = g.sh;
+    int* s_go = g.go;
+    int* s_fb = g.fb;
+    int* s_rep = g.rep;
+    const int t0 = unit * kGatherTiles;
     if (threadIdx.x < kGatherTiles) {
         const int ti = t0 + threadIdx.x;
         int go = 0, fb = 0, rep = -1;
@@ -463,6 +470,13 @@ __global__ void __launch_bounds__(kBlock) k_force_gather_mx(DevNet<float> n, int
         *reinterpret_cast<float4*>(p) = make_float4(m, f1.h, f1.l, f2.h);
         p[4] = f2.l;
     }
+}
+
+__global__ void __launch_bounds__(kBlock) k_force_gather_mx(DevNet<float> n, int want) {
+    pdl_trigger();   // the next kernel of the main lane may be scheduled now
+    MECH_TRACE_KERNEL(n, TK_GATHER_MX);
+    __shared__ GatherMxShared g;
+    gather_mx_unit(n, want, blockIdx.x, g);
 }
 
 // One block per replica: max |F|, the dots and the CG step logic after the gather.
@@ -948,13 +962,18 @@ __global__ void __launch_bounds__(kBlock) k_fil_force_bulk(DevNet<float> n, int 
             mbar_wait_bounded(&bar[q % kBulkStages], (unsigned)((q / kBulkStages) & 1), kBulkWaitLimit);
 }
 
-// Mixed engine: persistent direction update d = F + beta d with the d.F partials.
-__global__ void __launch_bounds__(kBlock) k_direction_mx(DevNet<float> n) {
-    pdl_wait();      // the previous kernel of the main lane has finished
-    pdl_trigger();   // the next kernel of the main lane may be scheduled now
-    MECH_TRACE_KERNEL(n, TK_DIRECTION_MX);
-    __shared__ double sh[32];
-    const int t0 = blockIdx.x * n.ptiles[2], t1 = min(t0 + n.ptiles[2], n.n_ftiles);
+// What the direction update needs of a replica's state.
+struct DirState {
+    int go, fb, xb, bk;
+    float beta;
+};
+
+// One direction unit (n.ptiles[2] consecutive tiles): the body of a
+// k_direction_mx block, also run unit after unit by k_tail_coop, which passes
+// the state its blocks hold instead of the one in memory.
+template <typename StateOf>
+__device__ void direction_mx_unit(const DevNet<float>& n, int unit, double* sh, StateOf state_of) {
+    const int t0 = unit * n.ptiles[2], t1 = min(t0 + n.ptiles[2], n.n_ftiles);
     int cur = -1, first = 0, cnt = 0, fb = 0, xb = 0, bk = 0;
     bool go = false;
     float beta = 0.f;
@@ -973,12 +992,12 @@ __global__ void __launch_bounds__(kBlock) k_direction_mx(DevNet<float> n) {
             first = ti;
             cnt = 0;
             dF = FF();
-            const CGState& S = n.st[cur];
-            go = S.phase == PH_DIR;
-            fb = S.fbuf;
-            xb = S.xbuf;
-            bk = S.backupPending;
-            beta = (float)S.beta;
+            const DirState ds = state_of(cur);
+            go = ds.go;
+            fb = ds.fb;
+            xb = ds.xb;
+            bk = ds.bk;
+            beta = ds.beta;
         }
         if (!go) continue;
         ++cnt;
@@ -995,6 +1014,159 @@ __global__ void __launch_bounds__(kBlock) k_direction_mx(DevNet<float> n) {
         }
     }
     if (cnt) finish(cur);
+}
+
+// Mixed engine: persistent direction update d = F + beta d with the d.F partials.
+__global__ void __launch_bounds__(kBlock) k_direction_mx(DevNet<float> n) {
+    pdl_wait();      // the previous kernel of the main lane has finished
+    pdl_trigger();   // the next kernel of the main lane may be scheduled now
+    MECH_TRACE_KERNEL(n, TK_DIRECTION_MX);
+    __shared__ double sh[32];
+    direction_mx_unit(n, blockIdx.x, sh, [&](int r) {
+        const CGState& S = n.st[r];
+        return DirState{S.phase == PH_DIR, S.fbuf, S.xbuf, S.backupPending, (float)S.beta};
+    });
+}
+
+// ---------------------------------------------------------------------------
+// Mixed engine, one replica: the tail of an iteration after the force lanes
+// as one cooperatively launched grid (every block resident at once): the
+// force gather, the force finalizer, the direction update, the direction
+// finalizer and the reset, with grid barriers where the separate launches
+// had a launch boundary.  The finalizers' reductions run in every block over
+// the same partial slots in the same order, so every block holds the same new
+// state, and block 0 stores it.  Work units, partial slots and reduction
+// order are those of k_force_gather_mx, k_finalize_force, k_direction_mx,
+// k_finalize_direction and k_reset, so the minimization is bitwise the one
+// the separate launches give.
+// ---------------------------------------------------------------------------
+constexpr unsigned kGridWaitLimit = 1u << 22;   // polls before a grid barrier counts as lost
+
+// Barrier over the blocks of a co-resident grid: gbar[0] counts arrivals,
+// gbar[1] is the generation that the last arrival advances.  A wait gives up
+// after kGridWaitLimit polls, sets error bit 64 and returns false in every
+// thread of its block.
+__device__ bool grid_sync(unsigned* gbar, unsigned* err) {
+    __shared__ int s_ok;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        volatile unsigned* gen = gbar + 1;
+        const unsigned g0 = *gen;
+        __threadfence();
+        const unsigned arrived = atomicAdd(gbar, 1u);
+        int ok = 1;
+        if (arrived == gridDim.x - 1) {
+            atomicExch(gbar, 0u);
+            __threadfence();
+            atomicAdd(gbar + 1, 1u);
+        } else {
+            unsigned polls = 0;
+            while (*gen == g0) {
+                if (++polls > kGridWaitLimit) {
+                    atomicOr(err, 64u);
+                    ok = 0;
+                    break;
+                }
+                __nanosleep(64);
+            }
+        }
+        __threadfence();
+        s_ok = ok;
+    }
+    __syncthreads();
+    return s_ok != 0;
+}
+
+__global__ void __launch_bounds__(kBlock) k_tail_coop(DevNet<float> n) {
+    MECH_TRACE_KERNEL(n, TK_TAIL_COOP);
+    __shared__ GatherMxShared g;
+    __shared__ double sh[32 * 3];
+    __shared__ int s_phase, s_fb, s_xb, s_bk;
+    __shared__ float s_beta;
+    __shared__ CGState S;   // the block's copy of the replica's state (thread 0 works on it)
+    if (threadIdx.x == 0) {
+        S = n.st[0];
+        s_phase = S.phase;
+        s_fb = S.fbuf;
+        if (blockIdx.x == 0) {   // as after every force evaluation: the exvol work lists restart empty
+            if (n.ev_list_count) *n.ev_list_count = 0;
+            if (n.ev_fb_count) *n.ev_fb_count = 0;
+        }
+    }
+    __syncthreads();
+    const int start = s_phase;
+    if (start != PH_FORCE && start != PH_RESET) return;   // the same decision in every block
+    const RepTiles rt = n.rt[0];
+    int phase = start;
+    if (phase == PH_FORCE) {
+        const int units = (n.n_ftiles + kGatherTiles - 1) / kGatherTiles;
+        for (int u = blockIdx.x; u < units; u += gridDim.x) {
+            gather_mx_unit(n, PH_FORCE, u, g);
+            __syncthreads();
+        }
+        if (!grid_sync(n.gbar, n.err)) return;
+        finalize_force(n, 0, rt, S, sh, false);
+        if (threadIdx.x == 0) {
+            s_phase = S.phase;
+            s_fb = S.fbuf;
+            s_xb = S.xbuf;
+            s_bk = S.backupPending;
+            s_beta = (float)S.beta;
+        }
+        __syncthreads();
+        phase = s_phase;
+        if (phase == PH_DIR) {
+            const DirState ds{1, s_fb, s_xb, s_bk, s_beta};
+            for (int u = blockIdx.x; u < n.pgrid[2]; u += gridDim.x) {
+                direction_mx_unit(n, u, sh, [&](int) { return ds; });
+                __syncthreads();
+            }
+            if (!grid_sync(n.gbar, n.err)) return;
+            finalize_direction(n, 0, rt, S, sh, false);
+            if (threadIdx.x == 0) {
+                s_phase = S.phase;
+                s_fb = S.fbuf;
+            }
+            __syncthreads();
+            phase = s_phase;
+        }
+    }
+    if (phase == PH_RESET) {   // d = F, then the new slope and the next iteration's start
+        const float* F = n.f[s_fb];
+        const size_t nv = 3 * (size_t)n.nb;
+        for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < nv; i += (size_t)gridDim.x * blockDim.x)
+            n.d[i] = F[i];
+        if (threadIdx.x == 0) {
+            S.slope = S.FdotF;
+            S.lastFdotF = S.FdotF;
+            begin_iteration(S);
+        }
+        // every block has read the state before block 0 replaces it (on the
+        // force path the barriers above already ensure that)
+        if (start == PH_RESET && !grid_sync(n.gbar, n.err)) return;
+    }
+    if (blockIdx.x == 0 && threadIdx.x == 0) n.st[0] = S;
+}
+
+int coop_tail_grid(int device) {
+    int sms = 0, per_sm = 0;
+    if (cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, device) != cudaSuccess) return 0;
+    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_tail_coop, kBlock, 0) != cudaSuccess) return 0;
+    return sms * per_sm;
+}
+
+static void launch_tail_coop(const DevNet<float>& n, int grid, cudaStream_t s) {
+    cudaLaunchConfig_t cfg = {};
+    cfg.gridDim = dim3((unsigned)grid);
+    cfg.blockDim = dim3(kBlock);
+    cfg.dynamicSmemBytes = 0;
+    cfg.stream = s;
+    cudaLaunchAttribute at[1];
+    at[0].id = cudaLaunchAttributeCooperative;
+    at[0].val.cooperative = 1;
+    cfg.attrs = at;
+    cfg.numAttrs = 1;
+    cudaLaunchKernelEx(&cfg, k_tail_coop, n);
 }
 
 // ---------------------------------------------------------------------------
@@ -1346,7 +1518,7 @@ int launch_energy(const DevNet<Real>& n, int want, int trial, const Lanes& L) {
 }
 
 template <typename Real>
-int launch_forces(const DevNet<Real>& n, int want, const Lanes& L) {
+int launch_forces(const DevNet<Real>& n, int want, const Lanes& L, int coop_grid) {
     int ev_t = 0, bb_t = 0;
     const int lm = n_lm_tiles(n, &ev_t, &bb_t);
     int launched = 0;
@@ -1368,6 +1540,12 @@ int launch_forces(const DevNet<Real>& n, int want, const Lanes& L) {
     if (!n.fil_first[1]) fil();
     cudaStreamWaitEvent(L.main, L.join, 0);
     cudaStreamWaitEvent(L.main, L.join2, 0);
+    if constexpr (sizeof(Real) == 4) {
+        if (coop_grid > 0) {
+            launch_tail_coop(n, coop_grid, L.main);
+            return launched + 2;
+        }
+    }
     if constexpr (sizeof(Real) == 4) k_force_gather_mx<<<(n.n_ftiles + kGatherTiles - 1) / kGatherTiles, kBlock, 0, L.main>>>(n, want);
     else k_force_gather<Real><<<(n.n_ftiles + kGatherTiles - 1) / kGatherTiles, kBlock, 0, L.main>>>(n, want);
     launch_k(n.pdl, k_finalize_force<Real>, n.R, kBlock, L.main, n, want);
@@ -1470,7 +1648,7 @@ int persistent_blocks(int device, int which, int per_sm) {
 #define MECH_INSTANTIATE(R)                                                             \
     template int launch_part<R>(const DevNet<R>&, int, cudaStream_t);                   \
     template int launch_energy<R>(const DevNet<R>&, int, int, const Lanes&);            \
-    template int launch_forces<R>(const DevNet<R>&, int, const Lanes&);                 \
+    template int launch_forces<R>(const DevNet<R>&, int, const Lanes&, int);            \
     template int launch_direction<R>(const DevNet<R>&, cudaStream_t);                   \
     template int launch_reset<R>(const DevNet<R>&, cudaStream_t);                       \
     template int launch_body_head<R>(const DevNet<R>&, cudaStream_t);                   \

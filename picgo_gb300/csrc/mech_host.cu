@@ -96,6 +96,7 @@ struct MechContext {
     DeviceBuffer perm_all, stage;   // caller -> internal bead map of all replicas; coordinate staging
     // Hessian-vector products, adjoint and Newton solves (FP64 engine)
     DeviceBuffer hv_a, hv_b, cg_x, cg_r, cg_p, cg_Ap, cg_scal, cg_part, cg_ticket;
+    DeviceBuffer gbar;   // grid barrier of the cooperative iteration tail (2 unsigned)
     int n_ftiles = 0, n_stiles = 0;
     int sp_tiles[K_NUM_SPARSE] = {0, 0, 0, 0};
     // host copies of the full tile lists, and the compacted view that a
@@ -953,6 +954,7 @@ static int pull_states(MechContext* c) {
 }
 // Status of the device error word's bits (kernels set them with atomicOr).
 static int err_status(unsigned bits) {
+    if (bits & 64u) return set_err(MECH_ERR_ITER_LIMIT, "a grid barrier of the cooperative iteration tail timed out");
     if (bits & 32u) return set_err(MECH_ERR_ITER_LIMIT, "a bulk shared-memory copy did not complete in time");
     if (bits & 16u) return set_err(MECH_ERR_CUDA, "a bulk shared-memory copy range was misaligned");
     if (bits & 1u) return set_err(MECH_ERR_NONFINITE, "excluded-volume numeric fallback failed");
@@ -1004,11 +1006,24 @@ template <typename Real>
 static int capture_iteration_graph(MechContext* c, cudaGraphExec_t* exec, int* nlaunch) {
     DevNet<Real> n = make_devnet<Real>(c);
     n.pdl = c->graph_mode == MECH_GRAPH_UNROLLED_PDL ? 1 : 0;
+    // the cooperative tail: mixed engine, one replica (its blocks reduce for replica 0)
+    int coop_grid = 0;
+    if (c->graph_mode == MECH_GRAPH_UNROLLED_COOP && sizeof(Real) == 4 && c->R == 1) {
+        coop_grid = coop_tail_grid(c->device);
+        if (coop_grid <= 0) return set_err(MECH_ERR_CUDA, "cooperative tail: no resident blocks");
+        CU(c->gbar.ensure(2 * sizeof(unsigned)));
+        CU(cudaMemsetAsync(c->gbar.p, 0, 2 * sizeof(unsigned), c->stream));
+        n.gbar = c->gbar.as<unsigned>();
+    }
     cudaGraph_t g = nullptr;
     CU(cudaStreamBeginCapture(c->stream, cudaStreamCaptureModeThreadLocal));
     int k = 0;
     for (int b = 0; b < kBlocksPerGraph; ++b) {
         k += trial_launches<Real>(n, c->lanes());
+        if (coop_grid > 0) {
+            k += launch_forces<Real>(n, PH_FORCE, c->lanes(), coop_grid);
+            continue;
+        }
         k += launch_forces<Real>(n, PH_FORCE, c->lanes());
         k += launch_direction<Real>(n, c->stream);
         k += launch_reset<Real>(n, c->stream);
@@ -1702,7 +1717,8 @@ int32_t mech_get_stretch_forces(MechContext* ctx, int32_t r, double* linker_f, d
 
 int32_t mech_set_graph_mode(MechContext* ctx, int32_t mode) {
     if (!ctx) return set_err(MECH_ERR_ARG, "null context");
-    if (mode != MECH_GRAPH_CONDITIONAL && mode != MECH_GRAPH_UNROLLED && mode != MECH_GRAPH_UNROLLED_PDL)
+    if (mode != MECH_GRAPH_CONDITIONAL && mode != MECH_GRAPH_UNROLLED && mode != MECH_GRAPH_UNROLLED_PDL &&
+        mode != MECH_GRAPH_UNROLLED_COOP)
         return set_err(MECH_ERR_ARG, "bad graph mode");
     ctx->graph_mode = mode;
     return MECH_OK;

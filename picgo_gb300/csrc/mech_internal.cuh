@@ -190,6 +190,8 @@ struct DevNet {
     // in the engine's precision (a conversion to double in the mixed kernels
     // would be scheduled whether or not the store happens)
     Real* terms;
+    // grid barrier of the cooperative iteration tail: [0] arrivals, [1] generation
+    unsigned* gbar;
     // kernel timeline (builds with MECH_TRACE only; null otherwise):
     // [0] records written, [1] capacity, then (start ns, end ns, kernel << 32 | block) per block
     unsigned long long* trace;
@@ -203,6 +205,7 @@ enum TraceKernel : unsigned {
     // sections of the energy / force finalizers (thread 0's view): partial
     // loads, block reduction, the CG step logic and the state store
     TK_SEC_FE_LOAD, TK_SEC_FE_REDUCE, TK_SEC_FE_TAIL, TK_SEC_FF_LOAD, TK_SEC_FF_REDUCE, TK_SEC_FF_TAIL,
+    TK_TAIL_COOP,
 };
 
 #if defined(__CUDACC__) && defined(MECH_TRACE)
@@ -297,7 +300,13 @@ struct Lanes {
     cudaEvent_t fork, join, join2;
 };
 template <typename Real> int launch_energy(const DevNet<Real>& n, int want, int trial, const Lanes& L);
-template <typename Real> int launch_forces(const DevNet<Real>& n, int want, const Lanes& L);
+// coop_grid > 0 (mixed engine, one replica): the gather, both finalizers, the
+// direction update and the reset run as one cooperative launch of that many
+// blocks (k_tail_coop) instead of launch_forces' gather and finalizer plus
+// launch_direction and launch_reset
+template <typename Real> int launch_forces(const DevNet<Real>& n, int want, const Lanes& L, int coop_grid = 0);
+// blocks of the cooperative iteration tail on `device` (all resident at once)
+int coop_tail_grid(int device);
 template <typename Real> int launch_direction(const DevNet<Real>& n, cudaStream_t s);
 template <typename Real> int launch_reset(const DevNet<Real>& n, cudaStream_t s);
 // head of a body of the minimizer's conditional graph: sets the phase

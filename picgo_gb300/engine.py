@@ -214,8 +214,11 @@ class Engine:
     def set_graph_mode(self, mode: str) -> None:
         """'unrolled' (default): relaunched graphs of 8 unrolled iteration blocks;
         'unrolled_pdl': the same with programmatic dependent launch around the reductions;
-        'conditional': one graph whose device while loop runs only the phases in use.  Same results."""
-        check(self._L.mech_set_graph_mode(self._ctx, {"conditional": 0, "unrolled": 1, "unrolled_pdl": 2}[mode]))
+        'conditional': one graph whose device while loop runs only the phases in use;
+        'unrolled_coop': the unrolled graph with each iteration's tail (gather, reductions, direction, reset) as one
+        cooperative launch (mixed, one replica; otherwise as 'unrolled').  Same results."""
+        check(self._L.mech_set_graph_mode(self._ctx, {"conditional": 0, "unrolled": 1, "unrolled_pdl": 2,
+                                                     "unrolled_coop": 3}[mode]))
 
     # -- second order (FP64 contexts) -----------------------------------------
     def hvp(self, v: np.ndarray, replica: int = 0, jacobian: bool = False) -> np.ndarray:

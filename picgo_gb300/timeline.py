@@ -28,7 +28,7 @@ NAMES = {
     13: "recover_maxabs", 14: "recover_move", 15: "backup", 16: "exvol_fb_force", 17: "exvol", 18: "exvol_ext",
     19: "exvol_tail", 20: "body_head", 21: "gather_mx",
     22: "fin_energy: loads", 23: "fin_energy: reduce", 24: "fin_energy: step", 25: "fin_force: loads",
-    26: "fin_force: reduce", 27: "fin_force: step",
+    26: "fin_force: reduce", 27: "fin_force: step", 28: "tail_coop",
 }
 SECTIONS = set(range(22, 28))
 
